@@ -1,0 +1,359 @@
+"""Benchmark of the accelerated PT diffusion solver (T_eff, the reference's metric).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload 2d_nonlin_4096]
+                    [--precision fp64|fp32_dc] [--impl ours|reference]
+
+Workload (default): 2D nonlinear diffusion D = H^3 on 4096^2 cells, 10x10
+domain, H0 = 1 + exp(-r^2), H = 1 on the boundary, dt = 0.2, tol = 1e-8,
+residual check every nchk = 100 iterations, FP64.  One bench *step* is one
+implicit physical time step: the PT iteration driven to err <= tol.
+
+Metric: T_eff = A_eff * iterations / time, with A_eff = (2*3+2)*nx*ny*8 bytes
+per PT iteration in 2D and (2*4+2)*nx*ny*nz*8 in 3D -- the reference's own
+effective-throughput definition (scripts/diff_2D_nonlin_perf.jl:107,
+scripts/diff_3D/diff_3D_nonlin_perf.jl:114), in GB/s (1e9 bytes).
+
+* ``value``: device-resident state, timed with CUDA events on the library's
+  stream around K physical steps (after W untimed ones), every check and the
+  stopping decision included.  The working set (7 arrays of 134 MB) is larger
+  than L2, so no flush is needed.
+* ``e2e``: the same metric through the C ABI call a driver makes,
+  ``ptd_solve`` on pinned host buffers (H0 uploaded, one physical step solved,
+  H downloaded) per step, wall clock.
+* ``roofline``: the fused PT kernel alone (fixed iterations, the reference's
+  perf protocol, scripts/diff_3D/diff_3D_nonlin_perf.jl:97-105), A_eff per
+  launch over the mean launch time, against the measured HBM copy bandwidth.
+* ``cpu_baseline`` / ``--impl reference``: the CPU restatement of the
+  reference (oracle/, OpenMP on all host cores; the reference's own Julia
+  Threads backend cannot run here: no Julia) on a bounded sample of the same
+  workload: a fixed number of PT iterations, timed, as T_eff.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "pseudotransientdiffusion.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+# Published T_eff of the reference for the same metric and size (A100 SXM4,
+# output/out_diff_2D_nonlin_perf_ampere.txt:40; 3D: out_diff_3D_nonlin_perf_ampere.txt:24).
+PUBLISHED = {"2d_nonlin_4096": 805.77, "3d_nonlin_512": 927.66}
+
+
+def a_eff_bytes(shape) -> float:
+    n = 1
+    for v in shape:
+        n *= v
+    arrays = {1: 2 * 2 + 2, 2: 2 * 3 + 2, 3: 2 * 4 + 2}[len(shape)]
+    return float(arrays * n * 8)
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(workload: str):
+    """dram bytes per launch of the dominant kernel, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"pt_kernel_{workload}.md")
+    try:
+        with open(path) as fh:
+            for ln in fh:
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    return float(ln.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(gpu_index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in out.splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def reduce_max(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(script, shape, budget_s=15.0):
+    """Time the oracle's fixed-iteration loop on all host cores (bounded sample)."""
+    from oracle import oracle as O
+
+    nth = os.cpu_count() or 1
+    H0 = __import__("ptdiff").initial_condition(script, *shape)
+    H = np.array(H0, order="F")
+    q = [np.zeros_like(H) for _ in range(3)]
+    t0 = time.perf_counter()
+    O.iterate(script, H, H0, q, 2, nthreads=nth)
+    t_probe = (time.perf_counter() - t0) / 2
+    n = int(max(2, min(2000, budget_s / max(t_probe, 1e-9))))
+    t0 = time.perf_counter()
+    O.iterate(script, H, H0, q, n, nthreads=nth)
+    dt = time.perf_counter() - t0
+    teff = a_eff_bytes(shape) * n / dt / 1e9
+    return {"value": round(teff, 3), "unit": "GB/s", "cores": nth, "kind": "port",
+            "sample": f"{n} fixed PT iterations (no checks) of the {len(shape)}D workload "
+                      f"{'x'.join(map(str, shape))}, {dt:.1f} s, CPU restatement of the reference "
+                      f"(OpenMP, {nth} threads); the reference's Julia Threads backend cannot run (no Julia)"}
+
+
+def run_reference(args, world, rank, pg):
+    import ptdiff
+
+    if rank != 0:
+        return 0
+    s = ptdiff.scripts.CONFIGS[args.workload]
+    shape = (s.default_n,) * s.ndim
+    cb = None
+    vals = []
+    for _ in range(args.warmup):
+        pass
+    budget = max(4.0, 60.0 / max(args.steps, 1))
+    for _ in range(args.steps):
+        cb = cpu_baseline(s, shape, budget_s=budget)
+        vals.append(cb["value"])
+    value = statistics.median(vals) if vals else 0.0
+    cb["value"] = value
+    line = {
+        "impl": "reference", "metric": "T_eff", "value": value, "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "shape": list(shape), "protocol": "fixed PT iterations"},
+        "cpu_baseline": cb,
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+
+    import ptdiff
+
+    s = ptdiff.scripts.CONFIGS[args.workload]
+    n = args.n or s.default_n
+    shape = (n,) * s.ndim
+    A = a_eff_bytes(shape)
+    torch.cuda.set_device(local)
+    H0 = ptdiff.initial_condition(s, *shape)
+    params = ptdiff.make_params(s, shape, nt=1, precision=args.precision)
+    sol = ptdiff.Solver(params)
+    ext = torch.cuda.ExternalStream(sol.stream)
+
+    # ---- device-resident value: W untimed physical steps, then K timed ones
+    sol.set_state(H0)
+    for _ in range(args.warmup):
+        sol.step(1)
+    sol.sync()
+    l0, i0 = sol.counters()
+    clocks = ClockSampler(local) if rank == 0 else None
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(ext)
+    step_iters = []
+    for _ in range(args.steps):
+        its, _ = sol.step(1)
+        step_iters.append(int(its[0]))
+    ev1.record(ext)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(pg)
+    clk = clocks.stop() if clocks else None
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    l1, i1 = sol.counters()
+    iters_timed = i1 - i0
+    t_max = reduce_max(pg, t_dev)
+    total_bytes = reduce_sum(pg, A * iters_timed)
+    value = total_bytes / t_max / 1e9
+
+    # ---- roofline: the fused kernel alone, fixed iterations (perf protocol)
+    nfix = args.fixed_iters
+    sol.iterate(8)
+    sol.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    sol.iterate(nfix)
+    e1.record(ext)
+    e1.synchronize()
+    t_launch = e0.elapsed_time(e1) / 1e3 / nfix
+    achieved = A / t_launch / 1e9
+    peak, peak_kind = read_peaks()
+    traffic = profile_traffic(args.workload)
+    sol.close()
+
+    # ---- e2e: ptd_solve on pinned host buffers, one physical step per call
+    pe = ptdiff.make_params(s, shape, nt=1, precision=args.precision)
+    sol2 = ptdiff.Solver(pe)
+    pin = torch.empty(H0.size, dtype=torch.float64, pin_memory=True)
+    Hh = pin.numpy()
+    for _ in range(args.warmup):
+        Hh[:] = np.ravel(H0, order="F")
+        sol2.solve(Hh)
+    barrier(pg)
+    e2e_time, e2e_iters = 0.0, 0
+    for _ in range(args.steps):
+        Hh[:] = np.ravel(H0, order="F")
+        t0 = time.perf_counter()
+        its, _, _ = sol2.solve(Hh)
+        e2e_time += time.perf_counter() - t0
+        e2e_iters += int(its.sum())
+    sol2.close()
+    e2e_t = reduce_max(pg, e2e_time)
+    e2e_val = reduce_sum(pg, A * e2e_iters) / e2e_t / 1e9
+
+    if rank != 0:
+        return 0
+    cb = cpu_baseline(s, shape, budget_s=args.cpu_budget) if world == 1 and not args.no_cpu else None
+    ws_gb = (7 if s.ndim == 2 else 9) * np.prod(shape) * 8 / 1e9
+    pub = PUBLISHED.get(args.workload) if args.precision == "fp64" else None
+    line = {
+        "metric": "T_eff", "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(t_max / max(args.steps, 1) * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": round(value / pub, 3) if pub else None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "shape": list(shape), "precision": args.precision,
+                   "nchk": s.nout, "tol": s.tol, "dt": s.dt, "step": "one physical time step to tol",
+                   "l2": f"inputs larger than L2 (working set {ws_gb:.2f} GB), no flush",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_kind": peak_kind, "kernel": f"pt{s.ndim}d_kernel (fused PT iteration)",
+                     "launch_us": round(t_launch * 1e6, 2), "algorithmic_bytes_per_launch": A},
+        "cpu_baseline": cb,
+        "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": int(H0.size * 8),
+                "d2h_bytes_per_step": int(H0.size * 8)},
+        "gpu_launches": int(l1 - l0),
+        "clocks": clk,
+        "pt_iterations_per_step": step_iters,
+        "time_to_tol_ms_per_step": round(t_max / max(args.steps, 1) * 1e3, 3),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="2d_nonlin_4096")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32_dc"])
+    ap.add_argument("--n", type=int, default=0, help="override the grid size (testing)")
+    ap.add_argument("--fixed-iters", type=int, default=200)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    world, rank, local, pg = dist_setup(args.gpus)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank, pg)
+        return run_ours(args, world, rank, local, pg)
+    finally:
+        if pg is not None:
+            pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

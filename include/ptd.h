@@ -1,0 +1,154 @@
+/*
+ * ptd.h -- C ABI of the GB300 (sm_103a) accelerated pseudo-transient (PT)
+ * diffusion library, libptd.so.
+ *
+ * Drop-in boundary.  The reference (PTsolvers/PseudoTransientDiffusion.jl) has
+ * no FFI of its own: its boundary is the script-level solver driver
+ * diffusion_{1,2,3}D_() (e.g. scripts/diff_2D_nonlin.jl:46-106), configured by
+ * NX/NY/NZ (scripts/diff_2D_nonlin.jl:6-7) and hard-coded physics/numerics,
+ * returning (xc[,yc,zc], H) (scripts/diff_2D_nonlin.jl:105,108-112) and
+ * printing the total PT iteration count (scripts/diff_2D_nonlin.jl:92).  The
+ * entry points below are what a host-language wrapper of that driver (a
+ * Julia `ccall`, Python `ctypes`) binds: the driver keeps its names and
+ * defaults, builds H0 (and D for the step model) exactly as the script does,
+ * and hands the PT solve to this library.
+ *
+ * Conventions
+ *  - Arrays are the reference's: Float64, nx*ny*nz cells including the frozen
+ *    boundary cells, x fastest (Julia column-major).  Pointers may be host
+ *    memory (pageable or pinned) or device memory of the current device; the
+ *    library detects which.
+ *  - Every function returns a ptd_status (0 = PTD_OK).  The library never
+ *    aborts the process; ptd_last_error() gives a one-line detail.
+ *  - Ownership: the caller owns H and D; a context owns its device buffers
+ *    (allocated by ptd_create, freed by ptd_destroy) and its CUDA stream.
+ *  - Threading: a context is used by one host thread at a time.
+ */
+#ifndef PTD_H
+#define PTD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTD_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define PTD_API __attribute__((visibility("default")))
+#else
+#define PTD_API
+#endif
+
+/* Status codes.  PTD_ENAN mirrors the reference's `if isnan(err) error("NaN")`
+ * after a physical step (scripts/diff_2D_nonlin.jl:90). */
+typedef enum ptd_status {
+    PTD_OK = 0,
+    PTD_EINVAL = 1,    /* invalid argument or parameter combination */
+    PTD_ENAN = 2,      /* the residual norm was NaN at the end of a physical step */
+    PTD_ENOTCONV = 3,  /* itmax reached without err <= tol (only with PTD_FLAG_STRICT) */
+    PTD_ECUDA = 4,     /* a CUDA runtime call failed */
+    PTD_ENOMEM = 5,    /* device or host allocation failed */
+    PTD_ESTATE = 6,    /* call out of order (e.g. stepping before a state was set) */
+    PTD_ETIMEOUT = 7   /* a device-side wait gave up (never expected) */
+} ptd_status;
+
+/* Diffusion models of the reference's solver scripts:
+ *  LIN      D = const                     scripts/diff_{1D,2D}_lin.jl, diff_3D_lin_multixpu.jl
+ *  LINSTEP  D = per-cell field (step)     scripts/diff_{1D,2D}_linstep.jl, diff_3D_linstep_multixpu.jl
+ *  NONLIN   D = H^3 (face: (avg H)^3)     scripts/diff_{1D,2D}_nonlin.jl, diff_3D_nonlin_multixpu.jl */
+enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2 };
+
+/* Arithmetic of the PT iterations.  FP64: every PT iteration in FP64 (the
+ * reference's form).  FP32_DC: FP32 PT iterations on a correction inside an
+ * FP64 defect-correction loop (residual, norm and H update in FP64). */
+enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1 };
+
+/* Residual used for the stopping test.  MIXED is the reference's: the
+ * undamped flux from the H the fluxes of that iteration were computed on, the
+ * time term from the updated H (scripts/diff_2D_nonlin.jl:157-158,167-170). */
+enum { PTD_RESID_MIXED = 0, PTD_RESID_CONSISTENT = 1 };
+
+/* Norm of the residual: RMS = norm(ResH)/sqrt(length(ResH)) (the reference,
+ * scripts/diff_2D_nonlin.jl:211), or MAX = max|R|. */
+enum { PTD_NORM_RMS = 0, PTD_NORM_MAX = 1 };
+
+/* Flags */
+#define PTD_FLAG_STRICT 0x1 /* return PTD_ENOTCONV when a step stops at itmax */
+
+typedef struct ptd_params {
+    int32_t ndim;        /* 1, 2, 3 */
+    int32_t model;       /* PTD_MODEL_* */
+    int32_t nx, ny, nz;  /* cells including boundary cells; unused dims = 1 */
+    double lx, ly, lz;   /* domain lengths */
+    double dt;           /* physical time step */
+    int32_t nt;          /* physical time steps solved by ptd_solve */
+    int32_t itmax;       /* PT iteration cap per physical step (itMax) */
+    int32_t nchk;        /* residual check cadence (nout) */
+    int32_t precision;   /* PTD_PREC_* */
+    double tol;          /* stop when err <= tol */
+    double cfl;          /* CFL: Vpdtau = cfl * min(dx,dy,dz) */
+    double resc;         /* iteration-parameter scaling (Resc); 1 for the linear models */
+    double D;            /* LIN: the diffusivity; LINSTEP: the D in Re (max(D1,D2)) */
+    int32_t resid_mode;  /* PTD_RESID_* */
+    int32_t norm;        /* PTD_NORM_* */
+    double norm_len;     /* RMS divisor; <= 0 means the number of inner cells */
+    int32_t flags;       /* PTD_FLAG_* */
+    int32_t dc_max_outer;/* FP32_DC: outer FP64 corrections per step cap (0: default) */
+    double dc_inner_rtol;/* FP32_DC: inner FP32 solve relative tolerance (0: default) */
+    int32_t reserved[8]; /* zero */
+} ptd_params;
+
+typedef struct ptd_ctx ptd_ctx;
+
+/* Fill p with the defaults of the reference script for (ndim, model):
+ * lx=ly=lz=10, dt=0.2, nt=5 (ttot=1), tol=1e-8, itmax=1e5, nchk=10, D=1,
+ * cfl = 0.99 (1D lin/linstep), 1.0 (1D nonlin), 1/sqrt(2) (2D), 1/sqrt(3) (3D),
+ * resc = 1/1.2 for 2D/3D nonlinear, else 1; n = 512 (1D/2D) or 64 (3D).
+ * Replaces: the parameter blocks of scripts/diff_1D_lin.jl:35-50,
+ * diff_2D_nonlin.jl:48-62, diff_3D/diff_3D_nonlin_multixpu.jl:59-74 (and siblings). */
+PTD_API int ptd_params_init(ptd_params* p, int32_t ndim, int32_t model);
+
+/* Validate p and allocate the device buffers of one grid.
+ * Replaces: the @zeros/@ones allocations of the driver (e.g.
+ * scripts/diff_2D_nonlin.jl:65-73). */
+PTD_API int ptd_create(ptd_ctx** ctx, const ptd_params* p);
+
+/* Solve p->nt physical steps: H in = H0, H out = H after nt steps.
+ * D: LINSTEP cell diffusivity (nx*ny*nz), else NULL.
+ * iters_per_step (nullable): PT iterations of each step (nt entries).
+ * err_hist (nullable): err of every residual check, in order, up to err_cap;
+ * n_err (nullable): number of checks performed.
+ * Replaces: the physical-time + PT loop of diffusion_2D_()
+ * (scripts/diff_2D_nonlin.jl:76-91; same in every driver). */
+PTD_API int ptd_solve(ptd_ctx* ctx, double* H, const double* D, int32_t* iters_per_step,
+              double* err_hist, int32_t err_cap, int32_t* n_err);
+
+/* Resident-state interface (the same loop split in pieces; used for timing
+ * and by callers that keep H on the device between calls). */
+PTD_API int ptd_set_state(ptd_ctx* ctx, const double* H, const double* D); /* H and Hold <- H, fluxes <- 0 */
+PTD_API int ptd_step(ptd_ctx* ctx, int32_t nsteps, int32_t* iters_per_step, double* err_hist,
+             int32_t err_cap, int32_t* n_err);                       /* nsteps physical steps */
+PTD_API int ptd_iterate(ptd_ctx* ctx, int32_t niter);  /* niter PT iterations, no checks (perf protocol,
+                                                  scripts/diff_3D/diff_3D_nonlin_perf.jl:97-105) */
+PTD_API int ptd_get_state(ptd_ctx* ctx, double* H);    /* H out */
+
+/* The context's CUDA stream (cudaStream_t) and a device synchronize of it. */
+PTD_API void* ptd_stream(ptd_ctx* ctx);
+PTD_API int ptd_sync(ptd_ctx* ctx);
+
+/* Counters since ptd_create: kernels launched by the library (each kernel of
+ * a replayed CUDA graph counts) and PT iterations executed. */
+PTD_API int ptd_counters(ptd_ctx* ctx, int64_t* kernel_launches, int64_t* pt_iterations);
+
+PTD_API void ptd_destroy(ptd_ctx* ctx);
+
+PTD_API const char* ptd_strerror(int status);
+PTD_API const char* ptd_last_error(void);   /* detail of the last failure on this thread */
+PTD_API int ptd_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PTD_H */

@@ -1,0 +1,108 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE).
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module; it checks the CUDA library and is never on the
+product path.  ``build()`` compiles ``ptd_oracle.c`` with the Makefile beside
+it (gcc, OpenMP, no FMA contraction).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libptd_oracle.so")
+
+
+class OraParams(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int32), ("model", C.c_int32),
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+        ("dt", C.c_double),
+        ("nt", C.c_int32), ("itmax", C.c_int32), ("nout", C.c_int32),
+        ("tol", C.c_double), ("cfl", C.c_double), ("resc", C.c_double), ("D", C.c_double),
+        ("recip", C.c_int32), ("resid", C.c_int32), ("norm", C.c_int32), ("nthreads", C.c_int32),
+        ("norm_len", C.c_double),
+    ]
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "ptd_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int32)
+        L.ora_solve.argtypes = [C.POINTER(OraParams), dp, dp, ip, dp, C.c_int32, ip]
+        L.ora_solve.restype = C.c_int
+        L.ora_iterate.argtypes = [C.POINTER(OraParams), dp, dp, dp, dp, dp, dp, C.c_int32]
+        L.ora_iterate.restype = C.c_int
+        L.ora_residual_norm.argtypes = [C.POINTER(OraParams), dp, dp, dp, dp]
+        L.ora_residual_norm.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _dptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def params(script, shape, *, nt=None, itmax=None, nout=None, resid=0, norm=0, nthreads=0,
+           norm_len=0.0):
+    s = script
+    nx = shape[0]
+    ny = shape[1] if len(shape) > 1 else 1
+    nz = shape[2] if len(shape) > 2 else 1
+    D = s.D if s.model == 0 else max(s.D, s.D2)
+    return OraParams(s.ndim, s.model, nx, ny, nz, s.lx, s.ly, s.lz, s.dt,
+                     s.nt if nt is None else nt,
+                     s.itmax if itmax is None else itmax,
+                     s.nout if nout is None else nout,
+                     s.tol, s.cfl, s.resc, D, int(s.recip), resid, norm, nthreads, norm_len)
+
+
+def solve(script, H0, D=None, *, nt=None, itmax=None, nout=None, resid=0, norm=0, nthreads=0,
+          errcap=100000, norm_len=0.0):
+    """Run the reference algorithm on the CPU.  Returns (H, iters_per_step, errhist, status)."""
+    H = np.array(H0, dtype=np.float64, order="F", copy=True)
+    p = params(script, H.shape, nt=nt, itmax=itmax, nout=nout, resid=resid, norm=norm,
+               nthreads=nthreads, norm_len=norm_len)
+    Dv = None if D is None else np.asfortranarray(D, dtype=np.float64)
+    iters = np.zeros(max(p.nt, 1), dtype=np.int32)
+    eh = np.zeros(errcap, dtype=np.float64)
+    ne = C.c_int32(0)
+    st = lib().ora_solve(C.byref(p), _dptr(H), _dptr(Dv),
+                         iters.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(eh), errcap, C.byref(ne))
+    return H, iters[: p.nt].copy(), eh[: min(ne.value, errcap)].copy(), st
+
+
+def iterate(script, H, Hold, q, niter, D=None, nthreads=0):
+    """Fixed-iteration kernel loop (timed CPU baseline): updates H and q (3 arrays) in place."""
+    p = params(script, H.shape, nthreads=nthreads)
+    Dv = None if D is None else np.asfortranarray(D, dtype=np.float64)
+    st = lib().ora_iterate(C.byref(p), _dptr(H), _dptr(Hold), _dptr(Dv),
+                           _dptr(q[0]), _dptr(q[1]), _dptr(q[2]), niter)
+    if st:
+        raise RuntimeError(f"ora_iterate failed ({st})")
+
+
+def residual_norm(script, H, Hold, Hpre=None, D=None, norm=0):
+    p = params(script, H.shape, norm=norm)
+    Dv = None if D is None else np.asfortranarray(D, dtype=np.float64)
+    return lib().ora_residual_norm(C.byref(p), _dptr(np.asfortranarray(H)),
+                                   _dptr(np.asfortranarray(Hold)),
+                                   _dptr(None if Hpre is None else np.asfortranarray(Hpre)), _dptr(Dv))

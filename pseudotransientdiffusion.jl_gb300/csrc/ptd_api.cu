@@ -1,0 +1,627 @@
+// ptd_api.cu -- the C ABI (include/ptd.h): contexts, the physical-time and
+// PT-iteration driver, host <-> device transfers.
+//
+// The driver restates the loop of the reference's diffusion_{1,2,3}D_()
+// (scripts/diff_2D_nonlin.jl:76-91, the same in every solver script):
+//   for each physical step: iter = 0, err = 2 tol;
+//     while err > tol and iter < itmax: one PT iteration; iter += 1;
+//       if iter % nout == 0: err = norm(ResH)/sqrt(length(ResH))
+//     Hold = H; NaN check
+// with the iterations, the checks and the stopping decision all on the GPU:
+// a CUDA graph holds one check block (nchk fused PT kernels, the last one
+// also forming the residual, then a one-thread judge kernel that computes err
+// and sets a done flag), and the host replays it in growing batches, reading
+// the small device state between batches.  Kernels that find the done flag
+// set return at entry, so the iteration count is exactly the reference's
+// (the first multiple of nchk at which err <= tol).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/ptd.h"
+#include "ptd_internal.h"
+
+using namespace ptd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int status, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+}  // namespace
+
+int ptd::set_error(int status, const char* msg)
+{
+    g_last_error = msg ? msg : "";
+    return status;
+}
+
+int ptd::cuda_fail(cudaError_t e, const char* where)
+{
+    return fail(PTD_ECUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return ptd::cuda_fail(_e, #call);   \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+extern "C" int ptd_abi_version(void) { return PTD_ABI_VERSION; }
+
+extern "C" const char* ptd_strerror(int status)
+{
+    switch (status) {
+    case PTD_OK: return "ok";
+    case PTD_EINVAL: return "invalid argument";
+    case PTD_ENAN: return "residual is NaN";
+    case PTD_ENOTCONV: return "not converged within itmax";
+    case PTD_ECUDA: return "CUDA error";
+    case PTD_ENOMEM: return "out of memory";
+    case PTD_ESTATE: return "call out of order";
+    case PTD_ETIMEOUT: return "device wait timed out";
+    }
+    return "unknown status";
+}
+
+extern "C" const char* ptd_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int ptd_params_init(ptd_params* p, int32_t ndim, int32_t model)
+{
+    if (!p) return fail(PTD_EINVAL, "ptd_params_init: p is NULL");
+    if (ndim < 1 || ndim > 3) return fail(PTD_EINVAL, "ptd_params_init: ndim must be 1, 2 or 3");
+    if (model < PTD_MODEL_LIN || model > PTD_MODEL_NONLIN)
+        return fail(PTD_EINVAL, "ptd_params_init: unknown model %d", model);
+    std::memset(p, 0, sizeof(*p));
+    p->ndim = ndim;
+    p->model = model;
+    const int n = ndim == 3 ? 64 : 512;
+    p->nx = n;
+    p->ny = ndim > 1 ? n : 1;
+    p->nz = ndim > 2 ? n : 1;
+    p->lx = p->ly = p->lz = 10.0;
+    p->dt = 0.2;
+    p->nt = 5;
+    p->itmax = 100000;
+    p->nchk = 10;
+    p->precision = PTD_PREC_FP64;
+    p->tol = 1e-8;
+    if (ndim == 1) p->cfl = model == PTD_MODEL_NONLIN ? 1.0 : 0.99;
+    else p->cfl = 1.0 / std::sqrt((double)ndim);
+    p->resc = (model == PTD_MODEL_NONLIN && ndim > 1) ? 1.0 / 1.2 : 1.0;
+    p->D = 1.0;
+    p->resid_mode = PTD_RESID_MIXED;
+    p->norm = PTD_NORM_RMS;
+    return PTD_OK;
+}
+
+int ptd::validate(const ptd_params* p)
+{
+    if (!p) return fail(PTD_EINVAL, "params is NULL");
+    if (p->ndim < 1 || p->ndim > 3) return fail(PTD_EINVAL, "ndim must be 1, 2 or 3 (got %d)", p->ndim);
+    if (p->model < PTD_MODEL_LIN || p->model > PTD_MODEL_NONLIN)
+        return fail(PTD_EINVAL, "unknown model %d", p->model);
+    const int n[3] = {p->nx, p->ny, p->nz};
+    for (int d = 0; d < 3; ++d) {
+        if (d < p->ndim && n[d] < 3)
+            return fail(PTD_EINVAL, "n[%d] = %d: each dimension needs >= 3 cells", d, n[d]);
+        if (d >= p->ndim && n[d] != 1)
+            return fail(PTD_EINVAL, "n[%d] = %d must be 1 for a %dD grid", d, n[d], p->ndim);
+        if (n[d] > (1 << 30)) return fail(PTD_EINVAL, "n[%d] too large", d);
+    }
+    const double l[3] = {p->lx, p->ly, p->lz};
+    for (int d = 0; d < p->ndim; ++d)
+        if (!(l[d] > 0.0) || !std::isfinite(l[d])) return fail(PTD_EINVAL, "domain length %d must be > 0", d);
+    if (!(p->dt > 0.0) || !std::isfinite(p->dt)) return fail(PTD_EINVAL, "dt must be > 0");
+    if (p->nt < 0) return fail(PTD_EINVAL, "nt must be >= 0");
+    if (p->itmax < 0) return fail(PTD_EINVAL, "itmax must be >= 0");
+    if (p->nchk < 1) return fail(PTD_EINVAL, "nchk must be >= 1");
+    if (!(p->tol >= 0.0)) return fail(PTD_EINVAL, "tol must be >= 0");
+    if (!(p->cfl > 0.0) || !std::isfinite(p->cfl)) return fail(PTD_EINVAL, "cfl must be > 0");
+    if (!(p->resc > 0.0) || !std::isfinite(p->resc)) return fail(PTD_EINVAL, "resc must be > 0");
+    if (p->model != PTD_MODEL_NONLIN && (!(p->D > 0.0) || !std::isfinite(p->D)))
+        return fail(PTD_EINVAL, "D must be > 0");
+    if (p->precision != PTD_PREC_FP64 && p->precision != PTD_PREC_FP32_DC)
+        return fail(PTD_EINVAL, "unknown precision %d", p->precision);
+    if (p->resid_mode != PTD_RESID_MIXED && p->resid_mode != PTD_RESID_CONSISTENT)
+        return fail(PTD_EINVAL, "unknown resid_mode %d", p->resid_mode);
+    if (p->norm != PTD_NORM_RMS && p->norm != PTD_NORM_MAX) return fail(PTD_EINVAL, "unknown norm %d", p->norm);
+    if (p->flags & ~PTD_FLAG_STRICT) return fail(PTD_EINVAL, "unknown flags 0x%x", p->flags);
+    for (int k = 0; k < 8; ++k)
+        if (p->reserved[k]) return fail(PTD_EINVAL, "reserved fields must be zero");
+    return PTD_OK;
+}
+
+// Scalar iteration parameters, restating the reference's a1 block
+// (scripts/diff_2D_lin.jl:49-53, diff_2D_linstep.jl:67-71, diff_2D_nonlin.jl:185-188):
+// dx = lx/nx, Vpdtau = CFL*min(dx..), L = max(lx..), Re = pi + sqrt(pi^2 + L^2/D/dt),
+// theta = L/Vpdtau/Re, dtau = Vpdtau*L/D/Re.
+void ptd::derive(const ptd_params& p, Derived& dv)
+{
+    const double pi = 3.141592653589793;
+    const double l[3] = {p.lx, p.ly, p.lz};
+    const int n[3] = {p.nx, p.ny, p.nz};
+    double hmin = 0.0, L = 0.0;
+    for (int d = 0; d < p.ndim; ++d) {
+        dv.h[d] = l[d] / (double)n[d];
+        hmin = d == 0 ? dv.h[d] : std::min(hmin, dv.h[d]);
+        L = d == 0 ? l[d] : std::max(L, l[d]);
+    }
+    dv.vpdt = p.cfl * hmin;
+    dv.L = L;
+    dv.rdt = 1.0 / p.dt;
+    double kappa = 1.0;
+    dv.c_lin = dv.e_lin = 0.0;
+    dv.k1 = dv.k2 = dv.k3 = 0.0;
+    if (p.model == PTD_MODEL_LIN) {
+        const double re = pi + std::sqrt(pi * pi + ((L * L / p.D) / p.dt));
+        const double theta = (L / dv.vpdt) / re;
+        const double dtau = ((dv.vpdt * L) / p.D) / re;
+        dv.c_lin = 1.0 / (1.0 + theta);
+        dv.e_lin = dtau / (1.0 + dtau / p.dt);
+        kappa = p.D;
+    } else if (p.model == PTD_MODEL_LINSTEP) {
+        const double re = pi + std::sqrt(pi * pi + ((L * L / p.D) / p.dt));
+        const double theta = (L / dv.vpdt) / re;
+        dv.c_lin = 1.0 / (1.0 + theta);
+        dv.k3 = re / (dv.vpdt * L);
+        kappa = 0.5;
+    } else {
+        dv.k1 = 1.0 / (dv.vpdt * L * p.resc);
+        dv.k2 = L * p.resc / dv.vpdt;
+        kappa = 0.125;
+    }
+    for (int d = 0; d < 3; ++d) dv.sig[d] = d < p.ndim ? kappa / (dv.h[d] * dv.h[d]) : 0.0;
+    dv.A = L * L / p.dt;
+    long long inner = 1;
+    for (int d = 0; d < p.ndim; ++d) inner *= (long long)(n[d] - 2);
+    dv.norm_den = p.norm_len > 0.0 ? p.norm_len : (double)inner;
+}
+
+void ptd::fill_args(const ptd_params& p, const Derived& dv, PTArgs& a)
+{
+    std::memset(&a, 0, sizeof(a));
+    a.nx = p.nx;
+    a.ny = p.ny;
+    a.nz = p.nz;
+    a.rdt = dv.rdt;
+    for (int d = 0; d < 3; ++d) a.sig[d] = dv.sig[d];
+    a.c_lin = dv.c_lin;
+    a.e_lin = dv.e_lin;
+    a.fA = (float)dv.A;
+    a.fpi = 3.14159265358979f;
+    a.fpi2 = (float)(3.141592653589793 * 3.141592653589793);
+    a.fk1 = (float)dv.k1;
+    a.fk2 = (float)dv.k2;
+    a.fk3 = (float)dv.k3;
+    a.frdt = (float)dv.rdt;
+    a.norm_max = p.norm == PTD_NORM_MAX;
+}
+
+// ---------------------------------------------------------------------------
+int ptd::copy_field_in(const ptd_ctx_base& g, double* dst, const double* src, cudaStream_t s)
+{
+    const size_t w = (size_t)g.nx * sizeof(double);
+    const size_t rows = (size_t)g.ny * g.nz;
+    CK(cudaMemcpy2DAsync(dst, (size_t)g.sy * sizeof(double), src, w, w, rows, cudaMemcpyDefault, s));
+    return PTD_OK;
+}
+
+int ptd::copy_field_out(const ptd_ctx_base& g, double* dst, const double* src, cudaStream_t s)
+{
+    const size_t w = (size_t)g.nx * sizeof(double);
+    const size_t rows = (size_t)g.ny * g.nz;
+    CK(cudaMemcpy2DAsync(dst, w, src, (size_t)g.sy * sizeof(double), w, rows, cudaMemcpyDefault, s));
+    return PTD_OK;
+}
+
+// ---------------------------------------------------------------------------
+struct ptd_ctx : ptd_ctx_base {
+    ptd_params p;
+    Derived dv;
+    LaunchCfg cfg;
+    cudaStream_t stream = nullptr;
+    double* H[2] = {nullptr, nullptr};
+    double* Hold = nullptr;
+    double* W[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    double* D = nullptr;
+    DevState* st = nullptr;
+    int* zero_flag = nullptr;
+    double* errhist = nullptr;
+    int errcap = 0;
+    DevState* h_st = nullptr;     // pinned mirror of *st
+    cudaGraphExec_t gblock[2] = {nullptr, nullptr};
+    cudaGraphExec_t gplain[2] = {nullptr, nullptr};
+    int plain_len = 32;
+    int cur = 0;                  // buffer holding the current H
+    bool have_state = false;
+    long long launches = 0, iterations = 0;
+    int kernels_per_block = 0;
+    DcState* dc = nullptr;        // FP32 defect-correction resources
+};
+
+static void args_for(const ptd_ctx* c, int parity, const int* done, PTArgs& a)
+{
+    fill_args(c->p, c->dv, a);
+    a.sy = c->sy;
+    a.sz = c->sz;
+    a.Hin = c->H[parity];
+    a.Hout = c->H[parity ^ 1];
+    a.Hold = c->Hold;
+    for (int d = 0; d < 3; ++d) {
+        a.win[d] = c->W[d][parity] ? c->W[d][parity] : c->W[0][parity];
+        a.wout[d] = c->W[d][parity ^ 1] ? c->W[d][parity ^ 1] : c->W[0][parity ^ 1];
+    }
+    a.D = c->D;
+    a.done = done;
+    a.acc = &c->st->acc;
+}
+
+static int capture_block(ptd_ctx* c, int parity, cudaGraphExec_t* out)
+{
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int par = parity;
+    const int nchk = c->p.nchk;
+    int nk = 0;
+    cudaError_t err = cudaSuccess;
+    for (int it = 0; it < nchk && err == cudaSuccess; ++it) {
+        PTArgs a;
+        args_for(c, par, &c->st->done, a);
+        const bool check = it == nchk - 1;
+        if (check && c->p.resid_mode == PTD_RESID_CONSISTENT) {
+            err = launch_pt_fp64(a, c->p.ndim, c->p.model, false, c->cfg, c->stream);
+            if (err == cudaSuccess) err = launch_resid_consistent(a, c->p.ndim, c->p.model, c->stream);
+            nk += 2;
+        } else {
+            err = launch_pt_fp64(a, c->p.ndim, c->p.model, check, c->cfg, c->stream);
+            nk += 1;
+        }
+        par ^= 1;
+    }
+    if (err == cudaSuccess)
+        err = launch_judge(c->st, c->errhist, c->errcap, nchk, c->p.itmax, c->p.tol, c->dv.norm_den,
+                           c->p.norm == PTD_NORM_MAX, c->stream);
+    nk += 1;
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (err != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(err, "capture check block");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    cudaError_t e3 = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+    c->kernels_per_block = nk;
+    return PTD_OK;
+}
+
+static int capture_plain(ptd_ctx* c, int parity, cudaGraphExec_t* out)
+{
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int par = parity;
+    cudaError_t err = cudaSuccess;
+    for (int it = 0; it < c->plain_len && err == cudaSuccess; ++it) {
+        PTArgs a;
+        args_for(c, par, c->zero_flag, a);
+        err = launch_pt_fp64(a, c->p.ndim, c->p.model, false, c->cfg, c->stream);
+        par ^= 1;
+    }
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (err != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(err, "capture plain block");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    cudaError_t e3 = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+    return PTD_OK;
+}
+
+static void free_ctx(ptd_ctx* c)
+{
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (int q = 0; q < 2; ++q) {
+        if (c->gblock[q]) cudaGraphExecDestroy(c->gblock[q]);
+        if (c->gplain[q]) cudaGraphExecDestroy(c->gplain[q]);
+    }
+    if (c->dc) dc_destroy(c->dc);
+    cudaFree(c->H[0]);
+    cudaFree(c->H[1]);
+    cudaFree(c->Hold);
+    for (int d = 0; d < 3; ++d)
+        for (int q = 0; q < 2; ++q) cudaFree(c->W[d][q]);
+    cudaFree(c->D);
+    cudaFree(c->st);
+    cudaFree(c->zero_flag);
+    cudaFree(c->errhist);
+    if (c->h_st) cudaFreeHost(c->h_st);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
+{
+    if (!out) return fail(PTD_EINVAL, "ptd_create: ctx is NULL");
+    *out = nullptr;
+    int rc = validate(p);
+    if (rc) return rc;
+    ptd_ctx* c = new (std::nothrow) ptd_ctx();
+    if (!c) return fail(PTD_ENOMEM, "ptd_create: host allocation failed");
+    c->p = *p;
+    derive(c->p, c->dv);
+    c->nx = p->nx;
+    c->ny = p->ny;
+    c->nz = p->nz;
+    c->sy = p->ndim == 1 ? p->nx : ((p->nx + 31) / 32) * 32;
+    c->sz = c->sy * p->ny;
+    c->nfield = c->sz * p->nz;
+    c->cfg = tuned_config(*p);
+    const size_t bytes = (size_t)c->nfield * sizeof(double);
+    auto alloc = [&](void** ptr, size_t n) -> int {
+        cudaError_t e = cudaMalloc(ptr, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(e == cudaErrorMemoryAllocation ? PTD_ENOMEM : PTD_ECUDA, "cudaMalloc(%zu): %s", n,
+                        cudaGetErrorString(e));
+        }
+        return PTD_OK;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        free_ctx(c);
+        return cuda_fail(e, "cudaStreamCreateWithFlags");
+    }
+    rc = alloc((void**)&c->H[0], bytes);
+    if (!rc) rc = alloc((void**)&c->H[1], bytes);
+    if (!rc) rc = alloc((void**)&c->Hold, bytes);
+    for (int d = 0; d < p->ndim && !rc; ++d)
+        for (int q = 0; q < 2 && !rc; ++q) rc = alloc((void**)&c->W[d][q], bytes);
+    if (!rc && p->model == PTD_MODEL_LINSTEP) rc = alloc((void**)&c->D, bytes);
+    if (!rc) rc = alloc((void**)&c->st, sizeof(DevState));
+    if (!rc) rc = alloc((void**)&c->zero_flag, sizeof(int));
+    c->errcap = (p->nchk <= p->itmax ? p->itmax / p->nchk : 0) + 2;
+    if (!rc) rc = alloc((void**)&c->errhist, (size_t)c->errcap * sizeof(double));
+    if (!rc && cudaMallocHost((void**)&c->h_st, sizeof(DevState)) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(PTD_ENOMEM, "cudaMallocHost failed");
+    }
+    if (rc) {
+        free_ctx(c);
+        return rc;
+    }
+    e = cudaMemsetAsync(c->zero_flag, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->st, 0, sizeof(DevState), c->stream);
+    if (e != cudaSuccess) {
+        free_ctx(c);
+        return cuda_fail(e, "cudaMemsetAsync");
+    }
+    if (p->precision == PTD_PREC_FP32_DC) {
+        rc = dc_create(*c, c->p, c->dv, c->stream, &c->dc);
+        if (rc) {
+            free_ctx(c);
+            return rc;
+        }
+    } else {
+        for (int q = 0; q < 2 && !rc; ++q) {
+            if (p->nchk <= p->itmax) rc = capture_block(c, q, &c->gblock[q]);
+            if (!rc) rc = capture_plain(c, q, &c->gplain[q]);
+        }
+        if (rc) {
+            free_ctx(c);
+            return rc;
+        }
+    }
+    *out = c;
+    return PTD_OK;
+}
+
+extern "C" void ptd_destroy(ptd_ctx* c) { free_ctx(c); }
+
+extern "C" void* ptd_stream(ptd_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int ptd_sync(ptd_ctx* c)
+{
+    if (!c) return fail(PTD_EINVAL, "ctx is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+    return PTD_OK;
+}
+
+extern "C" int ptd_counters(ptd_ctx* c, int64_t* launches, int64_t* iters)
+{
+    if (!c) return fail(PTD_EINVAL, "ctx is NULL");
+    long long l = c->launches, it = c->iterations;
+    if (c->dc) {
+        const DcCounters k = dc_counters(c->dc);
+        l += k.launches;
+        it += k.iterations;
+    }
+    if (launches) *launches = l;
+    if (iters) *iters = it;
+    return PTD_OK;
+}
+
+extern "C" int ptd_set_state(ptd_ctx* c, const double* H, const double* D)
+{
+    if (!c) return fail(PTD_EINVAL, "ctx is NULL");
+    if (!H) return fail(PTD_EINVAL, "H is NULL");
+    if (c->p.model == PTD_MODEL_LINSTEP && !D) return fail(PTD_EINVAL, "the step model needs D");
+    const size_t bytes = (size_t)c->nfield * sizeof(double);
+    // padding stays zero: clear whole buffers first
+    CK(cudaMemsetAsync(c->H[0], 0, bytes, c->stream));
+    int rc = copy_field_in(*c, c->H[0], H, c->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->H[1], c->H[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->Hold, c->H[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    for (int d = 0; d < 3; ++d)
+        for (int q = 0; q < 2; ++q)
+            if (c->W[d][q]) CK(cudaMemsetAsync(c->W[d][q], 0, bytes, c->stream));
+    if (c->p.model == PTD_MODEL_LINSTEP) {
+        CK(cudaMemsetAsync(c->D, 0, bytes, c->stream));
+        rc = copy_field_in(*c, c->D, D, c->stream);
+        if (rc) return rc;
+    }
+    c->cur = 0;
+    if (c->dc) {
+        rc = dc_set_state(c->dc, *c, c->H[0], c->Hold, c->D, c->stream);
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->have_state = true;
+    return PTD_OK;
+}
+
+extern "C" int ptd_get_state(ptd_ctx* c, double* H)
+{
+    if (!c) return fail(PTD_EINVAL, "ctx is NULL");
+    if (!H) return fail(PTD_EINVAL, "H is NULL");
+    if (!c->have_state) return fail(PTD_ESTATE, "no state set");
+    const double* src = c->dc ? dc_current(c->dc) : c->H[c->cur];
+    int rc = copy_field_out(*c, H, src, c->stream);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return PTD_OK;
+}
+
+// Run n PT iterations without checks starting from buffer c->cur.
+static int run_plain(ptd_ctx* c, long long n)
+{
+    while (n >= c->plain_len) {
+        CK(cudaGraphLaunch(c->gplain[c->cur], c->stream));
+        c->launches += c->plain_len;
+        c->iterations += c->plain_len;
+        if (c->plain_len & 1) c->cur ^= 1;
+        n -= c->plain_len;
+    }
+    for (; n > 0; --n) {
+        PTArgs a;
+        args_for(c, c->cur, c->zero_flag, a);
+        CK(launch_pt_fp64(a, c->p.ndim, c->p.model, false, c->cfg, c->stream));
+        c->launches += 1;
+        c->iterations += 1;
+        c->cur ^= 1;
+    }
+    return PTD_OK;
+}
+
+extern "C" int ptd_iterate(ptd_ctx* c, int32_t niter)
+{
+    if (!c) return fail(PTD_EINVAL, "ctx is NULL");
+    if (niter < 0) return fail(PTD_EINVAL, "niter must be >= 0");
+    if (!c->have_state) return fail(PTD_ESTATE, "no state set");
+    if (c->dc) return dc_iterate(c->dc, *c, niter);
+    return run_plain(c, niter);
+}
+
+// One physical step of the FP64 solver.  Returns the PT iteration count in
+// *iters and appends the step's errors to err_hist.
+static int fp64_step(ptd_ctx* c, int32_t* iters, double* err_hist, int32_t err_cap, int32_t* n_err,
+                     int* nan_flag, int* capped)
+{
+    const ptd_params& p = c->p;
+    CK(launch_reset_state(c->st, c->stream));
+    c->launches += 1;
+    const long long blocks_max = p.nchk <= p.itmax ? p.itmax / p.nchk : 0;
+    long long launched = 0;
+    long long batch = 1;
+    const int start = c->cur;
+    int done = DONE_RUNNING, iter = 0, nchecks = 0;
+    while (launched < blocks_max) {
+        const long long nb = std::min(batch, blocks_max - launched);
+        for (long long b = 0; b < nb; ++b) {
+            const int par = (int)((start + (launched + b) * p.nchk) & 1);
+            CK(cudaGraphLaunch(c->gblock[par], c->stream));
+            c->launches += c->kernels_per_block;
+        }
+        launched += nb;
+        CK(cudaMemcpyAsync(c->h_st, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        done = c->h_st->done;
+        iter = c->h_st->iter;
+        nchecks = c->h_st->nchecks;
+        if (done != DONE_RUNNING) break;
+        batch = std::min<long long>(batch * 2, 64);
+    }
+    c->iterations += iter;
+    c->cur = (start + iter) & 1;
+    if (done == DONE_RUNNING || done == DONE_CAP) {
+        const long long tail = (long long)p.itmax - iter;
+        int rc = run_plain(c, tail);
+        if (rc) return rc;
+        iter = p.itmax;
+        *capped = 1;
+    }
+    *iters = iter;
+    const size_t bytes = (size_t)c->nfield * sizeof(double);
+    CK(cudaMemcpyAsync(c->Hold, c->H[c->cur], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if (err_hist && nchecks > 0 && *n_err < err_cap) {
+        const int k = std::min(nchecks, std::min(err_cap - *n_err, c->errcap));
+        CK(cudaMemcpyAsync(err_hist + *n_err, c->errhist, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost,
+                           c->stream));
+    }
+    *n_err += nchecks;
+    CK(cudaStreamSynchronize(c->stream));
+    *nan_flag = done == DONE_NAN;
+    return PTD_OK;
+}
+
+extern "C" int ptd_step(ptd_ctx* c, int32_t nsteps, int32_t* iters_per_step, double* err_hist,
+                        int32_t err_cap, int32_t* n_err)
+{
+    if (!c) return fail(PTD_EINVAL, "ctx is NULL");
+    if (nsteps < 0) return fail(PTD_EINVAL, "nsteps must be >= 0");
+    if (!c->have_state) return fail(PTD_ESTATE, "no state set");
+    if (err_cap < 0) return fail(PTD_EINVAL, "err_cap must be >= 0");
+    int32_t ne = 0;
+    int any_capped = 0;
+    for (int s = 0; s < nsteps; ++s) {
+        int32_t it = 0;
+        int nan_flag = 0, capped = 0;
+        int rc = c->dc ? dc_step(c->dc, *c, &it, err_hist, err_cap, &ne, &nan_flag, &capped)
+                       : fp64_step(c, &it, err_hist, err_cap, &ne, &nan_flag, &capped);
+        if (rc) return rc;
+        if (iters_per_step) iters_per_step[s] = it;
+        any_capped |= capped;
+        if (nan_flag) {
+            if (n_err) *n_err = ne;
+            return fail(PTD_ENAN, "residual is NaN after physical step %d", s + 1);
+        }
+    }
+    if (n_err) *n_err = ne;
+    if ((c->p.flags & PTD_FLAG_STRICT) && any_capped)
+        return fail(PTD_ENOTCONV, "a physical step reached itmax = %d without err <= tol", c->p.itmax);
+    return PTD_OK;
+}
+
+extern "C" int ptd_solve(ptd_ctx* c, double* H, const double* D, int32_t* iters_per_step,
+                         double* err_hist, int32_t err_cap, int32_t* n_err)
+{
+    if (!c) return fail(PTD_EINVAL, "ctx is NULL");
+    int rc = ptd_set_state(c, H, D);
+    if (rc) return rc;
+    int rs = ptd_step(c, c->p.nt, iters_per_step, err_hist, err_cap, n_err);
+    if (rs && rs != PTD_ENAN && rs != PTD_ENOTCONV) return rs;
+    rc = ptd_get_state(c, H);
+    if (rc) return rc;
+    return rs;
+}

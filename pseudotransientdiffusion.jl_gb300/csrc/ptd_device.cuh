@@ -1,0 +1,217 @@
+// ptd_device.cuh -- device-side building blocks of the fused PT kernels.
+//
+// The reference evaluates the damped flux and the H update as
+//   q_new = (q*theta - D_f*dH/dx) / (1 + theta)                 (compute_flux!)
+//   H_new = (H + dtau*(Hold/dt - div q)) / (1 + dtau/dt)          (compute_update!)
+// (scripts/diff_2D_nonlin.jl:154-165).  Both are rewritten here in the
+// algebraically identical fixed-point-preserving form
+//   w_new = w - c * (w + K_f * g)          c = 1/(1+theta),  g = H_R - H_L
+//   H_new = H - e * ((H - Hold)/dt + sum_d (w_R - w_L) * sigma_d)
+//                                          e = dtau/(1 + dtau/dt)
+// where w is the flux scaled by dx/kappa (q = w * kappa / dx) and K_f the
+// face conductance without its constant factor kappa:
+//   LIN      K_f = 1,             kappa = D
+//   LINSTEP  K_f = D_L + D_R,     kappa = 1/2   (@av_xi(D) = (D_L+D_R)*0.5)
+//   NONLIN   K_f = (H_L + H_R)^3, kappa = 1/8   ((@av_xi(H))^3)
+// and sigma_d = kappa / dx_d^2.  At a fixed point w = -K_f g and
+// (H-Hold)/dt + div q = 0 whatever c and e are, so the iteration parameters
+// (Re, theta, dtau -- pure convergence accelerators) are evaluated in FP32
+// while everything that defines the solution (K_f, g, w, H, the divergence
+// and the residual) stays in FP64.  This removes every FP64 division and
+// square root from the hot loop; GB300's FP64 rate is a small fraction of its
+// FP32 rate, so the FP64 instruction count is what bounds the FP64 kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ptd {
+
+enum { LIN = 0, LINSTEP = 1, NONLIN = 2 };
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Everything a PT-iteration kernel needs, passed by value.
+struct PTArgs {
+    int nx, ny, nz;
+    long long sy;       // elements between consecutive y rows (row pitch)
+    long long sz;       // elements between consecutive z planes
+    double rdt;         // 1/dt
+    double sig[3];      // kappa / dx_d^2
+    double c_lin;       // LIN, LINSTEP: 1/(1+theta)
+    double e_lin;       // LIN: dtau/(1+dtau/dt)
+    float fA;           // L^2/dt
+    float fpi, fpi2;    // pi, pi^2
+    float fk1;          // NONLIN cell: 1/(Vpdtau*L*Resc)
+    float fk2;          // NONLIN face: L*Resc/Vpdtau
+    float fk3;          // LINSTEP cell: Re/(Vpdtau*L)
+    float frdt;         // 1/dt
+    const double* Hin;
+    double* Hout;
+    const double* Hold;
+    const double* win[3];
+    double* wout[3];
+    const double* D;    // LINSTEP cell diffusivity
+    const int* done;    // nonzero: the step has stopped, skip the iteration
+    double* acc;        // residual accumulator: sum R^2 (RMS) or max |R| bits (MAX)
+    int norm_max;
+};
+
+// ---------------------------------------------------------------------------
+// Exact FP32 -> FP64 and truncating FP64 -> FP32 conversions done with integer
+// operations (the hardware conversion instructions share the scarce FP64
+// pipe).  Only used for the iteration parameters, where any deterministic
+// approximation is acceptable.
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    unsigned b = __float_as_uint(f);
+    unsigned e = (b >> 23) & 0xffu;
+    unsigned hi = (b & 0x80000000u) | ((b & 0x7fffffffu) >> 3);
+    hi += (e == 0u) ? 0u : ((e == 255u) ? 0x70000000u : 0x38000000u);
+    unsigned lo = (e == 0u) ? 0u : (b << 29);
+    if (e == 0u) hi &= 0x80000000u;   // zero / denormal -> signed zero
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ float d2f_bits(double x)
+{
+    int hi = __double2hiint(x);
+    unsigned lo = (unsigned)__double2loint(x);
+    unsigned sign = (unsigned)hi & 0x80000000u;
+    int ef = ((hi >> 20) & 0x7ff) - 896;   // 1023 - 127
+    unsigned m = (((unsigned)hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned r = sign | ((unsigned)ef << 23) | m;
+    r = (ef <= 0) ? sign : r;
+    r = (ef >= 255) ? (sign | 0x7f800000u) : r;
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ float frcp(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float fsqrt(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// NONLIN face: c = 1/(1+theta), theta = L*Resc/(Vpdtau*Re_f),
+// Re_f = pi + sqrt(pi^2 + L^2/(D_f dt)), D_f = ((h_L+h_R)/2)^3
+// (scripts/diff_2D_nonlin.jl:145-151).  D_f -> 0 gives Re_f -> inf, c -> 1.
+__device__ __forceinline__ float nonlin_face_c(const PTArgs& a, float hsum)
+{
+    float m = 0.5f * hsum;
+    float df = m * m * m;
+    float re = a.fpi + fsqrt(a.fpi2 + a.fA * frcp(df));
+    float th = a.fk2 * frcp(re);
+    return frcp(1.0f + th);
+}
+
+// NONLIN cell: e = 1/(1/dtau + 1/dt) with
+// 1/dtau = H^3 Re / (Vpdtau L Resc) = (pi H^3 + sqrt(pi^2 H^6 + L^2 H^3/dt)) * k1
+// (scripts/diff_2D_nonlin.jl:149,152); finite for H^3 -> 0 (e -> dt).
+__device__ __forceinline__ float nonlin_cell_e(const PTArgs& a, float h)
+{
+    float h3 = h * h * h;
+    float inv = (a.fpi * h3 + fsqrt(a.fpi2 * h3 * h3 + a.fA * h3)) * a.fk1;
+    return frcp(inv + a.frdt);
+}
+
+// LINSTEP cell: 1/dtau = maxloc(D) * Re / (Vpdtau L) (compute_iter_params!,
+// scripts/diff_2D_linstep.jl:18-21).
+__device__ __forceinline__ float linstep_cell_e(const PTArgs& a, float dmax)
+{
+    return frcp(dmax * a.fk3 + a.frdt);
+}
+
+// One face: returns the new scaled flux; u = K_f * g (the undamped flux of
+// the residual, same scaling) when U is requested.
+template <int MODEL, bool U>
+__device__ __forceinline__ double face_update(const PTArgs& a, double HL, double HR, float hsum,
+                                              double DL, double DR, double w, double& u)
+{
+    double g = HR - HL;
+    double K, c;
+    if (MODEL == LIN) {
+        c = a.c_lin;
+        if (U) u = g;
+        return fma(-c, g + w, w);
+    } else if (MODEL == LINSTEP) {
+        K = DL + DR;
+        c = a.c_lin;
+    } else {
+        double s = HL + HR;
+        K = s * s * s;
+        c = f2d_bits(nonlin_face_c(a, hsum));
+    }
+    if (U) u = K * g;
+    return fma(-c, fma(K, g, w), w);
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(FULL, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// Block-wide residual reduction into a.acc (sum of squares, or max |R| as the
+// ordered bit pattern of a non-negative double; NaN orders above +inf).
+__device__ __forceinline__ void block_reduce_residual(const PTArgs& a, double part_sum,
+                                                      unsigned long long part_max)
+{
+    __shared__ double s_sum[32];
+    __shared__ unsigned long long s_max[32];
+    const int nthr = blockDim.x * blockDim.y * blockDim.z;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int wid = tid >> 5, ln = tid & 31;
+    const int nw = (nthr + 31) >> 5;
+    if (a.norm_max) {
+        part_max = warp_max_u64(part_max);
+        if (ln == 0) s_max[wid] = part_max;
+    } else {
+        part_sum = warp_sum(part_sum);
+        if (ln == 0) s_sum[wid] = part_sum;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        if (a.norm_max) {
+            unsigned long long v = ln < nw ? s_max[ln] : 0ull;
+            v = warp_max_u64(v);
+            if (ln == 0 && v) atomicMax(reinterpret_cast<unsigned long long*>(a.acc), v);
+        } else {
+            double v = ln < nw ? s_sum[ln] : 0.0;
+            v = warp_sum(v);
+            if (ln == 0) atomicAdd(a.acc, v);
+        }
+    }
+}
+
+__device__ __forceinline__ void accumulate_residual(double r, double& sum, unsigned long long& mx)
+{
+    sum = fma(r, r, sum);
+    unsigned long long b = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
+    mx = b > mx ? b : mx;
+}
+
+__device__ __forceinline__ bool step_done(const int* done)
+{
+    return __ldcg(done) != 0;
+}
+
+}  // namespace ptd

@@ -1,0 +1,202 @@
+"""Host-side mirror of the reference's solver drivers on top of libptd.so.
+
+``run_script(name, nx, ...)`` does what ``diffusion_{1,2,3}D_()`` of the named
+reference script does (e.g. scripts/diff_2D_nonlin.jl:46-106): it derives the
+grid, builds H0 (and the step field D) with the script's arithmetic, solves
+``nt`` physical steps with the accelerated PT iteration -- on the GPU, through
+the C ABI -- and returns the cell centres and H (the script's
+``USE_RETURN=true`` return value, scripts/diff_2D_nonlin.jl:105) together with
+the iteration counts it prints (:92) and the residual history.
+
+:class:`Solver` is the thin object wrapper of one ``ptd_ctx``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .scripts import LINSTEP, SCRIPTS, Script, cell_centres, grid_shape, initial_condition, step_field
+
+PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC}
+
+
+def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=None,
+                precision="fp64", resid="mixed", norm="rms", norm_len=0.0, strict=False,
+                dc_max_outer=0, dc_inner_rtol=0.0) -> _abi.PtdParams:
+    """ptd_params for a script at a grid shape (x fastest)."""
+    p = _abi.PtdParams()
+    _abi.check(_abi.lib().ptd_params_init(C.byref(p), script.ndim, script.model), "ptd_params_init")
+    p.nx = shape[0]
+    p.ny = shape[1] if script.ndim > 1 else 1
+    p.nz = shape[2] if script.ndim > 2 else 1
+    p.lx, p.ly, p.lz = script.lx, script.ly, script.lz
+    p.dt = script.dt
+    p.nt = script.nt if nt is None else nt
+    p.itmax = script.itmax if itmax is None else itmax
+    p.nchk = script.nout if nchk is None else nchk
+    p.tol = script.tol if tol is None else tol
+    p.cfl = script.cfl
+    p.resc = script.resc
+    p.D = script.D if script.model != LINSTEP else max(script.D, script.D2)
+    p.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    p.resid_mode = {"mixed": _abi.RESID_MIXED, "consistent": _abi.RESID_CONSISTENT}[resid]
+    p.norm = {"rms": _abi.NORM_RMS, "max": _abi.NORM_MAX}[norm]
+    p.norm_len = norm_len
+    p.flags = _abi.FLAG_STRICT if strict else 0
+    p.dc_max_outer = dc_max_outer
+    p.dc_inner_rtol = dc_inner_rtol
+    return p
+
+
+def _ptr(a):
+    """Address of a host numpy array or of a device tensor (anything with data_ptr())."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return C.c_void_p(a.ctypes.data)
+
+
+class Solver:
+    """One ptd_ctx: device buffers for one grid and parameter set."""
+
+    def __init__(self, params: _abi.PtdParams):
+        self.params = params
+        self._h = C.c_void_p()
+        _abi.check(_abi.lib().ptd_create(C.byref(self._h), C.byref(params)), "ptd_create")
+
+    def close(self):
+        if self._h:
+            _abi.lib().ptd_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check_array(self, a, name):
+        n = self.params.nx * self.params.ny * self.params.nz
+        if hasattr(a, "data_ptr"):
+            if a.numel() != n or not a.is_contiguous():
+                raise ValueError(f"{name}: expected a contiguous tensor of {n} elements")
+            return a
+        a = np.asarray(a)
+        if a.dtype != np.float64 or a.size != n:
+            raise ValueError(f"{name}: expected {n} float64 values")
+        if not (a.flags.f_contiguous or a.ndim == 1):
+            raise ValueError(f"{name}: expected x-fastest (Fortran-ordered) storage")
+        return a
+
+    def solve(self, H, D=None, err_cap: int = 100000, raise_on_nan: bool = True):
+        """Solve nt steps in place on H (numpy Fortran array or device tensor).
+        Returns (iters_per_step, errhist, status)."""
+        H = self._check_array(H, "H")
+        if D is not None:
+            D = self._check_array(D, "D")
+        nt = max(self.params.nt, 1)
+        iters = np.zeros(nt, dtype=np.int32)
+        eh = np.zeros(max(err_cap, 1), dtype=np.float64)
+        ne = C.c_int32(0)
+        st = _abi.lib().ptd_solve(self._h, _ptr(H), _ptr(D), iters.ctypes.data_as(C.POINTER(C.c_int32)),
+                                  eh.ctypes.data_as(C.POINTER(C.c_double)), err_cap, C.byref(ne))
+        if st not in (_abi.PTD_OK, _abi.PTD_ENAN, _abi.PTD_ENOTCONV) or (st == _abi.PTD_ENAN and raise_on_nan):
+            _abi.check(st, "ptd_solve")
+        return iters[: self.params.nt].copy(), eh[: min(ne.value, err_cap)].copy(), st
+
+    def set_state(self, H, D=None):
+        H = self._check_array(H, "H")
+        _abi.check(_abi.lib().ptd_set_state(self._h, _ptr(H), _ptr(D)), "ptd_set_state")
+
+    def step(self, nsteps: int, err_cap: int = 100000):
+        iters = np.zeros(max(nsteps, 1), dtype=np.int32)
+        eh = np.zeros(max(err_cap, 1), dtype=np.float64)
+        ne = C.c_int32(0)
+        st = _abi.lib().ptd_step(self._h, nsteps, iters.ctypes.data_as(C.POINTER(C.c_int32)),
+                                 eh.ctypes.data_as(C.POINTER(C.c_double)), err_cap, C.byref(ne))
+        _abi.check(st, "ptd_step")
+        return iters[:nsteps].copy(), eh[: min(ne.value, err_cap)].copy()
+
+    def iterate(self, niter: int):
+        _abi.check(_abi.lib().ptd_iterate(self._h, niter), "ptd_iterate")
+
+    def get_state(self, out=None):
+        if out is None:
+            shape = (self.params.nx, self.params.ny, self.params.nz)
+            out = np.zeros(shape, dtype=np.float64, order="F")
+        _abi.check(_abi.lib().ptd_get_state(self._h, _ptr(out)), "ptd_get_state")
+        return out
+
+    def sync(self):
+        _abi.check(_abi.lib().ptd_sync(self._h), "ptd_sync")
+
+    @property
+    def stream(self) -> int:
+        return _abi.lib().ptd_stream(self._h) or 0
+
+    def counters(self):
+        l, it = C.c_int64(0), C.c_int64(0)
+        _abi.check(_abi.lib().ptd_counters(self._h, C.byref(l), C.byref(it)), "ptd_counters")
+        return l.value, it.value
+
+
+@dataclass
+class Result:
+    """What a reference driver returns and prints."""
+
+    coords: tuple            # (xc,) / (xc, yc) / (xc, yc, zc)
+    H: np.ndarray            # final H, shape (nx[, ny[, nz]]), x fastest
+    iters: np.ndarray        # PT iterations per physical step
+    errhist: np.ndarray      # err of every residual check
+    status: int = 0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def ittot(self) -> int:
+        return int(np.sum(self.iters))
+
+    def as_return(self):
+        """The script's USE_RETURN tuple: (xc, H), (xc, yc, H) or (xc, yc, zc, H)."""
+        return (*self.coords, self.H)
+
+
+def _env_int(name, default):
+    v = os.environ.get(name)
+    return int(v) if v else default
+
+
+def run_script(name: str, nx: int | None = None, ny: int | None = None, nz: int | None = None, *,
+               script: Script | None = None, precision="fp64", verbose=False, **overrides) -> Result:
+    """Run the named reference driver on the GPU.  Grid sizes default to the
+    script's NX/NY/NZ environment variables (then to its built-in default)."""
+    s = script if script is not None else SCRIPTS[name]
+    nx = nx if nx is not None else _env_int("NX", s.default_n)
+    ny = ny if ny is not None else _env_int("NY", nx)
+    nz = nz if nz is not None else _env_int("NZ", nx)
+    shape = grid_shape(s, nx, ny, nz)
+    H = initial_condition(s, *shape)
+    D = step_field(s, *shape) if s.model == LINSTEP else None
+    params = make_params(s, shape, precision=precision, **overrides)
+    with Solver(params) as sol:
+        iters, eh, st = sol.solve(H, D)
+    lengths = (s.lx, s.ly, s.lz)
+    coords = tuple(cell_centres(lengths[d], shape[d]) for d in range(s.ndim))
+    res = Result(coords, H, iters, eh, st)
+    if verbose:
+        print(f"Total time = {s.ttot:.2f}, time steps = {len(iters)}, nx = {nx}, iterations tot = {res.ittot}")
+    return res

@@ -1,0 +1,181 @@
+"""Parity of the CUDA library (through the C ABI) with the CPU oracle and the
+reference's golden data.  Bar: PT iteration counts equal, relative L2 error of
+H <= 1e-10 (FP64)."""
+import numpy as np
+import pytest
+
+import ptdiff
+from golden_cases import (COUNT_SCRIPTS, GOLDEN_CASES, golden_array, load_counts, load_reftests,
+                          multirank_norm_len, reference_isapprox, sample)
+from oracle import oracle as O
+from ptdiff import _abi
+from ptdiff import scripts as S
+
+pytestmark = pytest.mark.gpu
+
+REF = load_reftests()
+COUNTS = load_counts()
+RTOL_FP64 = 1e-10
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def gpu_solve(s, shape, D=None, H0=None, **kw):
+    H = S.initial_condition(s, *shape) if H0 is None else np.array(H0, order="F", copy=True)
+    p = ptdiff.make_params(s, shape, **kw)
+    with ptdiff.Solver(p) as sol:
+        iters, eh, st = sol.solve(H, D, raise_on_nan=False)
+    return H, iters, eh, st
+
+
+def oracle_kw(kw):
+    out = {}
+    for k in ("nt", "itmax", "norm_len"):
+        if k in kw:
+            out[k] = kw[k]
+    if "nchk" in kw:
+        out["nout"] = kw["nchk"]
+    if kw.get("resid") == "consistent":
+        out["resid"] = 1
+    if kw.get("norm") == "max":
+        out["norm"] = 1
+    return out
+
+
+def compare(s, shape, **kw):
+    D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
+    H0 = S.initial_condition(s, *shape)
+    H, iters, eh, st = gpu_solve(s, shape, D, **kw)
+    Hr, iters_r, eh_r, st_r = O.solve(s, H0, D, **oracle_kw(kw))
+    assert st == 0 and st_r == 0
+    assert list(iters) == list(iters_r)
+    assert rel_l2(H, Hr) <= RTOL_FP64
+    assert len(eh) == len(eh_r)
+    if len(eh):
+        assert np.allclose(eh, eh_r, rtol=1e-6, atol=1e-12)
+    return H, iters
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN_CASES))
+def test_golden_cases(name):
+    n = GOLDEN_CASES[name]
+    s = S.SCRIPTS[name]
+    H, _ = compare(s, (n,) * s.ndim)
+    got = sample(H, n, s.ndim)
+    ref = golden_array(REF[name])
+    assert reference_isapprox(got, ref)
+    assert rel_l2(got, ref) <= RTOL_FP64
+
+
+def _count_cases():
+    limits = {1: 2048, 2: 256, 3: 126}
+    out = []
+    for key, rows in COUNTS.items():
+        s = S.SCRIPTS[COUNT_SCRIPTS[key]]
+        for row in rows:
+            if row[0] <= limits[s.ndim]:
+                out.append((key, tuple(row)))
+    return out
+
+
+@pytest.mark.parametrize("key,row", _count_cases())
+def test_published_iteration_counts(key, row):
+    s = S.SCRIPTS[COUNT_SCRIPTS[key]]
+    shape = row[: s.ndim]
+    D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
+    nl = multirank_norm_len(shape[0]) if s.ndim == 3 else 0.0
+    _, iters, _, st = gpu_solve(s, shape, D, norm_len=nl)
+    assert st == 0
+    assert int(iters.sum()) == row[s.ndim]
+
+
+@pytest.mark.parametrize("name,shape", [
+    ("diff_2D_nonlin", (37, 95)), ("diff_2D_lin", (3, 3)), ("diff_2D_linstep", (66, 33)),
+    ("diff_2D_nonlin", (200, 7)), ("diff_3D_nonlin_multixpu", (35, 17, 9)),
+    ("diff_3D_linstep_multixpu", (3, 4, 5)), ("diff_3D_lin_multixpu", (63, 33, 20)),
+    ("diff_1D_nonlin", (3,)), ("diff_1D_linstep", (1000,)),
+])
+def test_ragged_and_tiny_grids(name, shape):
+    compare(S.SCRIPTS[name], shape)
+
+
+@pytest.mark.parametrize("kw", [
+    dict(nchk=7), dict(nchk=1), dict(itmax=95), dict(itmax=50, nchk=200), dict(itmax=0),
+    dict(norm="max"), dict(resid="consistent"), dict(nt=0), dict(nchk=13, itmax=100),
+])
+@pytest.mark.parametrize("name,shape", [("diff_2D_nonlin", (48, 40)), ("diff_3D_linstep_multixpu", (20, 18, 16)),
+                                        ("diff_1D_lin", (64,))])
+def test_driver_options(name, shape, kw):
+    compare(S.SCRIPTS[name], shape, **kw)
+
+
+def test_perf_scripts_fixed_iterations():
+    for name, shape in [("diff_2D_nonlin_perf", (96, 64)), ("diff_3D_nonlin_perf", (40, 40, 40))]:
+        _, iters = compare(S.SCRIPTS[name], shape)
+        assert list(iters) == [S.SCRIPTS[name].itmax] * S.SCRIPTS[name].nt
+
+
+def test_nan_input_reports_enan():
+    s = S.SCRIPTS["diff_2D_nonlin"]
+    H0 = S.initial_condition(s, 40, 40)
+    H0[20, 20] = np.nan
+    _, _, _, st = gpu_solve(s, (40, 40), H0=H0)
+    assert st == _abi.PTD_ENAN
+    _, _, _, st_r = O.solve(s, H0)
+    assert st_r == 2
+
+
+def test_strict_mode_reports_not_converged():
+    s = S.SCRIPTS["diff_2D_lin"]
+    _, iters, _, st = gpu_solve(s, (64, 64), itmax=30, strict=True)
+    assert st == _abi.PTD_ENOTCONV
+    assert list(iters) == [30] * 5
+
+
+def test_device_pointers():
+    torch = pytest.importorskip("torch")
+    s = S.SCRIPTS["diff_2D_linstep"]
+    shape = (70, 50)
+    H0 = S.initial_condition(s, *shape)
+    D = S.step_field(s, *shape)
+    Hd = torch.from_numpy(np.ravel(H0, order="F").copy()).cuda()
+    Dd = torch.from_numpy(np.ravel(D, order="F").copy()).cuda()
+    p = ptdiff.make_params(s, shape)
+    with ptdiff.Solver(p) as sol:
+        iters, _, st = sol.solve(Hd, Dd)
+    Hr, iters_r, _, _ = O.solve(s, H0, D)
+    assert st == 0 and list(iters) == list(iters_r)
+    assert rel_l2(Hd.cpu().numpy(), np.ravel(Hr, order="F")) <= RTOL_FP64
+
+
+def test_resident_state_api_matches_solve():
+    s = S.SCRIPTS["diff_3D_nonlin_multixpu"]
+    shape = (24, 24, 24)
+    H0 = S.initial_condition(s, *shape)
+    p = ptdiff.make_params(s, shape)
+    with ptdiff.Solver(p) as sol:
+        sol.set_state(H0)
+        its = [int(sol.step(1)[0][0]) for _ in range(s.nt)]
+        H = sol.get_state().reshape(shape, order="F")
+        launches, iters_done = sol.counters()
+    Hr, iters_r, _, _ = O.solve(s, H0)
+    assert its == list(iters_r)
+    assert rel_l2(H, Hr) <= RTOL_FP64
+    assert iters_done >= sum(its) and launches > iters_done
+
+
+def test_iterate_matches_oracle_iterations():
+    s = S.SCRIPTS["diff_2D_nonlin_perf"]
+    shape = (130, 70)
+    H0 = S.initial_condition(s, *shape)
+    p = ptdiff.make_params(s, shape)
+    with ptdiff.Solver(p) as sol:
+        sol.set_state(H0)
+        sol.iterate(77)
+        H = sol.get_state().reshape(shape, order="F")
+    Hr = np.array(H0, order="F")
+    q = [np.zeros_like(Hr) for _ in range(3)]
+    O.iterate(s, Hr, H0.copy(order="F"), q, 77)
+    assert rel_l2(H, Hr) <= 1e-12

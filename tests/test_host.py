@@ -1,0 +1,134 @@
+"""Host-side logic and the C ABI surface (no GPU needed).
+
+* libptd.so loads and exports every entry point declared in include/ptd.h;
+* the ctypes mirror of ptd_params has the C layout (checked against gcc);
+* ptd_params_init restates the reference scripts' defaults;
+* ptd_create validates its parameters before touching the GPU;
+* the scripts table, grids and initial conditions follow the reference.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from ptdiff import _abi
+from ptdiff import scripts as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    declared = _abi.declared_functions()
+    assert "ptd_solve" in declared and "ptd_create" in declared
+    L = _abi.lib()
+    for name in declared:
+        assert hasattr(L, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", _abi.LIB_PATH], capture_output=True, text=True)
+    exported = {ln.split()[-1] for ln in out.stdout.splitlines() if " T " in ln}
+    assert set(declared) <= exported
+    # nothing but the C ABI is exported
+    assert all(n.startswith("ptd_") for n in exported), sorted(exported)
+    assert L.ptd_abi_version() == 1
+
+
+def test_params_layout_matches_c(tmp_path):
+    fields = [f for f, _ in _abi.PtdParams._fields_]
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/ptd.h"',
+             'int main(void){', 'printf("%zu\\n", sizeof(ptd_params));']
+    lines += [f'printf("%zu\\n", offsetof(ptd_params, {f}));' for f in fields]
+    lines += ['return 0;}']
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-o", str(exe), str(src)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                           check=True).stdout.split()]
+    assert vals[0] == C.sizeof(_abi.PtdParams)
+    for f, off in zip(fields, vals[1:]):
+        assert getattr(_abi.PtdParams, f).offset == off, f
+
+
+@pytest.mark.parametrize("ndim,model", [(1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2), (3, 0), (3, 1), (3, 2)])
+def test_params_init_matches_scripts(ndim, model):
+    p = _abi.PtdParams()
+    assert _abi.lib().ptd_params_init(C.byref(p), ndim, model) == 0
+    name = {0: "lin", 1: "linstep", 2: "nonlin"}[model]
+    s = S.SCRIPTS[f"diff_{ndim}D_{name}" + ("_multixpu" if ndim == 3 else "")]
+    assert p.cfl == s.cfl and p.resc == s.resc
+    assert p.tol == s.tol and p.itmax == s.itmax and p.nchk == s.nout
+    assert p.dt == s.dt and p.nt == s.nt and p.lx == s.lx
+    assert (p.nx, p.ny, p.nz)[:ndim] == (s.default_n,) * ndim
+
+
+def _create(**kw):
+    p = _abi.PtdParams()
+    _abi.lib().ptd_params_init(C.byref(p), kw.pop("ndim", 2), kw.pop("model", 2))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    h = C.c_void_p()
+    st = _abi.lib().ptd_create(C.byref(h), C.byref(p))
+    return st, _abi.last_error()
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(nx=2), "needs >= 3 cells"),
+    (dict(nz=4), "must be 1 for a 2D grid"),
+    (dict(dt=0.0), "dt must be > 0"),
+    (dict(nchk=0), "nchk must be >= 1"),
+    (dict(itmax=-1), "itmax must be >= 0"),
+    (dict(cfl=-1.0), "cfl must be > 0"),
+    (dict(precision=7), "unknown precision"),
+    (dict(resid_mode=3), "unknown resid_mode"),
+    (dict(norm=5), "unknown norm"),
+    (dict(flags=0x100), "unknown flags"),
+    (dict(model=0, D=0.0), "D must be > 0"),
+    (dict(ndim=4), "ndim must be"),
+])
+def test_create_rejects_invalid_params(kw, msg):
+    st, err = _create(**kw)
+    assert st == _abi.PTD_EINVAL
+    assert msg in err
+
+
+def test_strerror_and_null_args():
+    L = _abi.lib()
+    assert _abi.strerror(0) == "ok"
+    assert _abi.strerror(_abi.PTD_ENAN) == "residual is NaN"
+    assert L.ptd_create(None, None) == _abi.PTD_EINVAL
+    assert L.ptd_solve(None, None, None, None, None, 0, None) == _abi.PTD_EINVAL
+    assert L.ptd_step(None, 1, None, None, 0, None) == _abi.PTD_EINVAL
+    assert L.ptd_params_init(None, 2, 2) == _abi.PTD_EINVAL
+    L.ptd_destroy(None)
+
+
+def test_linrange_and_cell_centres():
+    x = S.linrange(0.5, 9.5, 10)
+    assert x[0] == 0.5 and x[-1] == 9.5
+    assert np.allclose(np.diff(x), 1.0)
+    xc = S.cell_centres(10.0, 64)
+    assert xc[0] == 10.0 / 64 / 2 and np.allclose(np.diff(xc), 10.0 / 64)
+    assert list(S.sample_indices(64)[:3]) == [0, 6, 12]
+
+
+def test_step_fields():
+    s1 = S.SCRIPTS["diff_1D_linstep"]
+    D = S.step_field(s1, 64)
+    assert (D[:30] == 1e-4).all() and (D[30:] == 1.0).all()  # ceil(64/2.2) = 30
+    s2 = S.SCRIPTS["diff_2D_linstep"]
+    D = S.step_field(s2, 64, 64)
+    assert (D[:30, :] == 1e-4).all() and (D[:, :30] == 1e-4).all() and (D[30:, 30:] == 1.0).all()
+    s3 = S.SCRIPTS["diff_3D_linstep_multixpu"]
+    D = S.step_field(s3, 32, 32, 32)
+    # x_g = (ix-1)*dx < lx/2.2 -> first 15 planes (14*0.3125 = 4.375 < 4.545)
+    assert (D[:15] == 1e-4).all() and (D[15:, 15:, :] == 1.0).all()
+
+
+def test_benchmark_initial_condition():
+    s = S.CONFIGS["2d_nonlin_4096"]
+    H = S.initial_condition(s, 32, 32)
+    assert H[0, 5] == 1.0 and H[-1, 5] == 1.0 and H[5, 0] == 1.0 and H[5, -1] == 1.0
+    assert np.isclose(H[15, 15], 1.0 + np.exp(-2 * (10 / 64) ** 2))
+    assert s.nout == 100 and s.nt == 5
+    assert S.CONFIGS["3d_nonlin_512"].nt == 3
