@@ -201,8 +201,6 @@ def run_reference(args, world, rank, pg):
     shape = (s.default_n,) * s.ndim
     cb = None
     vals = []
-    for _ in range(args.warmup):
-        pass
     budget = max(4.0, 60.0 / max(args.steps, 1))
     for _ in range(args.steps):
         cb = cpu_baseline(s, shape, budget_s=budget)
@@ -236,29 +234,35 @@ def run_ours(args, world, rank, local, pg):
     sol = ptdiff.Solver(params)
     ext = torch.cuda.ExternalStream(sol.stream)
 
-    # ---- device-resident value: W untimed physical steps, then K timed ones
-    sol.set_state(H0)
-    for _ in range(args.warmup):
-        sol.step(1)
-    sol.sync()
-    l0, i0 = sol.counters()
+    def timed_steps(sol_, nsteps):
+        """Set H0, run W untimed physical steps, set H0 again, time nsteps steps."""
+        sol_.set_state(H0)
+        for _ in range(args.warmup):
+            sol_.step(1)
+        sol_.set_state(H0)
+        sol_.sync()
+        l0_, i0_ = sol_.counters()
+        st = torch.cuda.ExternalStream(sol_.stream)
+        barrier(pg)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        its_ = []
+        for _ in range(nsteps):
+            its, _ = sol_.step(1)
+            its_.append(int(its[0]))
+        a1.record(st)
+        a1.synchronize()
+        torch.cuda.synchronize()
+        barrier(pg)
+        l1_, i1_ = sol_.counters()
+        return a0.elapsed_time(a1) / 1e3, its_, l1_ - l0_, i1_ - i0_
+
+    # ---- device-resident value: FP64 PT, K physical steps from H0
     clocks = ClockSampler(local) if rank == 0 else None
-    barrier(pg)
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(ext)
-    step_iters = []
-    for _ in range(args.steps):
-        its, _ = sol.step(1)
-        step_iters.append(int(its[0]))
-    ev1.record(ext)
-    ev1.synchronize()
-    torch.cuda.synchronize()
-    barrier(pg)
+    t_dev, step_iters, launches, iters_timed = timed_steps(sol, args.steps)
     clk = clocks.stop() if clocks else None
-    t_dev = ev0.elapsed_time(ev1) / 1e3
-    l1, i1 = sol.counters()
-    iters_timed = i1 - i0
+    H_fp64 = sol.get_state()
     t_max = reduce_max(pg, t_dev)
     total_bytes = reduce_sum(pg, A * iters_timed)
     value = total_bytes / t_max / 1e9
@@ -277,6 +281,21 @@ def run_ours(args, world, rank, local, pg):
     peak, peak_kind = read_peaks()
     traffic = profile_traffic(args.workload)
     sol.close()
+
+    # ---- time to tol: FP32 iterations + FP64 defect correction, same K steps from H0
+    ttt = None
+    if args.precision == "fp64" and not args.no_dc:
+        pdc = ptdiff.make_params(s, shape, nt=1, precision="fp32_dc")
+        sdc = ptdiff.Solver(pdc)
+        t_dc, dc_iters, _, _ = timed_steps(sdc, args.steps)
+        H_dc = sdc.get_state()
+        sdc.close()
+        t_dc = reduce_max(pg, t_dc)
+        rel = float(np.linalg.norm(H_dc - H_fp64) / np.linalg.norm(H_fp64))
+        ttt = {"fp64_ms_per_step": round(t_max / args.steps * 1e3, 3),
+               "fp32_dc_ms_per_step": round(t_dc / args.steps * 1e3, 3),
+               "speedup": round(t_max / t_dc, 3), "rel_l2_fp32_dc_vs_fp64": rel,
+               "fp32_inner_iterations_per_step": dc_iters}
 
     # ---- e2e: ptd_solve on pinned host buffers, one physical step per call
     pe = ptdiff.make_params(s, shape, nt=1, precision=args.precision)
@@ -321,10 +340,10 @@ def run_ours(args, world, rank, local, pg):
         "cpu_baseline": cb,
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": int(H0.size * 8),
                 "d2h_bytes_per_step": int(H0.size * 8)},
-        "gpu_launches": int(l1 - l0),
+        "gpu_launches": int(launches),
         "clocks": clk,
         "pt_iterations_per_step": step_iters,
-        "time_to_tol_ms_per_step": round(t_max / max(args.steps, 1) * 1e3, 3),
+        "time_to_tol": ttt,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -342,6 +361,7 @@ def main():
     ap.add_argument("--fixed-iters", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-dc", action="store_true", help="skip the FP32+DC time-to-tol comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -195,6 +195,19 @@ void ptd::derive(const ptd_params& p, Derived& dv)
     dv.norm_den = p.norm_len > 0.0 ? p.norm_len : (double)inner;
 }
 
+FParams ptd::fparams(const Derived& dv)
+{
+    FParams f;
+    f.fA = (float)dv.A;
+    f.fpi = 3.14159265358979f;
+    f.fpi2 = (float)(3.141592653589793 * 3.141592653589793);
+    f.fk1 = (float)dv.k1;
+    f.fk2 = (float)dv.k2;
+    f.fk3 = (float)dv.k3;
+    f.frdt = (float)dv.rdt;
+    return f;
+}
+
 void ptd::fill_args(const ptd_params& p, const Derived& dv, PTArgs& a)
 {
     std::memset(&a, 0, sizeof(a));
@@ -205,13 +218,7 @@ void ptd::fill_args(const ptd_params& p, const Derived& dv, PTArgs& a)
     for (int d = 0; d < 3; ++d) a.sig[d] = dv.sig[d];
     a.c_lin = dv.c_lin;
     a.e_lin = dv.e_lin;
-    a.fA = (float)dv.A;
-    a.fpi = 3.14159265358979f;
-    a.fpi2 = (float)(3.141592653589793 * 3.141592653589793);
-    a.fk1 = (float)dv.k1;
-    a.fk2 = (float)dv.k2;
-    a.fk3 = (float)dv.k3;
-    a.frdt = (float)dv.rdt;
+    a.f = fparams(dv);
     a.norm_max = p.norm == PTD_NORM_MAX;
 }
 

@@ -1,21 +1,739 @@
 // ptd_dc.cu -- FP32 PT iterations inside an FP64 defect-correction loop.
+//
+// Per physical step the FP64 problem is F(H) = (H - Hold)/dt + div q(H) = 0
+// with q the reference's face flux (K_f times the H difference, K_f = D,
+// (D_L+D_R)/2 or ((H_L+H_R)/2)^3).  The outer loop is an inexact Newton
+// iteration carried out in FP64 on the GPU:
+//   r = -F(H)                       FP64 residual (both flux terms from H)
+//   err = ||r|| (RMS or max);  stop when err <= tol
+//   solve J delta = r  approximately with the accelerated PT iteration in
+//                      FP32 (the same damped-wave scheme as the FP64 kernels,
+//                      applied to the linearised operator J; K_f and the
+//                      iteration parameters from an FP32 copy of H)
+//   H += delta                      FP64
+// J = I/dt + div(-K_f grad . - dK_f/dH grad H .) : for D = H^3 the Newton term
+// 3 s^2 (H_R - H_L) (delta_L + delta_R) (s = H_L + H_R, scaled by 1/8) is
+// included, so the outer iteration converges quadratically; the linear models
+// have none.  H, the residual, its norm and the update stay FP64, which is
+// what convergence to tol = 1e-8 needs; the FP32 inner iterations move half
+// the bytes of the FP64 ones and run on the FP32 pipe.
+//
+// The inner iterations use the fused-kernel layout of ptd_fp64.cu (31-cell x
+// tiles per warp, y march in 2D, z march with shared-memory y exchange in 3D)
+// and the same device-side check/judge/done protocol, so a CUDA graph of
+// nchk inner iterations is replayed without a host round trip per check.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
 #include "ptd_internal.h"
 
 namespace ptd {
 
-struct DcState {
-    DcCounters k;
+struct DcArgs {
+    int nx, ny, nz;
+    long long sy, sz;
+    float rdt;
+    float sig[3];
+    float c_lin, e_lin;
+    FParams f;
+    const float* din;     // correction delta (iteration k)
+    float* dout;          // correction delta (iteration k+1)
+    const float* win[3];
+    float* wout[3];
+    const float* Hf;      // FP32 copy of H (linearisation point)
+    const float* Df;      // LINSTEP: FP32 copy of D
+    const float* r;       // FP32 copy of the FP64 residual
+    const int* done;
+    double* acc;
+    int norm_max;
 };
 
-int dc_create(const ptd_ctx_base&, const ptd_params&, const Derived&, cudaStream_t, DcState**)
+// Control block of the inner solve (device), see DevState in ptd_kernels.h.
+struct DcDev {
+    int done;
+    int nchecks;
+    int iter;
+    int pad;
+    double acc;        // inner residual accumulator
+    double err;        // last inner err
+    double target;     // inner stopping threshold
+    double outer_acc;  // FP64 residual accumulator
+    double outer_err;  // FP64 residual norm
+};
+
+// One face of the linearised flux (scaled like ptd_device.cuh):
+// u = K_f (d_R - d_L) [+ 3 s^2 (h_R - h_L) (d_L + d_R)],  w <- w - c (w + u).
+template <int MODEL, bool U>
+__device__ __forceinline__ float face32(const DcArgs& a, float dL, float dR, float hL, float hR, float DL,
+                                        float DR, float w, float& u)
 {
-    return set_error(PTD_EINVAL, "precision FP32_DC is not available in this build");
+    const float gd = dR - dL;
+    float uu, c;
+    if (MODEL == LIN) {
+        uu = gd;
+        c = a.c_lin;
+    } else if (MODEL == LINSTEP) {
+        uu = (DL + DR) * gd;
+        c = a.c_lin;
+    } else {
+        const float s = hL + hR;
+        const float s2 = s * s;
+        uu = s2 * s * gd;
+        uu = fmaf(3.0f * s2 * (hR - hL), dL + dR, uu);
+        c = nonlin_face_c(a.f, s);
+    }
+    if (U) u = uu;
+    return fmaf(-c, w + uu, w);
 }
-void dc_destroy(DcState* dc) { delete dc; }
-int dc_set_state(DcState*, const ptd_ctx_base&, double*, double*, const double*, cudaStream_t) { return PTD_EINVAL; }
-int dc_step(DcState*, const ptd_ctx_base&, int32_t*, double*, int32_t, int32_t*, int*, int*) { return PTD_EINVAL; }
-int dc_iterate(DcState*, const ptd_ctx_base&, int32_t) { return PTD_EINVAL; }
-const double* dc_current(const DcState*) { return nullptr; }
+
+template <int MODEL>
+__device__ __forceinline__ float cell_e32(const DcArgs& a, float h, float dmax)
+{
+    if (MODEL == LIN) return a.e_lin;
+    if (MODEL == LINSTEP) return linstep_cell_e(a.f, dmax);
+    return nonlin_cell_e(a.f, h);
+}
+
+__device__ __forceinline__ bool dc_done(const int* done) { return __ldcg(done) != 0; }
+
+// ---------------------------------------------------------------------------
+template <int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) dc1d_kernel(DcArgs a)
+{
+    if (dc_done(a.done)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = a.nx;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    if (i < nx) {
+        const float dc = a.din[i], hc = a.Hf[i];
+        const float Dc = MODEL == LINSTEP ? a.Df[i] : 0.0f;
+        float wr = 0.0f, ur = 0.0f, Dr = 0.0f;
+        if (i <= nx - 2) {
+            Dr = MODEL == LINSTEP ? a.Df[i + 1] : 0.0f;
+            wr = face32<MODEL, CHECK>(a, dc, a.din[i + 1], hc, a.Hf[i + 1], Dc, Dr, a.win[0][i], ur);
+            a.wout[0][i] = wr;
+        }
+        if (i >= 1 && i <= nx - 2) {
+            const float Dl = MODEL == LINSTEP ? a.Df[i - 1] : 0.0f;
+            float ul = 0.0f;
+            const float wl = face32<MODEL, CHECK>(a, a.din[i - 1], dc, a.Hf[i - 1], hc, Dl, Dc, a.win[0][i - 1], ul);
+            const float rr = a.r[i];
+            const float e = cell_e32<MODEL>(a, hc, fmaxf(fmaxf(Dl, Dr), Dc));
+            const float div = (wr - wl) * a.sig[0];
+            const float dn = fmaf(-e, fmaf(dc, a.rdt, div - rr), dc);
+            a.dout[i] = dn;
+            if (CHECK) accumulate_residual((double)fmaf(-dn, a.rdt, rr + (ur - ul) * a.sig[0]), part, pmax);
+        }
+    }
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+}
+
+template <int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) dc2d_kernel(DcArgs a, int chunk)
+{
+    if (dc_done(a.done)) return;
+    const int lane = threadIdx.x;
+    const int tile = blockIdx.x * blockDim.y + threadIdx.y;
+    const int i = 31 * tile + lane;
+    const int nx = a.nx, ny = a.ny;
+    const int j0 = 1 + blockIdx.y * chunk;
+    const int j1 = min(j0 + chunk, ny - 1);
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    if ((31 * tile < nx - 1) && (j0 < j1)) {
+        const int ic = min(i, nx - 1);
+        const bool xface = i <= nx - 2;
+        const bool upd = i >= 1 && i <= nx - 2 && lane >= 1;
+        const bool own_x = xface && (lane >= 1 || tile == 0);
+        const long long sy = a.sy;
+        long long idx = (long long)j0 * sy + ic;
+        float dc = a.din[idx], hc = a.Hf[idx];
+        float Dc = MODEL == LINSTEP ? a.Df[idx] : 0.0f, Db = 0.0f;
+        float wyb = 0.0f, uyb = 0.0f;
+        if (upd) {
+            Db = MODEL == LINSTEP ? a.Df[idx - sy] : 0.0f;
+            wyb = face32<MODEL, CHECK>(a, a.din[idx - sy], dc, a.Hf[idx - sy], hc, Db, Dc, a.win[1][idx - sy], uyb);
+            if (j0 == 1) a.wout[1][idx - sy] = wyb;
+        }
+        for (int j = j0; j < j1; ++j, idx += sy) {
+            const float dn = a.din[idx + sy], hn = a.Hf[idx + sy];
+            const float wx = a.win[0][idx], wy = a.win[1][idx], rr = a.r[idx];
+            const float Dn = MODEL == LINSTEP ? a.Df[idx + sy] : 0.0f;
+            float dr = __shfl_down_sync(FULL, dc, 1);
+            float hr = __shfl_down_sync(FULL, hc, 1);
+            float Dr = MODEL == LINSTEP ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
+            if (lane == 31) {
+                const bool ok = ic + 1 < nx;
+                dr = ok ? a.din[idx + 1] : dc;
+                hr = ok ? a.Hf[idx + 1] : hc;
+                if (MODEL == LINSTEP) Dr = ok ? a.Df[idx + 1] : Dc;
+            }
+            float ux = 0.0f, uy = 0.0f, wxn = 0.0f, wyn = 0.0f;
+            if (xface) wxn = face32<MODEL, CHECK>(a, dc, dr, hc, hr, Dc, Dr, wx, ux);
+            if (upd) wyn = face32<MODEL, CHECK>(a, dc, dn, hc, hn, Dc, Dn, wy, uy);
+            const float wxl = __shfl_up_sync(FULL, wxn, 1);
+            const float uxl = CHECK ? __shfl_up_sync(FULL, ux, 1) : 0.0f;
+            const float Dl = MODEL == LINSTEP ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
+            if (own_x) a.wout[0][idx] = wxn;
+            if (upd) {
+                a.wout[1][idx] = wyn;
+                const float e = cell_e32<MODEL>(a, hc, fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Db)), Dn));
+                const float div = fmaf(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]);
+                const float dnew = fmaf(-e, fmaf(dc, a.rdt, div - rr), dc);
+                a.dout[idx] = dnew;
+                if (CHECK) {
+                    const float divu = fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]);
+                    accumulate_residual((double)fmaf(-dnew, a.rdt, rr + divu), part, pmax);
+                }
+            }
+            dc = dn;
+            hc = hn;
+            wyb = wyn;
+            uyb = uy;
+            if (MODEL == LINSTEP) {
+                Db = Dc;
+                Dc = Dn;
+            }
+        }
+    }
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+}
+
+template <int MODEL, bool CHECK, int R>
+__global__ void __launch_bounds__(32 * R) dc3d_kernel(DcArgs a, int chunk)
+{
+    if (dc_done(a.done)) return;
+    __shared__ float sd[2][R][32];
+    __shared__ float sh[2][R][32];
+    __shared__ float sw[2][R][32];
+    __shared__ float su[CHECK ? 2 : 1][CHECK ? R : 1][32];
+    __shared__ float sD[MODEL == LINSTEP ? 2 : 1][MODEL == LINSTEP ? R : 1][32];
+    const int lane = threadIdx.x, r = threadIdx.y;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int i = 31 * blockIdx.x + lane;
+    const int j = (R - 1) * blockIdx.y + r;
+    const int k0 = 1 + blockIdx.z * chunk;
+    const int k1 = min(k0 + chunk, nz - 1);
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    if (k0 < k1) {
+        const int ic = min(i, nx - 1), jc = min(j, ny - 1);
+        const bool inner_x = i >= 1 && i <= nx - 2, inner_y = j >= 1 && j <= ny - 2;
+        const bool xface = i <= nx - 2 && inner_y && r >= 1;
+        const bool yface = j <= ny - 2 && inner_x;
+        const bool upd = inner_x && inner_y && lane >= 1 && r >= 1;
+        const bool own_x = xface && (lane >= 1 || blockIdx.x == 0);
+        const bool own_y = yface && lane >= 1 && (r >= 1 || blockIdx.y == 0);
+        const bool top = r == R - 1, up_ok = jc + 1 < ny;
+        const long long sy = a.sy, sz = a.sz;
+        long long idx = (long long)k0 * sz + (long long)jc * sy + ic;
+        float dc = a.din[idx], hc = a.Hf[idx];
+        float Dc = MODEL == LINSTEP ? a.Df[idx] : 0.0f, Db = 0.0f;
+        float wzb = 0.0f, uzb = 0.0f;
+        if (upd) {
+            Db = MODEL == LINSTEP ? a.Df[idx - sz] : 0.0f;
+            wzb = face32<MODEL, CHECK>(a, a.din[idx - sz], dc, a.Hf[idx - sz], hc, Db, Dc, a.win[2][idx - sz], uzb);
+            if (k0 == 1) a.wout[2][idx - sz] = wzb;
+        }
+        int p = 0;
+        sd[0][r][lane] = dc;
+        sh[0][r][lane] = hc;
+        if (MODEL == LINSTEP) sD[0][r][lane] = Dc;
+        __syncthreads();
+        for (int k = k0; k < k1; ++k, idx += sz) {
+            const float dn = a.din[idx + sz], hn = a.Hf[idx + sz];
+            const float wx = a.win[0][idx], wy = a.win[1][idx], wz = a.win[2][idx], rr = a.r[idx];
+            const float Dn = MODEL == LINSTEP ? a.Df[idx + sz] : 0.0f;
+            float du, hu, Du = 0.0f;
+            if (!top) {
+                du = sd[p][r + 1][lane];
+                hu = sh[p][r + 1][lane];
+                if (MODEL == LINSTEP) Du = sD[p][r + 1][lane];
+            } else {
+                du = up_ok ? a.din[idx + sy] : dc;
+                hu = up_ok ? a.Hf[idx + sy] : hc;
+                if (MODEL == LINSTEP) Du = up_ok ? a.Df[idx + sy] : Dc;
+            }
+            const float Dd = (MODEL == LINSTEP && r >= 1) ? sD[p][r - 1][lane] : 0.0f;
+            float dr = __shfl_down_sync(FULL, dc, 1);
+            float hr = __shfl_down_sync(FULL, hc, 1);
+            float Dr = MODEL == LINSTEP ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
+            if (lane == 31) {
+                const bool ok = ic + 1 < nx;
+                dr = ok ? a.din[idx + 1] : dc;
+                hr = ok ? a.Hf[idx + 1] : hc;
+                if (MODEL == LINSTEP) Dr = ok ? a.Df[idx + 1] : Dc;
+            }
+            float ux = 0.0f, uy = 0.0f, uz = 0.0f, wxn = 0.0f, wyn = 0.0f, wzn = 0.0f;
+            if (xface) wxn = face32<MODEL, CHECK>(a, dc, dr, hc, hr, Dc, Dr, wx, ux);
+            if (yface) wyn = face32<MODEL, CHECK>(a, dc, du, hc, hu, Dc, Du, wy, uy);
+            if (upd) wzn = face32<MODEL, CHECK>(a, dc, dn, hc, hn, Dc, Dn, wz, uz);
+            if (own_x) a.wout[0][idx] = wxn;
+            if (own_y) a.wout[1][idx] = wyn;
+            if (upd) a.wout[2][idx] = wzn;
+            const float wxl = __shfl_up_sync(FULL, wxn, 1);
+            const float uxl = CHECK ? __shfl_up_sync(FULL, ux, 1) : 0.0f;
+            const float Dl = MODEL == LINSTEP ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
+            sw[p][r][lane] = wyn;
+            if (CHECK) su[p][r][lane] = uy;
+            sd[p ^ 1][r][lane] = dn;
+            sh[p ^ 1][r][lane] = hn;
+            if (MODEL == LINSTEP) sD[p ^ 1][r][lane] = Dn;
+            __syncthreads();
+            if (upd) {
+                const float wyb = sw[p][r - 1][lane];
+                const float e = cell_e32<MODEL>(
+                    a, hc, fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Du)), fmaxf(fmaxf(Dd, Db), Dn)));
+                const float div = fmaf(wzn - wzb, a.sig[2], fmaf(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]));
+                const float dnew = fmaf(-e, fmaf(dc, a.rdt, div - rr), dc);
+                a.dout[idx] = dnew;
+                if (CHECK) {
+                    const float uyb = su[p][r - 1][lane];
+                    const float divu = fmaf(uz - uzb, a.sig[2], fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]));
+                    accumulate_residual((double)fmaf(-dnew, a.rdt, rr + divu), part, pmax);
+                }
+            }
+            dc = dn;
+            hc = hn;
+            wzb = wzn;
+            uzb = uz;
+            if (MODEL == LINSTEP) {
+                Db = Dc;
+                Dc = Dn;
+            }
+            p ^= 1;
+        }
+    }
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 residual r = -F(H) with both flux terms from H (consistent form of
+// check_res!, scripts/diff_2D_nonlin.jl:167-170), written as FP32 for the
+// inner solve and reduced (sum r^2 or max |r|) in FP64.
+template <int MODEL>
+__global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, float* rf, double* acc)
+{
+    const long long nix = a.nx - 2;
+    const long long niy = ndim > 1 ? a.ny - 2 : 1;
+    const long long niz = ndim > 2 ? a.nz - 2 : 1;
+    const long long total = nix * niy * niz;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long ix = 1 + t % nix;
+        const long long rest = t / nix;
+        const long long iy = ndim > 1 ? 1 + rest % niy : 0;
+        const long long iz = ndim > 2 ? 1 + rest / niy : 0;
+        const long long c = iz * a.sz + iy * a.sy + ix;
+        const long long st[3] = {1, a.sy, a.sz};
+        const double H = a.Hin[c];
+        double div = 0.0;
+        for (int d = 0; d < ndim; ++d) {
+            const double HR = a.Hin[c + st[d]], HL = a.Hin[c - st[d]];
+            double uR, uL;
+            if (MODEL == LIN) {
+                uR = HR - H;
+                uL = H - HL;
+            } else if (MODEL == LINSTEP) {
+                uR = (a.D[c] + a.D[c + st[d]]) * (HR - H);
+                uL = (a.D[c - st[d]] + a.D[c]) * (H - HL);
+            } else {
+                const double sR = H + HR, sL = HL + H;
+                uR = sR * sR * sR * (HR - H);
+                uL = sL * sL * sL * (H - HL);
+            }
+            div = fma(uR - uL, a.sig[d], div);
+        }
+        const double r = fma(-(H - a.Hold[c]), a.rdt, div);
+        rf[c] = (float)r;
+        accumulate_residual(r, part, pmax);
+    }
+    block_reduce_residual(acc, a.norm_max, part, pmax);
+}
+
+// H += delta on every cell (delta is zero on the boundary); refresh the FP32 copy.
+__global__ void dc_apply_kernel(double* H, float* Hf, const float* delta, long long n)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const double h = H[t] + (double)delta[t];
+        H[t] = h;
+        Hf[t] = __double2float_rn(h);
+    }
+}
+
+__global__ void dc_tofloat_kernel(const double* src, float* dst, long long n)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x)
+        dst[t] = __double2float_rn(src[t]);
+}
+
+// Outer judge: err of the FP64 residual; sets the inner target and resets
+// the inner control block.
+__global__ void dc_outer_judge_kernel(DcDev* st, double norm_den, int norm_max, double rtol, double tol)
+{
+    const double acc = st->outer_acc;
+    st->outer_acc = 0.0;
+    const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
+    st->outer_err = err;
+    st->target = fmax(rtol * err, 0.25 * tol);
+    st->done = 0;
+    st->nchecks = 0;
+    st->iter = 0;
+    st->acc = 0.0;
+    st->err = 0.0;
+}
+
+__global__ void dc_inner_judge_kernel(DcDev* st, int nchk, int itmax, double norm_den, int norm_max)
+{
+    if (st->done) return;
+    const double acc = st->acc;
+    st->acc = 0.0;
+    const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
+    st->err = err;
+    st->nchecks += 1;
+    st->iter += nchk;
+    if (!(err > st->target)) st->done = (err != err) ? DONE_NAN : DONE_CONVERGED;
+    else if (st->iter + nchk > itmax) st->done = DONE_CAP;
+}
+
+// ---------------------------------------------------------------------------
+struct DcState {
+    ptd_params p;
+    Derived dv;
+    LaunchCfg cfg;
+    cudaStream_t s = nullptr;
+    int ndim = 0, model = 0;
+    long long nfield = 0;
+    float* d[2] = {nullptr, nullptr};
+    float* w[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    float* Hf = nullptr;
+    float* Df = nullptr;
+    float* rf = nullptr;
+    double* H = nullptr;       // owned by the context: current FP64 H
+    double* Hold = nullptr;    // owned by the context
+    const double* D = nullptr; // owned by the context (LINSTEP)
+    DcDev* dev = nullptr;
+    DcDev* h_dev = nullptr;
+    int* zero_flag = nullptr;
+    cudaGraphExec_t gblock[2] = {nullptr, nullptr};
+    int kernels_per_block = 0;
+    int nchk = 0;
+    int cur = 0;
+    double rtol = 1e-3;
+    int max_outer = 30;
+    DcCounters k;
+    ptd_ctx_base g;
+};
+
+template <int MODEL, bool CHECK>
+static cudaError_t dc_launch_model(const DcArgs& a, int ndim, const LaunchCfg& cfg, cudaStream_t s)
+{
+    if (ndim == 1) {
+        dc1d_kernel<MODEL, CHECK><<<(a.nx + 255) / 256, 256, 0, s>>>(a);
+    } else if (ndim == 2) {
+        const int W = cfg.warps2d;
+        const int tiles = (a.nx - 2 + 30) / 31;
+        dim3 grid((tiles + W - 1) / W, (a.ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);
+        dc2d_kernel<MODEL, CHECK><<<grid, dim3(32, W), 0, s>>>(a, cfg.chunk2d);
+    } else {
+        const int tx = (a.nx - 2 + 30) / 31;
+        dim3 grid(tx, (a.ny - 2 + 14) / 15, (a.nz - 2 + cfg.chunk3d - 1) / cfg.chunk3d);
+        dc3d_kernel<MODEL, CHECK, 16><<<grid, dim3(32, 16), 0, s>>>(a, cfg.chunk3d);
+    }
+    return cudaGetLastError();
+}
+
+static cudaError_t dc_launch(const DcArgs& a, int ndim, int model, bool check, const LaunchCfg& cfg,
+                             cudaStream_t s)
+{
+    switch (model * 2 + (check ? 1 : 0)) {
+    case 0: return dc_launch_model<LIN, false>(a, ndim, cfg, s);
+    case 1: return dc_launch_model<LIN, true>(a, ndim, cfg, s);
+    case 2: return dc_launch_model<LINSTEP, false>(a, ndim, cfg, s);
+    case 3: return dc_launch_model<LINSTEP, true>(a, ndim, cfg, s);
+    case 4: return dc_launch_model<NONLIN, false>(a, ndim, cfg, s);
+    case 5: return dc_launch_model<NONLIN, true>(a, ndim, cfg, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+static void dc_args(const DcState* dc, int parity, const int* done, DcArgs& a)
+{
+    std::memset(&a, 0, sizeof(a));
+    a.nx = dc->g.nx;
+    a.ny = dc->g.ny;
+    a.nz = dc->g.nz;
+    a.sy = dc->g.sy;
+    a.sz = dc->g.sz;
+    a.rdt = (float)dc->dv.rdt;
+    for (int d = 0; d < 3; ++d) a.sig[d] = (float)dc->dv.sig[d];
+    a.c_lin = (float)dc->dv.c_lin;
+    a.e_lin = (float)dc->dv.e_lin;
+    a.f = fparams(dc->dv);
+    a.din = dc->d[parity];
+    a.dout = dc->d[parity ^ 1];
+    for (int d = 0; d < 3; ++d) {
+        a.win[d] = dc->w[d][parity] ? dc->w[d][parity] : dc->w[0][parity];
+        a.wout[d] = dc->w[d][parity ^ 1] ? dc->w[d][parity ^ 1] : dc->w[0][parity ^ 1];
+    }
+    a.Hf = dc->Hf;
+    a.Df = dc->Df;
+    a.r = dc->rf;
+    a.done = done;
+    a.acc = &dc->dev->acc;
+    a.norm_max = dc->p.norm == PTD_NORM_MAX;
+}
+
+#define DCK(call)                                                 \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);       \
+    } while (0)
+
+static int dc_capture(DcState* dc, int parity)
+{
+    cudaGraph_t g = nullptr;
+    DCK(cudaStreamBeginCapture(dc->s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t err = cudaSuccess;
+    int par = parity, nk = 0;
+    for (int it = 0; it < dc->nchk && err == cudaSuccess; ++it) {
+        DcArgs a;
+        dc_args(dc, par, &dc->dev->done, a);
+        err = dc_launch(a, dc->ndim, dc->model, it == dc->nchk - 1, dc->cfg, dc->s);
+        ++nk;
+        par ^= 1;
+    }
+    if (err == cudaSuccess) {
+        dc_inner_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->nchk, dc->p.itmax, dc->dv.norm_den,
+                                                   dc->p.norm == PTD_NORM_MAX);
+        err = cudaGetLastError();
+        ++nk;
+    }
+    cudaError_t e2 = cudaStreamEndCapture(dc->s, &g);
+    if (err != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(err, "capture inner block");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    cudaError_t e3 = cudaGraphInstantiate(&dc->gblock[parity], g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+    dc->kernels_per_block = nk;
+    return PTD_OK;
+}
+
+int dc_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cudaStream_t s, DcState** out)
+{
+    *out = nullptr;
+    DcState* dc = new (std::nothrow) DcState();
+    if (!dc) return set_error(PTD_ENOMEM, "dc_create: host allocation failed");
+    dc->p = p;
+    dc->dv = dv;
+    dc->g = g;
+    dc->s = s;
+    dc->ndim = p.ndim;
+    dc->model = p.model;
+    dc->nfield = g.nfield;
+    dc->cfg = tuned_config(p);
+    dc->nchk = std::max(1, std::min(p.nchk, 50));
+    dc->rtol = p.dc_inner_rtol > 0.0 ? p.dc_inner_rtol : 1e-3;
+    dc->max_outer = p.dc_max_outer > 0 ? p.dc_max_outer : 30;
+    const size_t fb = (size_t)g.nfield * sizeof(float);
+    auto alloc = [&](void** ptr, size_t n) -> int {
+        cudaError_t e = cudaMalloc(ptr, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(e == cudaErrorMemoryAllocation ? PTD_ENOMEM : PTD_ECUDA, "dc: cudaMalloc failed");
+        }
+        return PTD_OK;
+    };
+    int rc = alloc((void**)&dc->d[0], fb);
+    if (!rc) rc = alloc((void**)&dc->d[1], fb);
+    for (int d = 0; d < p.ndim && !rc; ++d)
+        for (int q = 0; q < 2 && !rc; ++q) rc = alloc((void**)&dc->w[d][q], fb);
+    if (!rc) rc = alloc((void**)&dc->Hf, fb);
+    if (!rc) rc = alloc((void**)&dc->rf, fb);
+    if (!rc && p.model == PTD_MODEL_LINSTEP) rc = alloc((void**)&dc->Df, fb);
+    if (!rc) rc = alloc((void**)&dc->dev, sizeof(DcDev));
+    if (!rc) rc = alloc((void**)&dc->zero_flag, sizeof(int));
+    if (!rc && cudaMallocHost((void**)&dc->h_dev, sizeof(DcDev)) != cudaSuccess) {
+        cudaGetLastError();
+        rc = set_error(PTD_ENOMEM, "dc: cudaMallocHost failed");
+    }
+    if (!rc) {
+        cudaError_t e = cudaMemsetAsync(dc->dev, 0, sizeof(DcDev), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dc->zero_flag, 0, sizeof(int), s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "dc: cudaMemsetAsync");
+    }
+    for (int q = 0; q < 2 && !rc; ++q) rc = dc_capture(dc, q);
+    if (rc) {
+        dc_destroy(dc);
+        return rc;
+    }
+    *out = dc;
+    return PTD_OK;
+}
+
+void dc_destroy(DcState* dc)
+{
+    if (!dc) return;
+    if (dc->s) cudaStreamSynchronize(dc->s);
+    for (int q = 0; q < 2; ++q)
+        if (dc->gblock[q]) cudaGraphExecDestroy(dc->gblock[q]);
+    cudaFree(dc->d[0]);
+    cudaFree(dc->d[1]);
+    for (int d = 0; d < 3; ++d)
+        for (int q = 0; q < 2; ++q) cudaFree(dc->w[d][q]);
+    cudaFree(dc->Hf);
+    cudaFree(dc->rf);
+    cudaFree(dc->Df);
+    cudaFree(dc->dev);
+    cudaFree(dc->zero_flag);
+    if (dc->h_dev) cudaFreeHost(dc->h_dev);
+    delete dc;
+}
+
+int dc_set_state(DcState* dc, const ptd_ctx_base&, double* H, double* Hold, const double* D, cudaStream_t s)
+{
+    dc->H = H;
+    dc->Hold = Hold;
+    dc->D = D;
+    const size_t fb = (size_t)dc->nfield * sizeof(float);
+    DCK(cudaMemsetAsync(dc->d[0], 0, fb, s));
+    DCK(cudaMemsetAsync(dc->d[1], 0, fb, s));
+    for (int d = 0; d < 3; ++d)
+        for (int q = 0; q < 2; ++q)
+            if (dc->w[d][q]) DCK(cudaMemsetAsync(dc->w[d][q], 0, fb, s));
+    DCK(cudaMemsetAsync(dc->rf, 0, fb, s));
+    const int nb = 152 * 8;
+    dc_tofloat_kernel<<<nb, 256, 0, s>>>(H, dc->Hf, dc->nfield);
+    DCK(cudaGetLastError());
+    if (dc->Df) {
+        dc_tofloat_kernel<<<nb, 256, 0, s>>>(D, dc->Df, dc->nfield);
+        DCK(cudaGetLastError());
+    }
+    dc->cur = 0;
+    return PTD_OK;
+}
+
+static int dc_residual(DcState* dc, double* err)
+{
+    PTArgs a;
+    fill_args(dc->p, dc->dv, a);
+    a.sy = dc->g.sy;
+    a.sz = dc->g.sz;
+    a.Hin = dc->H;
+    a.Hold = dc->Hold;
+    a.D = dc->D;
+    const int nb = 152 * 8;
+    if (dc->model == LIN) dc_resid64_kernel<LIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
+    else if (dc->model == LINSTEP)
+        dc_resid64_kernel<LINSTEP><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
+    else dc_resid64_kernel<NONLIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
+    DCK(cudaGetLastError());
+    dc_outer_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->dv.norm_den, dc->p.norm == PTD_NORM_MAX, dc->rtol,
+                                              dc->p.tol);
+    DCK(cudaGetLastError());
+    dc->k.launches += 2;
+    DCK(cudaMemcpyAsync(dc->h_dev, dc->dev, sizeof(DcDev), cudaMemcpyDeviceToHost, dc->s));
+    DCK(cudaStreamSynchronize(dc->s));
+    *err = dc->h_dev->outer_err;
+    return PTD_OK;
+}
+
+// Inner FP32 solve of J delta = r from delta = 0; returns its iterations.
+static int dc_inner(DcState* dc, long long budget, int* iters)
+{
+    const size_t fb = (size_t)dc->nfield * sizeof(float);
+    DCK(cudaMemsetAsync(dc->d[0], 0, fb, dc->s));
+    DCK(cudaMemsetAsync(dc->d[1], 0, fb, dc->s));
+    for (int d = 0; d < dc->ndim; ++d) {
+        DCK(cudaMemsetAsync(dc->w[d][0], 0, fb, dc->s));
+        DCK(cudaMemsetAsync(dc->w[d][1], 0, fb, dc->s));
+    }
+    dc->cur = 0;
+    const long long blocks_max = std::max<long long>(1, budget / dc->nchk);
+    long long launched = 0, batch = 1;
+    int done = DONE_RUNNING, iter = 0;
+    while (launched < blocks_max) {
+        const long long nb = std::min(batch, blocks_max - launched);
+        for (long long b = 0; b < nb; ++b) {
+            const int par = (int)(((launched + b) * dc->nchk) & 1);
+            DCK(cudaGraphLaunch(dc->gblock[par], dc->s));
+            dc->k.launches += dc->kernels_per_block;
+        }
+        launched += nb;
+        DCK(cudaMemcpyAsync(dc->h_dev, dc->dev, sizeof(DcDev), cudaMemcpyDeviceToHost, dc->s));
+        DCK(cudaStreamSynchronize(dc->s));
+        done = dc->h_dev->done;
+        iter = dc->h_dev->iter;
+        if (done != DONE_RUNNING) break;
+        batch = std::min<long long>(batch * 2, 32);
+    }
+    dc->cur = iter & 1;
+    dc->k.iterations += iter;
+    *iters = iter;
+    return PTD_OK;
+}
+
+int dc_step(DcState* dc, const ptd_ctx_base& g, int32_t* iters, double* err_hist, int32_t err_cap,
+            int32_t* n_err, int* nan_flag, int* capped)
+{
+    (void)g;
+    long long total = 0;
+    int converged = 0;
+    for (int outer = 0; outer <= dc->max_outer; ++outer) {
+        double err = 0.0;
+        int rc = dc_residual(dc, &err);
+        if (rc) return rc;
+        if (err_hist && *n_err < err_cap) err_hist[*n_err] = err;
+        *n_err += 1;
+        if (err != err) {
+            *nan_flag = 1;
+            break;
+        }
+        if (err <= dc->p.tol) {
+            converged = 1;
+            break;
+        }
+        if (outer == dc->max_outer || total >= dc->p.itmax) break;
+        int it = 0;
+        rc = dc_inner(dc, (long long)dc->p.itmax - total, &it);
+        if (rc) return rc;
+        total += it;
+        dc_apply_kernel<<<152 * 8, 256, 0, dc->s>>>(dc->H, dc->Hf, dc->d[dc->cur], dc->nfield);
+        DCK(cudaGetLastError());
+        dc->k.launches += 1;
+    }
+    *iters = (int32_t)total;
+    if (!converged && !*nan_flag) *capped = 1;
+    const size_t bytes = (size_t)dc->nfield * sizeof(double);
+    DCK(cudaMemcpyAsync(dc->Hold, dc->H, bytes, cudaMemcpyDeviceToDevice, dc->s));
+    DCK(cudaStreamSynchronize(dc->s));
+    return PTD_OK;
+}
+
+int dc_iterate(DcState* dc, const ptd_ctx_base&, int32_t niter)
+{
+    for (int32_t it = 0; it < niter; ++it) {
+        DcArgs a;
+        dc_args(dc, dc->cur, dc->zero_flag, a);
+        DCK(dc_launch(a, dc->ndim, dc->model, false, dc->cfg, dc->s));
+        dc->cur ^= 1;
+        dc->k.launches += 1;
+        dc->k.iterations += 1;
+    }
+    return PTD_OK;
+}
+
+const double* dc_current(const DcState* dc) { return dc->H; }
 DcCounters dc_counters(const DcState* dc) { return dc ? dc->k : DcCounters{}; }
 
 }  // namespace ptd

@@ -31,6 +31,16 @@ enum { LIN = 0, LINSTEP = 1, NONLIN = 2 };
 
 constexpr unsigned FULL = 0xffffffffu;
 
+// FP32 constants of the iteration-parameter formulas.
+struct FParams {
+    float fA;           // L^2/dt
+    float fpi, fpi2;    // pi, pi^2
+    float fk1;          // NONLIN cell: 1/(Vpdtau*L*Resc)
+    float fk2;          // NONLIN face: L*Resc/Vpdtau
+    float fk3;          // LINSTEP cell: Re/(Vpdtau*L)
+    float frdt;         // 1/dt
+};
+
 // Everything a PT-iteration kernel needs, passed by value.
 struct PTArgs {
     int nx, ny, nz;
@@ -40,12 +50,7 @@ struct PTArgs {
     double sig[3];      // kappa / dx_d^2
     double c_lin;       // LIN, LINSTEP: 1/(1+theta)
     double e_lin;       // LIN: dtau/(1+dtau/dt)
-    float fA;           // L^2/dt
-    float fpi, fpi2;    // pi, pi^2
-    float fk1;          // NONLIN cell: 1/(Vpdtau*L*Resc)
-    float fk2;          // NONLIN face: L*Resc/Vpdtau
-    float fk3;          // LINSTEP cell: Re/(Vpdtau*L)
-    float frdt;         // 1/dt
+    FParams f;
     const double* Hin;
     double* Hout;
     const double* Hold;
@@ -103,7 +108,7 @@ __device__ __forceinline__ float fsqrt(float x)
 // NONLIN face: c = 1/(1+theta), theta = L*Resc/(Vpdtau*Re_f),
 // Re_f = pi + sqrt(pi^2 + L^2/(D_f dt)), D_f = ((h_L+h_R)/2)^3
 // (scripts/diff_2D_nonlin.jl:145-151).  D_f -> 0 gives Re_f -> inf, c -> 1.
-__device__ __forceinline__ float nonlin_face_c(const PTArgs& a, float hsum)
+__device__ __forceinline__ float nonlin_face_c(const FParams& a, float hsum)
 {
     float m = 0.5f * hsum;
     float df = m * m * m;
@@ -115,7 +120,7 @@ __device__ __forceinline__ float nonlin_face_c(const PTArgs& a, float hsum)
 // NONLIN cell: e = 1/(1/dtau + 1/dt) with
 // 1/dtau = H^3 Re / (Vpdtau L Resc) = (pi H^3 + sqrt(pi^2 H^6 + L^2 H^3/dt)) * k1
 // (scripts/diff_2D_nonlin.jl:149,152); finite for H^3 -> 0 (e -> dt).
-__device__ __forceinline__ float nonlin_cell_e(const PTArgs& a, float h)
+__device__ __forceinline__ float nonlin_cell_e(const FParams& a, float h)
 {
     float h3 = h * h * h;
     float inv = (a.fpi * h3 + fsqrt(a.fpi2 * h3 * h3 + a.fA * h3)) * a.fk1;
@@ -124,7 +129,7 @@ __device__ __forceinline__ float nonlin_cell_e(const PTArgs& a, float h)
 
 // LINSTEP cell: 1/dtau = maxloc(D) * Re / (Vpdtau L) (compute_iter_params!,
 // scripts/diff_2D_linstep.jl:18-21).
-__device__ __forceinline__ float linstep_cell_e(const PTArgs& a, float dmax)
+__device__ __forceinline__ float linstep_cell_e(const FParams& a, float dmax)
 {
     return frcp(dmax * a.fk3 + a.frdt);
 }
@@ -147,7 +152,7 @@ __device__ __forceinline__ double face_update(const PTArgs& a, double HL, double
     } else {
         double s = HL + HR;
         K = s * s * s;
-        c = f2d_bits(nonlin_face_c(a, hsum));
+        c = f2d_bits(nonlin_face_c(a.f, hsum));
     }
     if (U) u = K * g;
     return fma(-c, fma(K, g, w), w);
@@ -170,9 +175,9 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
     return v;
 }
 
-// Block-wide residual reduction into a.acc (sum of squares, or max |R| as the
+// Block-wide residual reduction into acc (sum of squares, or max |R| as the
 // ordered bit pattern of a non-negative double; NaN orders above +inf).
-__device__ __forceinline__ void block_reduce_residual(const PTArgs& a, double part_sum,
+__device__ __forceinline__ void block_reduce_residual(double* acc, int norm_max, double part_sum,
                                                       unsigned long long part_max)
 {
     __shared__ double s_sum[32];
@@ -181,7 +186,7 @@ __device__ __forceinline__ void block_reduce_residual(const PTArgs& a, double pa
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int wid = tid >> 5, ln = tid & 31;
     const int nw = (nthr + 31) >> 5;
-    if (a.norm_max) {
+    if (norm_max) {
         part_max = warp_max_u64(part_max);
         if (ln == 0) s_max[wid] = part_max;
     } else {
@@ -190,16 +195,22 @@ __device__ __forceinline__ void block_reduce_residual(const PTArgs& a, double pa
     }
     __syncthreads();
     if (wid == 0) {
-        if (a.norm_max) {
+        if (norm_max) {
             unsigned long long v = ln < nw ? s_max[ln] : 0ull;
             v = warp_max_u64(v);
-            if (ln == 0 && v) atomicMax(reinterpret_cast<unsigned long long*>(a.acc), v);
+            if (ln == 0 && v) atomicMax(reinterpret_cast<unsigned long long*>(acc), v);
         } else {
             double v = ln < nw ? s_sum[ln] : 0.0;
             v = warp_sum(v);
-            if (ln == 0) atomicAdd(a.acc, v);
+            if (ln == 0) atomicAdd(acc, v);
         }
     }
+}
+
+__device__ __forceinline__ void block_reduce_residual(const PTArgs& a, double part_sum,
+                                                      unsigned long long part_max)
+{
+    block_reduce_residual(a.acc, a.norm_max, part_sum, part_max);
 }
 
 __device__ __forceinline__ void accumulate_residual(double r, double& sum, unsigned long long& mx)

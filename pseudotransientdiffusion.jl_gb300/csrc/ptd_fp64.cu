@@ -61,9 +61,9 @@ __global__ void __launch_bounds__(256) pt1d_kernel(PTArgs a)
                 e = a.e_lin;
             } else if (MODEL == LINSTEP) {
                 const float dmax = fmaxf(fmaxf(d2f_bits(Dl), d2f_bits(Dr)), d2f_bits(Dc));
-                e = f2d_bits(linstep_cell_e(a, dmax));
+                e = f2d_bits(linstep_cell_e(a.f, dmax));
             } else {
-                e = f2d_bits(nonlin_cell_e(a, hc));
+                e = f2d_bits(nonlin_cell_e(a.f, hc));
             }
             const double Hn = fma(-e, fma(Hc - Ho, a.rdt, div), Hc);
             a.Hout[i] = Hn;
@@ -149,9 +149,9 @@ __global__ void __launch_bounds__(256) pt2d_kernel(PTArgs a, int chunk)
                 } else if (MODEL == LINSTEP) {
                     const float dmax =
                         fmaxf(fmaxf(fmaxf(dcf, dlf), fmaxf(d2f_bits(Dr), dbf)), dnf);
-                    e = f2d_bits(linstep_cell_e(a, dmax));
+                    e = f2d_bits(linstep_cell_e(a.f, dmax));
                 } else {
-                    e = f2d_bits(nonlin_cell_e(a, hc));
+                    e = f2d_bits(nonlin_cell_e(a.f, hc));
                 }
                 const double div = fma(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]);
                 const double Hnew = fma(-e, fma(Hc - Ho, a.rdt, div), Hc);
@@ -302,9 +302,9 @@ __global__ void __launch_bounds__(32 * R) pt3d_kernel(PTArgs a, int chunk)
                 } else if (MODEL == LINSTEP) {
                     const float dmax = fmaxf(fmaxf(fmaxf(dcf, dlf), fmaxf(d2f_bits(Dr), duf)),
                                              fmaxf(fmaxf(ddf, dbf), dnf));
-                    e = f2d_bits(linstep_cell_e(a, dmax));
+                    e = f2d_bits(linstep_cell_e(a.f, dmax));
                 } else {
-                    e = f2d_bits(nonlin_cell_e(a, hc));
+                    e = f2d_bits(nonlin_cell_e(a.f, hc));
                 }
                 const double div =
                     fma(wzn - wzb, a.sig[2], fma(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]));

@@ -1,0 +1,63 @@
+"""FP32 PT iterations inside the FP64 defect-correction loop (precision
+FP32_DC): the result must match the FP64 oracle to a relative L2 error of
+1e-8 or better, with every step converged to tol in the FP64 residual."""
+import numpy as np
+import pytest
+
+import ptdiff
+from oracle import oracle as O
+from ptdiff import _abi
+from ptdiff import scripts as S
+
+pytestmark = pytest.mark.gpu
+RTOL_DC = 1e-8
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def run_dc(s, shape, **kw):
+    H = S.initial_condition(s, *shape)
+    D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
+    p = ptdiff.make_params(s, shape, precision="fp32_dc", **kw)
+    with ptdiff.Solver(p) as sol:
+        iters, eh, st = sol.solve(H, D)
+    return H, D, iters, eh, st
+
+
+@pytest.mark.parametrize("name,shape", [
+    ("diff_1D_lin", (128,)), ("diff_1D_linstep", (128,)), ("diff_1D_nonlin", (128,)),
+    ("diff_2D_lin", (64, 64)), ("diff_2D_linstep", (64, 64)), ("diff_2D_nonlin", (64, 64)),
+    ("diff_2D_nonlin", (97, 130)), ("diff_3D_lin_multixpu", (32, 32, 32)),
+    ("diff_3D_linstep_multixpu", (32, 32, 32)), ("diff_3D_nonlin_multixpu", (32, 30, 34)),
+])
+def test_dc_matches_fp64_oracle(name, shape):
+    s = S.SCRIPTS[name]
+    H, D, iters, eh, st = run_dc(s, shape)
+    H0 = S.initial_condition(s, *shape)
+    Hr, _, _, st_r = O.solve(s, H0, D)
+    assert st == 0 and st_r == 0
+    assert rel_l2(H, Hr) <= RTOL_DC
+    assert len(eh) >= s.nt and eh[-1] <= s.tol
+    assert (iters > 0).all()
+
+
+@pytest.mark.parametrize("name,shape", [("1d_lin_512", (512,)), ("2d_nonlin_4096", (256, 256)),
+                                        ("3d_nonlin_512", (40, 40, 40))])
+def test_dc_benchmark_problems(name, shape):
+    s = S.CONFIGS[name]
+    H, _, iters, eh, st = run_dc(s, shape)
+    Hr, _, _, st_r = O.solve(s, S.initial_condition(s, *shape))
+    assert st == 0 and st_r == 0
+    assert rel_l2(H, Hr) <= RTOL_DC
+
+
+def test_dc_nan_input():
+    s = S.SCRIPTS["diff_2D_nonlin"]
+    H0 = S.initial_condition(s, 40, 40)
+    H0[20, 20] = np.nan
+    p = ptdiff.make_params(s, (40, 40), precision="fp32_dc")
+    with ptdiff.Solver(p) as sol:
+        _, _, st = sol.solve(H0, raise_on_nan=False)
+    assert st == _abi.PTD_ENAN
