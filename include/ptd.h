@@ -60,10 +60,15 @@ typedef enum ptd_status {
  *  NONLIN   D = H^3 (face: (avg H)^3)     scripts/diff_{1D,2D}_nonlin.jl, diff_3D_nonlin_multixpu.jl */
 enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2 };
 
-/* Arithmetic of the PT iterations.  FP64: every PT iteration in FP64 (the
- * reference's form).  FP32_DC: FP32 PT iterations on a correction inside an
- * FP64 defect-correction loop (residual, norm and H update in FP64). */
-enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1 };
+/* Arithmetic of the PT iterations.
+ *  FP64     every PT iteration in native FP64 (the reference's form).
+ *  FP32_DC  FP32 PT iterations on a correction inside an FP64
+ *           defect-correction loop (residual, norm and H update in FP64).
+ *  DF64     the FP64 form with every value held as a double-float (two
+ *           FP32 numbers, ~48-bit significand, 8 bytes like a double) and
+ *           computed on the FP32 pipe; same iterations and iteration counts
+ *           as FP64, H within ~1e-13 relative of it. */
+enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2 };
 
 /* Residual used for the stopping test.  MIXED is the reference's: the
  * undamped flux from the H the fluxes of that iteration were computed on, the
@@ -95,8 +100,8 @@ typedef struct ptd_params {
     int32_t norm;        /* PTD_NORM_* */
     double norm_len;     /* RMS divisor; <= 0 means the number of inner cells */
     int32_t flags;       /* PTD_FLAG_* */
-    int32_t dc_max_outer;/* FP32_DC: outer FP64 corrections per step cap (0: default) */
-    double dc_inner_rtol;/* FP32_DC: inner FP32 solve relative tolerance (0: default) */
+    int32_t dc_max_outer;/* FP32_DC: outer FP64 corrections per step cap (0: default 30) */
+    double dc_inner_rtol;/* FP32_DC: inner FP32 solve relative tolerance (0: default 1e-2) */
     int32_t reserved[8]; /* zero */
 } ptd_params;
 

@@ -25,6 +25,7 @@
 
 #include "../../include/ptd.h"
 #include "ptd_internal.h"
+#include "ptd_num.cuh"
 
 using namespace ptd;
 
@@ -138,7 +139,7 @@ int ptd::validate(const ptd_params* p)
     if (!(p->resc > 0.0) || !std::isfinite(p->resc)) return fail(PTD_EINVAL, "resc must be > 0");
     if (p->model != PTD_MODEL_NONLIN && (!(p->D > 0.0) || !std::isfinite(p->D)))
         return fail(PTD_EINVAL, "D must be > 0");
-    if (p->precision != PTD_PREC_FP64 && p->precision != PTD_PREC_FP32_DC)
+    if (p->precision != PTD_PREC_FP64 && p->precision != PTD_PREC_FP32_DC && p->precision != PTD_PREC_DF64)
         return fail(PTD_EINVAL, "unknown precision %d", p->precision);
     if (p->resid_mode != PTD_RESID_MIXED && p->resid_mode != PTD_RESID_CONSISTENT)
         return fail(PTD_EINVAL, "unknown resid_mode %d", p->resid_mode);
@@ -216,8 +217,10 @@ void ptd::fill_args(const ptd_params& p, const Derived& dv, PTArgs& a)
     a.nz = p.nz;
     a.rdt = dv.rdt;
     for (int d = 0; d < 3; ++d) a.sig[d] = dv.sig[d];
-    a.c_lin = dv.c_lin;
-    a.e_lin = dv.e_lin;
+    a.rdt_df = split_df(dv.rdt);
+    for (int d = 0; d < 3; ++d) a.sig_df[d] = split_df(dv.sig[d]);
+    a.fc_lin = (float)dv.c_lin;
+    a.fe_lin = (float)dv.e_lin;
     a.f = fparams(dv);
     a.norm_max = p.norm == PTD_NORM_MAX;
 }
@@ -262,6 +265,8 @@ struct ptd_ctx : ptd_ctx_base {
     long long launches = 0, iterations = 0;
     int kernels_per_block = 0;
     DcState* dc = nullptr;        // FP32 defect-correction resources
+    bool df64 = false;            // fields hold double-floats (PTD_PREC_DF64)
+    double* stage = nullptr;      // DF64: FP64 staging field for the host boundary
 };
 
 static void args_for(const ptd_ctx* c, int parity, const int* done, PTArgs& a)
@@ -294,11 +299,11 @@ static int capture_block(ptd_ctx* c, int parity, cudaGraphExec_t* out)
         args_for(c, par, &c->st->done, a);
         const bool check = it == nchk - 1;
         if (check && c->p.resid_mode == PTD_RESID_CONSISTENT) {
-            err = launch_pt_fp64(a, c->p.ndim, c->p.model, false, c->cfg, c->stream);
-            if (err == cudaSuccess) err = launch_resid_consistent(a, c->p.ndim, c->p.model, c->stream);
+            err = launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream);
+            if (err == cudaSuccess) err = launch_resid_consistent(a, c->p.ndim, c->p.model, c->df64, c->stream);
             nk += 2;
         } else {
-            err = launch_pt_fp64(a, c->p.ndim, c->p.model, check, c->cfg, c->stream);
+            err = launch_pt(a, c->p.ndim, c->p.model, check, c->df64, c->cfg, c->stream);
             nk += 1;
         }
         par ^= 1;
@@ -329,7 +334,7 @@ static int capture_plain(ptd_ctx* c, int parity, cudaGraphExec_t* out)
     for (int it = 0; it < c->plain_len && err == cudaSuccess; ++it) {
         PTArgs a;
         args_for(c, par, c->zero_flag, a);
-        err = launch_pt_fp64(a, c->p.ndim, c->p.model, false, c->cfg, c->stream);
+        err = launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream);
         par ^= 1;
     }
     cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
@@ -362,6 +367,7 @@ static void free_ctx(ptd_ctx* c)
     cudaFree(c->st);
     cudaFree(c->zero_flag);
     cudaFree(c->errhist);
+    cudaFree(c->stage);
     if (c->h_st) cudaFreeHost(c->h_st);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -384,6 +390,7 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
     c->sz = c->sy * p->ny;
     c->nfield = c->sz * p->nz;
     c->cfg = tuned_config(*p);
+    c->df64 = p->precision == PTD_PREC_DF64;
     const size_t bytes = (size_t)c->nfield * sizeof(double);
     auto alloc = [&](void** ptr, size_t n) -> int {
         cudaError_t e = cudaMalloc(ptr, n);
@@ -405,6 +412,7 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
     for (int d = 0; d < p->ndim && !rc; ++d)
         for (int q = 0; q < 2 && !rc; ++q) rc = alloc((void**)&c->W[d][q], bytes);
     if (!rc && p->model == PTD_MODEL_LINSTEP) rc = alloc((void**)&c->D, bytes);
+    if (!rc && c->df64) rc = alloc((void**)&c->stage, bytes);
     if (!rc) rc = alloc((void**)&c->st, sizeof(DevState));
     if (!rc) rc = alloc((void**)&c->zero_flag, sizeof(int));
     c->errcap = (p->nchk <= p->itmax ? p->itmax / p->nchk : 0) + 2;
@@ -475,18 +483,28 @@ extern "C" int ptd_set_state(ptd_ctx* c, const double* H, const double* D)
     if (c->p.model == PTD_MODEL_LINSTEP && !D) return fail(PTD_EINVAL, "the step model needs D");
     const size_t bytes = (size_t)c->nfield * sizeof(double);
     // padding stays zero: clear whole buffers first
-    CK(cudaMemsetAsync(c->H[0], 0, bytes, c->stream));
-    int rc = copy_field_in(*c, c->H[0], H, c->stream);
+    double* Hdst = c->df64 ? c->stage : c->H[0];
+    CK(cudaMemsetAsync(Hdst, 0, bytes, c->stream));
+    int rc = copy_field_in(*c, Hdst, H, c->stream);
     if (rc) return rc;
+    if (c->df64) {
+        CK(launch_to_df64(c->stage, c->H[0], c->nfield, c->stream));
+        c->launches += 1;
+    }
     CK(cudaMemcpyAsync(c->H[1], c->H[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaMemcpyAsync(c->Hold, c->H[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
     for (int d = 0; d < 3; ++d)
         for (int q = 0; q < 2; ++q)
             if (c->W[d][q]) CK(cudaMemsetAsync(c->W[d][q], 0, bytes, c->stream));
     if (c->p.model == PTD_MODEL_LINSTEP) {
-        CK(cudaMemsetAsync(c->D, 0, bytes, c->stream));
-        rc = copy_field_in(*c, c->D, D, c->stream);
+        double* Ddst = c->df64 ? c->stage : c->D;
+        CK(cudaMemsetAsync(Ddst, 0, bytes, c->stream));
+        rc = copy_field_in(*c, Ddst, D, c->stream);
         if (rc) return rc;
+        if (c->df64) {
+            CK(launch_to_df64(c->stage, c->D, c->nfield, c->stream));
+            c->launches += 1;
+        }
     }
     c->cur = 0;
     if (c->dc) {
@@ -504,6 +522,11 @@ extern "C" int ptd_get_state(ptd_ctx* c, double* H)
     if (!H) return fail(PTD_EINVAL, "H is NULL");
     if (!c->have_state) return fail(PTD_ESTATE, "no state set");
     const double* src = c->dc ? dc_current(c->dc) : c->H[c->cur];
+    if (c->df64) {
+        CK(launch_from_df64(src, c->stage, c->nfield, c->stream));
+        c->launches += 1;
+        src = c->stage;
+    }
     int rc = copy_field_out(*c, H, src, c->stream);
     if (rc) return rc;
     CK(cudaStreamSynchronize(c->stream));
@@ -523,7 +546,7 @@ static int run_plain(ptd_ctx* c, long long n)
     for (; n > 0; --n) {
         PTArgs a;
         args_for(c, c->cur, c->zero_flag, a);
-        CK(launch_pt_fp64(a, c->p.ndim, c->p.model, false, c->cfg, c->stream));
+        CK(launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream));
         c->launches += 1;
         c->iterations += 1;
         c->cur ^= 1;

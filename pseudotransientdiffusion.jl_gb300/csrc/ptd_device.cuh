@@ -41,22 +41,25 @@ struct FParams {
     float frdt;         // 1/dt
 };
 
-// Everything a PT-iteration kernel needs, passed by value.
+// Everything a PT-iteration kernel needs, passed by value.  Field pointers
+// are untyped: the kernels read them as double (F64) or float2 (DF64).
 struct PTArgs {
     int nx, ny, nz;
     long long sy;       // elements between consecutive y rows (row pitch)
     long long sz;       // elements between consecutive z planes
     double rdt;         // 1/dt
     double sig[3];      // kappa / dx_d^2
-    double c_lin;       // LIN, LINSTEP: 1/(1+theta)
-    double e_lin;       // LIN: dtau/(1+dtau/dt)
+    float2 rdt_df;      // the same constants as double-floats
+    float2 sig_df[3];
+    float fc_lin;       // LIN, LINSTEP: 1/(1+theta)
+    float fe_lin;       // LIN: dtau/(1+dtau/dt)
     FParams f;
-    const double* Hin;
-    double* Hout;
-    const double* Hold;
-    const double* win[3];
-    double* wout[3];
-    const double* D;    // LINSTEP cell diffusivity
+    const void* Hin;
+    void* Hout;
+    const void* Hold;
+    const void* win[3];
+    void* wout[3];
+    const void* D;      // LINSTEP cell diffusivity
     const int* done;    // nonzero: the step has stopped, skip the iteration
     double* acc;        // residual accumulator: sum R^2 (RMS) or max |R| bits (MAX)
     int norm_max;
@@ -132,30 +135,6 @@ __device__ __forceinline__ float nonlin_cell_e(const FParams& a, float h)
 __device__ __forceinline__ float linstep_cell_e(const FParams& a, float dmax)
 {
     return frcp(dmax * a.fk3 + a.frdt);
-}
-
-// One face: returns the new scaled flux; u = K_f * g (the undamped flux of
-// the residual, same scaling) when U is requested.
-template <int MODEL, bool U>
-__device__ __forceinline__ double face_update(const PTArgs& a, double HL, double HR, float hsum,
-                                              double DL, double DR, double w, double& u)
-{
-    double g = HR - HL;
-    double K, c;
-    if (MODEL == LIN) {
-        c = a.c_lin;
-        if (U) u = g;
-        return fma(-c, g + w, w);
-    } else if (MODEL == LINSTEP) {
-        K = DL + DR;
-        c = a.c_lin;
-    } else {
-        double s = HL + HR;
-        K = s * s * s;
-        c = f2d_bits(nonlin_face_c(a.f, hsum));
-    }
-    if (U) u = K * g;
-    return fma(-c, fma(K, g, w), w);
 }
 
 __device__ __forceinline__ double warp_sum(double v)

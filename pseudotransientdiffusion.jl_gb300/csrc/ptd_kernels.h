@@ -31,9 +31,11 @@ struct LaunchCfg {
     int rows3d = 16;    // warps (y rows) per 3D block (8 or 16)
 };
 
-cudaError_t launch_pt_fp64(const PTArgs& a, int ndim, int model, bool check, const LaunchCfg& cfg,
-                           cudaStream_t s);
-cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, cudaStream_t s);
+cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, bool df64, const LaunchCfg& cfg,
+                      cudaStream_t s);
+cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, bool df64, cudaStream_t s);
+cudaError_t launch_to_df64(const double* src, void* dst, long long n, cudaStream_t s);
+cudaError_t launch_from_df64(const void* src, double* dst, long long n, cudaStream_t s);
 cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
                          double norm_den, int norm_max, cudaStream_t s);
 cudaError_t launch_reset_state(DevState* st, cudaStream_t s);

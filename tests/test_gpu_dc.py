@@ -1,6 +1,11 @@
 """FP32 PT iterations inside the FP64 defect-correction loop (precision
-FP32_DC): the result must match the FP64 oracle to a relative L2 error of
-1e-8 or better, with every step converged to tol in the FP64 residual."""
+FP32_DC).  Every step must end with the FP64 residual <= tol.  Against the FP64
+oracle the bar is a relative L2 error of 1e-8 on the benchmark problems
+(H0 = 1 + exp(-r^2), ||H|| ~ 1).  On the reference's own initial condition
+exp(-r^2) ||H|| is ~0.1, and two solutions each converged to an RMS residual of
+tol = 1e-8 differ by up to ~dt*tol/||H||_rms ~ 2e-8 relative whatever the
+arithmetic, so there the bar is 5e-8 against the oracle and 1e-8 against a
+tightly converged (tol 1e-11) oracle solution."""
 import numpy as np
 import pytest
 
@@ -11,6 +16,7 @@ from ptdiff import scripts as S
 
 pytestmark = pytest.mark.gpu
 RTOL_DC = 1e-8
+RTOL_DC_REFIC = 5e-8
 
 
 def rel_l2(a, b):
@@ -37,8 +43,10 @@ def test_dc_matches_fp64_oracle(name, shape):
     H, D, iters, eh, st = run_dc(s, shape)
     H0 = S.initial_condition(s, *shape)
     Hr, _, _, st_r = O.solve(s, H0, D)
+    Ht, _, _, _ = O.solve(s.with_(tol=1e-11), H0, D)
     assert st == 0 and st_r == 0
-    assert rel_l2(H, Hr) <= RTOL_DC
+    assert rel_l2(H, Hr) <= RTOL_DC_REFIC
+    assert rel_l2(H, Ht) <= RTOL_DC
     assert len(eh) >= s.nt and eh[-1] <= s.tol
     assert (iters > 0).all()
 
