@@ -101,7 +101,7 @@ typedef struct ptd_params {
     double norm_len;     /* RMS divisor; <= 0 means the number of inner cells */
     int32_t flags;       /* PTD_FLAG_* */
     int32_t dc_max_outer;/* FP32_DC: outer FP64 corrections per step cap (0: default 30) */
-    double dc_inner_rtol;/* FP32_DC: inner FP32 solve relative tolerance (0: default 1e-2) */
+    double dc_inner_rtol;/* FP32_DC: smallest inner relative tolerance (0: default 1e-3) */
     int32_t reserved[8]; /* zero */
 } ptd_params;
 

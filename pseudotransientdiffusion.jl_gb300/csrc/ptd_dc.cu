@@ -359,12 +359,12 @@ __global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, flo
     block_reduce_residual(acc, a.norm_max, part, pmax);
 }
 
-// H += delta on every cell (delta is zero on the boundary); refresh the FP32 copy.
-__global__ void dc_apply_kernel(double* H, float* Hf, const float* delta, long long n)
+// H += a * delta on every cell (delta is zero on the boundary); refresh the FP32 copy.
+__global__ void dc_apply_kernel(double* H, float* Hf, const float* delta, double a, long long n)
 {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
          t += (long long)gridDim.x * blockDim.x) {
-        const double h = H[t] + (double)delta[t];
+        const double h = fma(a, (double)delta[t], H[t]);
         H[t] = h;
         Hf[t] = __double2float_rn(h);
     }
@@ -395,7 +395,7 @@ __global__ void dc_outer_judge_kernel(DcDev* st, double norm_den, int norm_max, 
     st->best = err;
 }
 
-__global__ void dc_inner_judge_kernel(DcDev* st, int nchk, int itmax, double norm_den, int norm_max)
+__global__ void dc_inner_judge_kernel(DcDev* st, int nchk, int itmax, double norm_den, int norm_max, int stall)
 {
     if (st->done) return;
     const double acc = st->acc;
@@ -410,10 +410,12 @@ __global__ void dc_inner_judge_kernel(DcDev* st, int nchk, int itmax, double nor
     }
     if (!(err > st->target)) st->done = (err != err) ? DONE_NAN : DONE_CONVERGED;
     else if (st->iter + nchk > itmax) st->done = DONE_CAP;
-    // FP32 attainable accuracy reached: the inner residual has stopped
-    // decreasing (no 5% gain over the last `stall` checks); the outer FP64
+    // FP32 attainable accuracy reached (about eps_32 * cond(J)): the inner
+    // residual has stopped decreasing (no 5% gain over the last `stall`
+    // checks, a window that grows with the grid so that the PT transient of
+    // a large grid is not mistaken for stagnation); the FP64 outer
     // correction takes over from here.
-    else if (st->nchecks - st->best_at >= 6) st->done = DONE_CONVERGED;
+    else if (st->nchecks - st->best_at >= stall) st->done = DONE_CONVERGED;
 }
 
 // ---------------------------------------------------------------------------
@@ -441,6 +443,7 @@ struct DcState {
     int cur = 0;
     double rtol = 1e-3;
     int max_outer = 30;
+    int stall = 6;             // inner stagnation window, in checks
     DcCounters k;
     ptd_ctx_base g;
 };
@@ -525,7 +528,7 @@ static int dc_capture(DcState* dc, int parity)
     }
     if (err == cudaSuccess) {
         dc_inner_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->nchk, dc->p.itmax, dc->dv.norm_den,
-                                                   dc->p.norm == PTD_NORM_MAX);
+                                                   dc->p.norm == PTD_NORM_MAX, dc->stall);
         err = cudaGetLastError();
         ++nk;
     }
@@ -556,8 +559,12 @@ int dc_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     dc->nfield = g.nfield;
     dc->cfg = tuned_config(p);
     dc->nchk = std::max(1, std::min(p.nchk, 50));
-    dc->rtol = p.dc_inner_rtol > 0.0 ? p.dc_inner_rtol : 1e-2;
+    dc->rtol = p.dc_inner_rtol > 0.0 ? p.dc_inner_rtol : 1e-3;
     dc->max_outer = p.dc_max_outer > 0 ? p.dc_max_outer : 30;
+    {
+        const int nmax = std::max(p.nx, std::max(p.ny, p.nz));
+        dc->stall = std::max(6, (nmax / 2 + dc->nchk - 1) / dc->nchk);
+    }
     const size_t fb = (size_t)g.nfield * sizeof(float);
     auto alloc = [&](void** ptr, size_t n) -> int {
         cudaError_t e = cudaMalloc(ptr, n);
@@ -636,7 +643,7 @@ int dc_set_state(DcState* dc, const ptd_ctx_base&, double* H, double* Hold, cons
     return PTD_OK;
 }
 
-static int dc_residual(DcState* dc, double* err)
+static int dc_residual(DcState* dc, double eta, double* err)
 {
     PTArgs a;
     fill_args(dc->p, dc->dv, a);
@@ -651,7 +658,7 @@ static int dc_residual(DcState* dc, double* err)
         dc_resid64_kernel<LINSTEP><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
     else dc_resid64_kernel<NONLIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
     DCK(cudaGetLastError());
-    dc_outer_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->dv.norm_den, dc->p.norm == PTD_NORM_MAX, dc->rtol,
+    dc_outer_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->dv.norm_den, dc->p.norm == PTD_NORM_MAX, eta,
                                               dc->p.tol);
     DCK(cudaGetLastError());
     dc->k.launches += 2;
@@ -696,35 +703,65 @@ static int dc_inner(DcState* dc, long long budget, int* iters)
     return PTD_OK;
 }
 
+static int dc_apply(DcState* dc, double a)
+{
+    dc_apply_kernel<<<152 * 8, 256, 0, dc->s>>>(dc->H, dc->Hf, dc->d[dc->cur], a, dc->nfield);
+    DCK(cudaGetLastError());
+    dc->k.launches += 1;
+    return PTD_OK;
+}
+
+// One physical step: inexact Newton in FP64 around FP32 PT inner solves.
+// Forcing term (inner relative tolerance) eta: 0.1 on the first correction,
+// then Eisenstat-Walker 0.9*(err_k/err_{k-1})^2 clamped to [dc_inner_rtol, 0.5];
+// a correction that does not lower the FP64 residual is halved (at most 4 times).
 int dc_step(DcState* dc, const ptd_ctx_base& g, int32_t* iters, double* err_hist, int32_t err_cap,
             int32_t* n_err, int* nan_flag, int* capped)
 {
     (void)g;
     long long total = 0;
     int converged = 0;
-    for (int outer = 0; outer <= dc->max_outer; ++outer) {
-        double err = 0.0;
-        int rc = dc_residual(dc, &err);
-        if (rc) return rc;
+    double err_prev = -1.0, eta = 0.1;
+    int outer = 0;
+    double err = 0.0;
+    int rc = dc_residual(dc, eta, &err);
+    if (rc) return rc;
+    while (true) {
         if (err_hist && *n_err < err_cap) err_hist[*n_err] = err;
         *n_err += 1;
-        if (err != err) {
-            *nan_flag = 1;
-            break;
-        }
         if (err <= dc->p.tol) {
             converged = 1;
             break;
         }
-        if (outer == dc->max_outer || total >= dc->p.itmax) break;
+        if (outer >= dc->max_outer || total >= dc->p.itmax || err != err) break;
+        if (err_prev > 0.0) eta = std::min(0.5, std::max(dc->rtol, 0.9 * (err / err_prev) * (err / err_prev)));
+        // dc_residual left r and the inner target for this eta in place
+        if (err_prev > 0.0) {
+            rc = dc_residual(dc, eta, &err);
+            if (rc) return rc;
+        }
         int it = 0;
         rc = dc_inner(dc, (long long)dc->p.itmax - total, &it);
         if (rc) return rc;
         total += it;
-        dc_apply_kernel<<<152 * 8, 256, 0, dc->s>>>(dc->H, dc->Hf, dc->d[dc->cur], dc->nfield);
-        DCK(cudaGetLastError());
-        dc->k.launches += 1;
+        rc = dc_apply(dc, 1.0);
+        if (rc) return rc;
+        double err_new = 0.0;
+        rc = dc_residual(dc, eta, &err_new);
+        if (rc) return rc;
+        double a = 1.0;
+        for (int h = 0; h < 4 && !(err_new < err); ++h) {   // also catches NaN
+            rc = dc_apply(dc, -0.5 * a);
+            if (rc) return rc;
+            a *= 0.5;
+            rc = dc_residual(dc, eta, &err_new);
+            if (rc) return rc;
+        }
+        err_prev = err;
+        err = err_new;
+        ++outer;
     }
+    if (err != err) *nan_flag = 1;
     *iters = (int32_t)total;
     if (!converged && !*nan_flag) *capped = 1;
     const size_t bytes = (size_t)dc->nfield * sizeof(double);
