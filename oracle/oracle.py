@@ -53,6 +53,8 @@ def lib():
         L.ora_iterate.restype = C.c_int
         L.ora_residual_norm.argtypes = [C.POINTER(OraParams), dp, dp, dp, dp]
         L.ora_residual_norm.restype = C.c_double
+        L.ora_adjoint.argtypes = [C.POINTER(OraParams), dp, dp, dp, dp, dp, C.c_double]
+        L.ora_adjoint.restype = C.c_int
         _lib = L
     return _lib
 
@@ -106,3 +108,34 @@ def residual_norm(script, H, Hold, Hpre=None, D=None, norm=0):
     return lib().ora_residual_norm(C.byref(p), _dptr(np.asfortranarray(H)),
                                    _dptr(np.asfortranarray(Hold)),
                                    _dptr(None if Hpre is None else np.asfortranarray(Hpre)), _dptr(Dv))
+
+
+def forward_checkpoints(script, H0, m=None, *, nt=None, tol=None, itmax=None, nthreads=0):
+    """H^0..H^nt of nt implicit steps, each solved from the previous state
+    (fluxes restarted at every step).  Returns an array (nt+1, *H0.shape)."""
+    s = script if tol is None else script.with_(tol=tol)
+    nt = s.nt if nt is None else nt
+    Hs = [np.array(H0, dtype=np.float64, order="F")]
+    for _ in range(nt):
+        H, _, _, st = solve(s, Hs[-1], m, nt=1, itmax=itmax, nthreads=nthreads)
+        if st:
+            raise RuntimeError(f"oracle forward failed ({st})")
+        Hs.append(H)
+    return np.stack(Hs)
+
+
+def adjoint(script, Hs, Ht, m=None, rtol=1e-12, nthreads=0):
+    """CPU FP64 reference adjoint: (grad_m, grad_H0) of 1/2 sum_inner (H^nt - Ht)^2."""
+    shape = Hs.shape[1:]
+    nt = Hs.shape[0] - 1
+    p = params(script, shape, nt=nt, nthreads=nthreads)
+    Hcat = np.concatenate([np.ravel(h, order="F") for h in Hs])
+    gm = np.zeros(int(np.prod(shape)))
+    gh = np.zeros(int(np.prod(shape)))
+    mv = None if m is None else np.ravel(np.asarray(m, dtype=np.float64), order="F").copy()
+    htv = np.ravel(np.asarray(Ht, dtype=np.float64), order="F").copy()
+    st = lib().ora_adjoint(C.byref(p), _dptr(Hcat), _dptr(mv), _dptr(htv),
+                           _dptr(gm) if m is not None else None, _dptr(gh), rtol)
+    if st == 1:
+        raise RuntimeError("ora_adjoint: bad arguments")
+    return gm.reshape(shape, order="F"), gh.reshape(shape, order="F"), st

@@ -61,7 +61,7 @@ static int setup(octx* c, const ora_params* p)
 {
     memset(c, 0, sizeof(*c));
     c->p = p;
-    if (!p || p->ndim < 1 || p->ndim > 3 || p->model < 0 || p->model > 2) return 1;
+    if (!p || p->ndim < 1 || p->ndim > 3 || p->model < 0 || p->model > 3) return 1;
     c->ndim = p->ndim;
     c->n[0] = p->nx;
     c->n[1] = p->ndim > 1 ? p->ny : 1;
@@ -85,7 +85,7 @@ static int setup(octx* c, const ora_params* p)
     c->pi = 3.141592653589793;
     c->pipi = c->pi * c->pi;
     c->rdt = 1.0 / p->dt;
-    if (p->model != 2) {
+    if (p->model < 2) {
         /* Re = pi + sqrt(pi^2 + (L^2 / D / dt)) -- diff_2D_lin.jl:152, diff_2D_linstep.jl:70 */
         c->re = c->pi + sqrt(c->pipi + ((c->L2 / p->D) / p->dt));
         c->theta = (c->L / c->vpdt) / c->re;
@@ -118,6 +118,7 @@ static inline void face_coef(const octx* c, const double* H, const double* Df, l
     if (p->model == 1) { *Dface = (Df[i] + Df[ir]) * 0.5; *th = c->theta; return; }
     double a = (H[i] + H[ir]) * 0.5;
     double d3 = a * a * a;
+    if (p->model == 3) d3 = ((Df[i] + Df[ir]) * 0.5) * d3;   /* Df holds exp(m) */
     double re = p->recip ? c->pi + sqrt(c->pipi + (c->L2 / d3) * c->rdt)
                          : c->pi + sqrt(c->pipi + (c->L2 / d3) / p->dt);
     *Dface = d3;
@@ -177,6 +178,14 @@ static void inner_range(const octx* c, long lo[3], long hi[3])
     for (int e = 0; e < 3; ++e) face_range(c, -1, e, &lo[e], &hi[e]);
 }
 
+static int is_inner(const octx* c, long idx)
+{
+    long ii[3] = {idx % c->n[0], (idx / c->n[0]) % c->n[1], idx / (c->n[0] * c->n[1])};
+    for (int d = 0; d < c->ndim; ++d)
+        if (ii[d] < 1 || ii[d] > c->n[d] - 2) return 0;
+    return 1;
+}
+
 /* Divergence of the three face arrays at inner cell i, in the reference's
  * order ((qx/dx + qy/dy) + qz/dz) -- diff_2D_nonlin.jl:163. */
 static inline double divergence(const octx* c, double* const q[3], long i)
@@ -198,6 +207,7 @@ static inline double cell_dtau(const octx* c, const double* H, const double* dta
     if (p->model == 0) return c->dtau;
     if (p->model == 1) return dtau_arr[i];
     double h3 = H[i] * H[i] * H[i];
+    if (p->model == 3) h3 = dtau_arr[i] * h3;   /* dtau_arr holds exp(m) for model 3 */
     double re = p->recip ? c->pi + sqrt(c->pipi + (c->L2 / h3) * c->rdt)
                          : c->pi + sqrt(c->pipi + (c->L2 / h3) / p->dt);
     return (((c->vpdt * c->L) / h3) / re) * p->resc;
@@ -276,12 +286,13 @@ int ora_solve(const ora_params* p, double* H, const double* Dfield, int32_t* ite
 {
     octx c;
     if (setup(&c, p) || !H || !iters || p->nt < 0 || p->nout < 1) return 1;
-    if (p->model == 1 && !Dfield) return 1;
+    if ((p->model == 1 || p->model == 3) && !Dfield) return 1;
     long N = c.n[0] * c.n[1] * c.n[2];
     double* Hold = (double*)malloc(sizeof(double) * N);
     double* buf = (double*)calloc((size_t)6 * N, sizeof(double));
-    double* dtau_arr = p->model == 1 ? (double*)calloc(N, sizeof(double)) : NULL;
-    if (!Hold || !buf || (p->model == 1 && !dtau_arr)) {
+    double* dtau_arr = (p->model == 1 || p->model == 3) ? (double*)calloc(N, sizeof(double)) : NULL;
+    double* expm = NULL;
+    if (!Hold || !buf || ((p->model == 1 || p->model == 3) && !dtau_arr)) {
         free(Hold); free(buf); free(dtau_arr);
         return 1;
     }
@@ -289,6 +300,11 @@ int ora_solve(const ora_params* p, double* H, const double* Dfield, int32_t* ite
     double* q2[3] = {buf + 3 * N, buf + 4 * N, buf + 5 * N};
     memcpy(Hold, H, sizeof(double) * N);
     if (p->model == 1) step_dtau(&c, Dfield, dtau_arr);
+    if (p->model == 3) {
+        for (long i = 0; i < N; ++i) dtau_arr[i] = exp(Dfield[i]);
+        expm = dtau_arr;
+    }
+    const double* Dcoef = p->model == 3 ? expm : Dfield;
     int32_t ne = 0, status = 0;
     for (int it = 0; it < p->nt; ++it) {
         int32_t iter = 0;
@@ -296,12 +312,12 @@ int ora_solve(const ora_params* p, double* H, const double* Dfield, int32_t* ite
         while (err > p->tol && iter < p->itmax) {
             int check = ((iter + 1) % p->nout) == 0;
             for (int d = 0; d < c.ndim; ++d)
-                flux_dim(&c, d, q[d], (check && p->resid == 0) ? q2[d] : NULL, H, Dfield);
+                flux_dim(&c, d, q[d], (check && p->resid == 0) ? q2[d] : NULL, H, Dcoef);
             update(&c, H, Hold, q, dtau_arr);
             iter += 1;
             if (check) {
                 if (p->resid == 1)
-                    for (int d = 0; d < c.ndim; ++d) flux2_dim(&c, d, q2[d], H, Dfield);
+                    for (int d = 0; d < c.ndim; ++d) flux2_dim(&c, d, q2[d], H, Dcoef);
                 err = residual_norm(&c, H, Hold, q2);
                 if (errhist && ne < errcap) errhist[ne] = err;
                 ne += 1;
@@ -323,17 +339,20 @@ int ora_iterate(const ora_params* p, double* H, const double* Hold, const double
 {
     octx c;
     if (setup(&c, p) || !H || !Hold || !qx) return 1;
-    if (p->model == 1 && !Dfield) return 1;
+    if ((p->model == 1 || p->model == 3) && !Dfield) return 1;
     double* q[3] = {qx, qy ? qy : qx, qz ? qz : qx};
     double* dtau_arr = NULL;
-    if (p->model == 1) {
+    if (p->model == 1 || p->model == 3) {
         long N = c.n[0] * c.n[1] * c.n[2];
         dtau_arr = (double*)calloc(N, sizeof(double));
         if (!dtau_arr) return 1;
-        step_dtau(&c, Dfield, dtau_arr);
+        if (p->model == 1) step_dtau(&c, Dfield, dtau_arr);
+        else
+            for (long i = 0; i < N; ++i) dtau_arr[i] = exp(Dfield[i]);
     }
+    const double* Dcoef = p->model == 3 ? dtau_arr : Dfield;
     for (int32_t it = 0; it < niter; ++it) {
-        for (int d = 0; d < c.ndim; ++d) flux_dim(&c, d, q[d], NULL, H, Dfield);
+        for (int d = 0; d < c.ndim; ++d) flux_dim(&c, d, q[d], NULL, H, Dcoef);
         update(&c, H, Hold, q, dtau_arr);
     }
     free(dtau_arr);
@@ -346,11 +365,187 @@ double ora_residual_norm(const ora_params* p, const double* H, const double* Hol
     octx c;
     if (setup(&c, p)) return NAN;
     long N = c.n[0] * c.n[1] * c.n[2];
-    double* buf = (double*)calloc((size_t)3 * N, sizeof(double));
+    double* buf = (double*)calloc((size_t)4 * N, sizeof(double));
     if (!buf) return NAN;
     double* q2[3] = {buf, buf + N, buf + 2 * N};
-    for (int d = 0; d < c.ndim; ++d) flux2_dim(&c, d, q2[d], Hpre ? Hpre : H, Dfield);
+    const double* Dcoef = Dfield;
+    if (p->model == 3) {
+        for (long i = 0; i < N; ++i) buf[3 * N + i] = exp(Dfield[i]);
+        Dcoef = buf + 3 * N;
+    }
+    for (int d = 0; d < c.ndim; ++d) flux2_dim(&c, d, q2[d], Hpre ? Hpre : H, Dcoef);
     double r = residual_norm(&c, H, Hold, q2);
     free(buf);
     return r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Discrete adjoint of nt implicit steps (models 2 and 3), FP64 reference.
+ * Physical-unit restatement: q_f = -D_f (H_R - H_L)/h, D_f = E_f a^3,
+ * a = (H_L+H_R)/2, E_f = (E_L+E_R)/2 (E = exp(m); E = 1 for model 2);
+ * F_i = (H_i - Hold_i)/dt + sum_d (q_{i+1/2} - q_{i-1/2})/h_d = 0 per step.
+ * L = 1/2 sum_inner (H^N - Ht)^2.  For n = N..1: J_n^T lam = g (BiCGSTAB,
+ * matrix-free), dL/dm -= lam^T dF/dm, dL/dH0_boundary -= lam^T dF/dH_b,
+ * g <- lam/dt; finally dL/dH0_inner = g.  This is new work (the reference has
+ * no adjoint); it is the checker of the GPU adjoint. */
+typedef struct {
+    const octx* c;
+    const double* H;   /* linearisation point H^n */
+    const double* E;   /* exp(m) or NULL (model 2) */
+} adj_ctx;
+
+static inline double e_at(const adj_ctx* A, long i) { return A->E ? A->E[i] : 1.0; }
+
+/* y = J^T x on inner cells (x zero on the boundary, y zero there). */
+static void apply_JT(const adj_ctx* A, const double* x, double* y)
+{
+    const octx* c = A->c;
+    long lo[3], hi[3];
+    inner_range(c, lo, hi);
+    const double rdt = 1.0 / c->p->dt;
+#pragma omp parallel for collapse(2) schedule(static) num_threads(c->nth)
+    for (long k = lo[2]; k < hi[2]; ++k)
+        for (long j = lo[1]; j < hi[1]; ++j)
+            for (long i = lo[0]; i < hi[0]; ++i) {
+                long ic = i + c->s[1] * j + c->s[2] * k;
+                double acc = x[ic] * rdt;
+                for (int d = 0; d < c->ndim; ++d) {
+                    const double h = c->h[d];
+                    for (int side = 0; side < 2; ++side) {
+                        long L = side ? ic : ic - c->s[d];
+                        long R = L + c->s[d];
+                        const double HL = A->H[L], HR = A->H[R];
+                        const double a = (HL + HR) * 0.5;
+                        const double Ef = (e_at(A, L) + e_at(A, R)) * 0.5;
+                        const double Df = Ef * a * a * a, dD = Ef * 1.5 * a * a;
+                        const double g = HR - HL;
+                        /* dq/dH_L = (D - dD g)/h, dq/dH_R = (-D - dD g)/h */
+                        const double dq = side ? (Df - dD * g) / h : (-Df - dD * g) / h;
+                        acc += (x[L] - x[R]) / h * dq;
+                    }
+                }
+                y[ic] = acc;
+            }
+}
+
+static double dot_inner(const octx* c, const double* a, const double* b)
+{
+    long lo[3], hi[3];
+    inner_range(c, lo, hi);
+    double s = 0.0;
+#pragma omp parallel for collapse(2) schedule(static) num_threads(c->nth) reduction(+ : s)
+    for (long k = lo[2]; k < hi[2]; ++k)
+        for (long j = lo[1]; j < hi[1]; ++j)
+            for (long i = lo[0]; i < hi[0]; ++i) {
+                long ic = i + c->s[1] * j + c->s[2] * k;
+                s += a[ic] * b[ic];
+            }
+    return s;
+}
+
+/* BiCGSTAB for J^T x = b (inner cells), x0 = 0. */
+static int bicgstab_JT(const adj_ctx* A, const double* b, double* x, double rtol, long N)
+{
+    double* r = (double*)calloc(N, sizeof(double));
+    double* r0 = (double*)calloc(N, sizeof(double));
+    double* pv = (double*)calloc(N, sizeof(double));
+    double* v = (double*)calloc(N, sizeof(double));
+    double* sv = (double*)calloc(N, sizeof(double));
+    double* t = (double*)calloc(N, sizeof(double));
+    if (!r || !r0 || !pv || !v || !sv || !t) {
+        free(r); free(r0); free(pv); free(v); free(sv); free(t);
+        return 1;
+    }
+    memset(x, 0, sizeof(double) * N);
+    memcpy(r, b, sizeof(double) * N);
+    memcpy(r0, b, sizeof(double) * N);
+    double bn = sqrt(dot_inner(A->c, b, b));
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
+    int ok = 1;
+    for (int it = 0; it < 20000 && bn > 0.0; ++it) {
+        double rho1 = dot_inner(A->c, r0, r);
+        double beta = (rho1 / rho) * (alpha / omega);
+        for (long i = 0; i < N; ++i) pv[i] = r[i] + beta * (pv[i] - omega * v[i]);
+        apply_JT(A, pv, v);
+        alpha = rho1 / dot_inner(A->c, r0, v);
+        for (long i = 0; i < N; ++i) sv[i] = r[i] - alpha * v[i];
+        apply_JT(A, sv, t);
+        omega = dot_inner(A->c, t, sv) / dot_inner(A->c, t, t);
+        for (long i = 0; i < N; ++i) {
+            x[i] += alpha * pv[i] + omega * sv[i];
+            r[i] = sv[i] - omega * t[i];
+        }
+        rho = rho1;
+        if (sqrt(dot_inner(A->c, r, r)) <= rtol * bn) { ok = 1; break; }
+        ok = 0;
+    }
+    free(r); free(r0); free(pv); free(v); free(sv); free(t);
+    return ok ? 0 : 3;
+}
+
+int ora_adjoint(const ora_params* p, const double* Hs, const double* m, const double* Ht,
+                double* grad_m, double* grad_H0, double rtol)
+{
+    octx c;
+    if (setup(&c, p) || (p->model != 2 && p->model != 3) || !Hs || !Ht || !grad_H0) return 1;
+    if (p->model == 3 && (!m || !grad_m)) return 1;
+    const long N = c.n[0] * c.n[1] * c.n[2];
+    double* E = NULL;
+    double* g = (double*)calloc(N, sizeof(double));
+    double* lam = (double*)calloc(N, sizeof(double));
+    if (p->model == 3) {
+        E = (double*)malloc(sizeof(double) * N);
+        for (long i = 0; i < N; ++i) E[i] = exp(m[i]);
+        memset(grad_m, 0, sizeof(double) * N);
+    }
+    memset(grad_H0, 0, sizeof(double) * N);
+    long lo[3], hi[3];
+    inner_range(&c, lo, hi);
+    const double* HN = Hs + (size_t)p->nt * N;
+    for (long k = lo[2]; k < hi[2]; ++k)
+        for (long j = lo[1]; j < hi[1]; ++j)
+            for (long i = lo[0]; i < hi[0]; ++i) {
+                long ic = i + c.s[1] * j + c.s[2] * k;
+                g[ic] = HN[ic] - Ht[ic];
+            }
+    int status = 0;
+    for (int n = p->nt; n >= 1; --n) {
+        adj_ctx A = {&c, Hs + (size_t)n * N, E};
+        if (bicgstab_JT(&A, g, lam, rtol, N)) status = 3;
+        /* accumulate dL/dm and the boundary part of dL/dH0 face by face */
+        for (int d = 0; d < c.ndim; ++d) {
+            long flo[3], fhi[3];
+            for (int e = 0; e < 3; ++e) face_range(&c, d, e, &flo[e], &fhi[e]);
+            const double h = c.h[d];
+            for (long k = flo[2]; k < fhi[2]; ++k)
+                for (long j = flo[1]; j < fhi[1]; ++j)
+                    for (long i = flo[0]; i < fhi[0]; ++i) {
+                        long L = i + c.s[1] * j + c.s[2] * k, R = L + c.s[d];
+                        const double HL = A.H[L], HR = A.H[R];
+                        const double a = (HL + HR) * 0.5, gg = HR - HL;
+                        const double EL = e_at(&A, L), ER = e_at(&A, R);
+                        const double Ef = (EL + ER) * 0.5;
+                        const double Df = Ef * a * a * a, dD = Ef * 1.5 * a * a;
+                        const double w = (lam[L] - lam[R]) / h;   /* lam^T dF = w * dq */
+                        if (E) {
+                            /* dq/dm_L = -(0.5 E_L a^3) g / h */
+                            grad_m[L] -= w * (-(0.5 * EL * a * a * a) * gg / h);
+                            grad_m[R] -= w * (-(0.5 * ER * a * a * a) * gg / h);
+                        }
+                        /* boundary cells of H (frozen = H0 there) */
+                        const int Lb = !is_inner(&c, L), Rb = !is_inner(&c, R);
+                        if (Lb) grad_H0[L] -= w * ((Df - dD * gg) / h);
+                        if (Rb) grad_H0[R] -= w * ((-Df - dD * gg) / h);
+                    }
+        }
+        for (long i = 0; i < N; ++i) g[i] = lam[i] / p->dt;
+    }
+    for (long k = lo[2]; k < hi[2]; ++k)
+        for (long j = lo[1]; j < hi[1]; ++j)
+            for (long i = lo[0]; i < hi[0]; ++i) {
+                long ic = i + c.s[1] * j + c.s[2] * k;
+                grad_H0[ic] += g[ic];
+            }
+    free(E); free(g); free(lam);
+    return status;
 }

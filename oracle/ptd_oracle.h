@@ -23,7 +23,9 @@ extern "C" {
 
 typedef struct ora_params {
     int32_t ndim;       /* 1, 2 or 3 */
-    int32_t model;      /* 0 linear (scalar D), 1 step (D field), 2 nonlinear (D = H^3) */
+    int32_t model;      /* 0 linear (scalar D), 1 step (D field), 2 nonlinear (D = H^3),
+                           3 nonlinear with a log-coefficient field m: D = exp(m) H^3,
+                           face value ((exp(m_L)+exp(m_R))/2) ((H_L+H_R)/2)^3 */
     int32_t nx, ny, nz; /* cells including the two frozen boundary cells per dimension */
     double lx, ly, lz;  /* domain lengths */
     double dt;          /* physical time step */
@@ -46,7 +48,8 @@ typedef struct ora_params {
 
 /* Solve nt physical steps in place.
  *   H        in: H0 (nx*ny*nz, x fastest); out: H after nt steps.
- *   Dfield   model 1 only: cell diffusivity (nx*ny*nz), else NULL.
+ *   Dfield   model 1: cell diffusivity; model 3: the log-coefficient m (nx*ny*nz);
+ *            else NULL.
  *   iters    out: PT iterations of each physical step (nt entries).
  *   errhist  out (nullable): err of every residual check, in order.
  *   errcap   capacity of errhist;  nerr out (nullable): checks performed.
@@ -66,6 +69,15 @@ int ora_iterate(const ora_params* p, double* H, const double* Hold, const double
  * H_pre (the state the fluxes were evaluated on), returns the norm (p->norm). */
 double ora_residual_norm(const ora_params* p, const double* H, const double* Hold,
                          const double* Hpre, const double* Dfield);
+
+/* Discrete adjoint (models 2 and 3) of nt implicit steps whose converged
+ * states are Hs[0..nt] (Hs[0] = H0, each nx*ny*nz): gradient of
+ * L = 1/2 sum_inner (H^nt - Ht)^2 with respect to m (model 3) and H0 (all
+ * cells; the boundary cells stay frozen at H0 through every step).  Each
+ * transposed step J^T lam = g is solved by BiCGSTAB to relative residual rtol.
+ * Returns 0, 1 on bad arguments, 3 when a linear solve did not reach rtol. */
+int ora_adjoint(const ora_params* p, const double* Hs, const double* m, const double* Ht,
+                double* grad_m, double* grad_H0, double rtol);
 
 #ifdef __cplusplus
 }

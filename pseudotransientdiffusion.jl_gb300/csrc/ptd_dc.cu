@@ -62,6 +62,7 @@ struct DcDev {
     double target;     // inner stopping threshold
     double outer_acc;  // FP64 residual accumulator
     double outer_err;  // FP64 residual norm
+    unsigned long long hmax_bits;  // max |H| over the grid (bit pattern), for the FP32 floor
 };
 
 // One face of the linearised flux (scaled like ptd_device.cuh):
@@ -316,8 +317,10 @@ __global__ void __launch_bounds__(32 * R) dc3d_kernel(DcArgs a, int chunk)
 // check_res!, scripts/diff_2D_nonlin.jl:167-170), written as FP32 for the
 // inner solve and reduced (sum r^2 or max |r|) in FP64.
 template <int MODEL>
-__global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, float* rf, double* acc)
+__global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, float* rf, double* acc,
+                                                         unsigned long long* hmax)
 {
+    unsigned long long hm = 0ull;
     const long long nix = a.nx - 2;
     const long long niy = ndim > 1 ? a.ny - 2 : 1;
     const long long niz = ndim > 2 ? a.nz - 2 : 1;
@@ -355,7 +358,11 @@ __global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, flo
         const double r = fma(-(H - static_cast<const double*>(a.Hold)[c]), a.rdt, div);
         rf[c] = (float)r;
         accumulate_residual(r, part, pmax);
+        const unsigned long long hb = (unsigned long long)__double_as_longlong(H) & 0x7fffffffffffffffull;
+        hm = hb > hm ? hb : hm;
     }
+    hm = warp_max_u64(hm);
+    if ((threadIdx.x & 31) == 0 && hm) atomicMax(hmax, hm);
     block_reduce_residual(acc, a.norm_max, part, pmax);
 }
 
@@ -378,14 +385,21 @@ __global__ void dc_tofloat_kernel(const double* src, float* dst, long long n)
 }
 
 // Outer judge: err of the FP64 residual; sets the inner target and resets
-// the inner control block.
-__global__ void dc_outer_judge_kernel(DcDev* st, double norm_den, int norm_max, double rtol, double tol)
+// the inner control block.  The target is max(eta, floor) * err with floor
+// the attainable relative accuracy of an FP32 solve, ~ eps_32 * cond(J),
+// cond(J) ~ 1 + dt * Dmax * sum_d 4/dx_d^2 (Dmax = H_max^3 for D = H^3).
+__global__ void dc_outer_judge_kernel(DcDev* st, double norm_den, int norm_max, double rtol, double tol,
+                                      double cond_scale, double dconst, int nonlin)
 {
     const double acc = st->outer_acc;
     st->outer_acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
     st->outer_err = err;
-    st->target = fmax(rtol * err, 0.25 * tol);
+    const double hmax = __longlong_as_double((long long)st->hmax_bits);
+    st->hmax_bits = 0ull;
+    const double dmax = nonlin ? hmax * hmax * hmax : dconst;
+    const double floor = fmin(0.5, 0.5 * 5.96e-8 * (1.0 + cond_scale * dmax));
+    st->target = fmax(fmax(rtol, floor) * err, 0.25 * tol);
     st->done = 0;
     st->nchecks = 0;
     st->iter = 0;
@@ -563,7 +577,7 @@ int dc_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     dc->max_outer = p.dc_max_outer > 0 ? p.dc_max_outer : 30;
     {
         const int nmax = std::max(p.nx, std::max(p.ny, p.nz));
-        dc->stall = std::max(6, (nmax / 2 + dc->nchk - 1) / dc->nchk);
+        dc->stall = std::max(10, (2 * nmax + dc->nchk - 1) / dc->nchk);
     }
     const size_t fb = (size_t)g.nfield * sizeof(float);
     auto alloc = [&](void** ptr, size_t n) -> int {
@@ -653,13 +667,17 @@ static int dc_residual(DcState* dc, double eta, double* err)
     a.Hold = dc->Hold;
     a.D = dc->D;
     const int nb = 152 * 8;
-    if (dc->model == LIN) dc_resid64_kernel<LIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
+    unsigned long long* hm = &dc->dev->hmax_bits;
+    if (dc->model == LIN) dc_resid64_kernel<LIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc, hm);
     else if (dc->model == LINSTEP)
-        dc_resid64_kernel<LINSTEP><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
-    else dc_resid64_kernel<NONLIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc);
+        dc_resid64_kernel<LINSTEP><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc, hm);
+    else dc_resid64_kernel<NONLIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc, hm);
     DCK(cudaGetLastError());
+    double cond_scale = 0.0;
+    for (int d = 0; d < dc->ndim; ++d) cond_scale += 4.0 / (dc->dv.h[d] * dc->dv.h[d]);
+    cond_scale *= dc->p.dt;
     dc_outer_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->dv.norm_den, dc->p.norm == PTD_NORM_MAX, eta,
-                                              dc->p.tol);
+                                              dc->p.tol, cond_scale, dc->p.D, dc->model == NONLIN);
     DCK(cudaGetLastError());
     dc->k.launches += 2;
     DCK(cudaMemcpyAsync(dc->h_dev, dc->dev, sizeof(DcDev), cudaMemcpyDeviceToHost, dc->s));

@@ -19,6 +19,8 @@
 
 #include <cuda_runtime.h>
 
+#include "ptd_device.cuh"
+
 namespace ptd {
 
 struct F64 {
@@ -29,7 +31,9 @@ struct F64 {
     __device__ static __forceinline__ T mul(T a, T b) { return a * b; }
     __device__ static __forceinline__ T mad(T a, T b, T c) { return fma(a, b, c); }        // a*b + c
     __device__ static __forceinline__ T nmad(T a, T b, T c) { return fma(-a, b, c); }      // c - a*b
-    __device__ static __forceinline__ float lo_f(T a) { return (float)a; }
+    // (the hardware f64<->f32 conversions issue on the FP64 pipe: use the
+    // integer-pipe bit conversions of ptd_device.cuh instead)
+    __device__ static __forceinline__ float lo_f(T a) { return d2f_bits(a); }
     __device__ static __forceinline__ double to_d(T a) { return a; }
     __device__ static __forceinline__ T zero() { return 0.0; }
     __device__ static __forceinline__ T shfl_down(T v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }

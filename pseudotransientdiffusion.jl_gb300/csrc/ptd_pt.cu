@@ -29,7 +29,7 @@
 namespace ptd {
 
 // w - c*t with a float damping coefficient c.
-__device__ __forceinline__ double nmadf(F64, float c, double t, double w) { return fma(-(double)c, t, w); }
+__device__ __forceinline__ double nmadf(F64, float c, double t, double w) { return fma(-f2d_bits(c), t, w); }
 __device__ __forceinline__ float2 nmadf(DF64, float c, float2 t, float2 w) { return DF64::sub(w, DF64::mulf(t, c)); }
 
 template <class N>
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256) pt1d_kernel(PTArgs a)
             st<N>(a.Hout, i, Hn);
             if (CHECK) {
                 const T r = N::sub(N::mul(N::sub(ur, ul), cst<N>(a, 0)), N::mul(N::sub(Hn, Ho), cst<N>(a, 3)));
-                accumulate_residual(N::native ? N::to_d(r) : (double)N::lo_f(r), part, pmax);
+                accumulate_residual(N::to_d(r), part, pmax);
             }
         }
     }
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) pt2d_kernel(PTArgs a, int chunk)
                 if (CHECK) {
                     const T divu = N::mad(N::sub(uy, uyb), cst<N>(a, 1), N::mul(N::sub(ux, uxl), cst<N>(a, 0)));
                     const T r = N::sub(divu, N::mul(N::sub(Hnew, Ho), cst<N>(a, 3)));
-                    accumulate_residual(N::native ? N::to_d(r) : (double)N::lo_f(r), part, pmax);
+                    accumulate_residual(N::to_d(r), part, pmax);
                 }
             }
             Hc = Hn;
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(32 * R) pt3d_kernel(PTArgs a, int chunk)
                     const T divu = N::mad(N::sub(uz, uzb), cst<N>(a, 2),
                                           N::mad(N::sub(uy, uyb), cst<N>(a, 1), N::mul(N::sub(ux, uxl), cst<N>(a, 0))));
                     const T r2 = N::sub(divu, N::mul(N::sub(Hnew, Ho), cst<N>(a, 3)));
-                    accumulate_residual(N::native ? N::to_d(r2) : (double)N::lo_f(r2), part, pmax);
+                    accumulate_residual(N::to_d(r2), part, pmax);
                 }
             }
             Hc = Hn;
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(256) resid_consistent_kernel(PTArgs a, int ndi
             div = N::mad(N::sub(uR, uL), cst<N>(a, d), div);
         }
         const T r = N::sub(div, N::mul(N::sub(H, ld<N>(a.Hold, c)), cst<N>(a, 3)));
-        accumulate_residual(N::native ? N::to_d(r) : (double)N::lo_f(r), part, pmax);
+        accumulate_residual(N::to_d(r), part, pmax);
     }
     block_reduce_residual(a, part, pmax);
 }

@@ -34,8 +34,8 @@ from dataclasses import dataclass, field, replace
 
 import numpy as np
 
-LIN, LINSTEP, NONLIN = 0, 1, 2
-MODEL_NAMES = {"lin": LIN, "linstep": LINSTEP, "nonlin": NONLIN}
+LIN, LINSTEP, NONLIN, NONLIN_EXPM = 0, 1, 2, 3
+MODEL_NAMES = {"lin": LIN, "linstep": LINSTEP, "nonlin": NONLIN, "nonlin_expm": NONLIN_EXPM}
 
 
 @dataclass(frozen=True)
@@ -229,3 +229,21 @@ CONFIGS = {
                                                               dirichlet=1.0, ttot=0.6, ic="linrange",
                                                               default_n=512),
 }
+
+
+def log_coefficient_field(shape, lengths=(10.0, 10.0, 10.0), corr=1.0, std=0.3, seed=0):
+    """Smooth Gaussian random field m (cell centres, x fastest): white noise
+    filtered in Fourier space by a Gaussian kernel of correlation length
+    `corr`, rescaled to standard deviation `std`; seeded."""
+    rng = np.random.default_rng(seed)
+    z = rng.standard_normal(shape)
+    k2 = np.zeros(shape)
+    for d, n in enumerate(shape):
+        h = lengths[d] / n
+        k = 2 * np.pi * np.fft.fftfreq(n, d=h)
+        sh = [1] * len(shape)
+        sh[d] = n
+        k2 = k2 + (k ** 2).reshape(sh)
+    f = np.real(np.fft.ifftn(np.fft.fftn(z) * np.exp(-0.25 * corr * corr * k2)))
+    f = (f - f.mean()) / f.std() * std
+    return np.asfortranarray(f)

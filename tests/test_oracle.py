@@ -89,3 +89,39 @@ def test_fixed_iterations_match_solve():
     q = [np.zeros_like(H) for _ in range(3)]
     O.iterate(s, H, H0.copy(order="F"), q, int(iters[0]))
     assert np.array_equal(H, H1)
+
+
+def _adjoint_problem(ndim):
+    base = S.SCRIPTS["diff_2D_nonlin" if ndim == 2 else "diff_3D_nonlin_multixpu"]
+    s = base.with_(name=f"adj{ndim}d", model=S.NONLIN_EXPM, shift=1.0, dirichlet=1.0, ttot=0.3, dt=0.1,
+                   tol=1e-13, itmax=400000, ic="linrange")
+    shape = (24, 20) if ndim == 2 else (12, 11, 10)
+    H0 = S.initial_condition(s, *shape)
+    m = S.log_coefficient_field(shape, seed=1)
+    Ht = O.forward_checkpoints(s, H0, m + 0.3 * S.log_coefficient_field(shape, seed=2))[-1]
+    return s, shape, H0, m, Ht
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_reference_adjoint_matches_finite_differences(ndim):
+    """The CPU FP64 adjoint (checker of the GPU adjoint) against central
+    differences of the oracle forward model, in random directions."""
+    s, shape, H0, m, Ht = _adjoint_problem(ndim)
+    inner = (slice(1, -1),) * ndim
+
+    def loss(mm, hh):
+        d = (O.forward_checkpoints(s, hh, mm)[-1] - Ht)[inner]
+        return 0.5 * float(np.sum(d * d))
+
+    Hs = O.forward_checkpoints(s, H0, m)
+    gm, gh, st = O.adjoint(s, Hs, Ht, m)
+    assert st == 0
+    rng = np.random.default_rng(7)
+    eps = 1e-5
+    for _ in range(2):
+        dm = rng.standard_normal(shape)
+        fd = (loss(m + eps * dm, H0) - loss(m - eps * dm, H0)) / (2 * eps)
+        assert abs(fd - np.sum(gm * dm)) <= 1e-6 * abs(fd)
+        dh = rng.standard_normal(shape)
+        fd = (loss(m, H0 + eps * dh) - loss(m, H0 - eps * dh)) / (2 * eps)
+        assert abs(fd - np.sum(gh * dh)) <= 1e-6 * abs(fd)
