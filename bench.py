@@ -354,7 +354,8 @@ def run_ours(args, world, rank, local, pg):
         "ms_per_step": round(t_max / max(args.steps, 1) * 1e3, 3),
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": round(value / pub, 3) if pub else None,
-        "dtype": "f64", "data": "synthetic",
+        "dtype": {"fp64": "f64", "df64": "df64 (f32x2)", "fp32_dc": "f32 inner + f64 outer"}[args.precision],
+        "data": "synthetic",
         "config": {"workload": args.workload, "shape": list(shape), "precision": args.precision,
                    "nchk": s.nout, "tol": s.tol, "dt": s.dt, "step": "one physical time step to tol",
                    "l2": f"inputs larger than L2 (working set {ws_gb:.2f} GB), no flush",
@@ -383,7 +384,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="2d_nonlin_4096")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32_dc"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "fp32_dc"])
     ap.add_argument("--n", type=int, default=0, help="override the grid size (testing)")
     ap.add_argument("--fixed-iters", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=15.0)

@@ -58,7 +58,11 @@ typedef enum ptd_status {
  *  LIN      D = const                     scripts/diff_{1D,2D}_lin.jl, diff_3D_lin_multixpu.jl
  *  LINSTEP  D = per-cell field (step)     scripts/diff_{1D,2D}_linstep.jl, diff_3D_linstep_multixpu.jl
  *  NONLIN   D = H^3 (face: (avg H)^3)     scripts/diff_{1D,2D}_nonlin.jl, diff_3D_nonlin_multixpu.jl */
-enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2 };
+enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL_NONLIN_EXPM = 3 };
+/* PTD_MODEL_NONLIN_EXPM (no reference counterpart; the model of the adjoint
+ * solver): D = exp(m) H^3 with a per-cell log-coefficient field m passed in
+ * place of D; face value ((exp(m_L)+exp(m_R))/2) ((H_L+H_R)/2)^3.  FP64 and
+ * DF64 only. */
 
 /* Arithmetic of the PT iterations.
  *  FP64     every PT iteration in native FP64 (the reference's form).
@@ -148,6 +152,60 @@ PTD_API int ptd_sync(ptd_ctx* ctx);
 PTD_API int ptd_counters(ptd_ctx* ctx, int64_t* kernel_launches, int64_t* pt_iterations);
 
 PTD_API void ptd_destroy(ptd_ctx* ctx);
+
+/* ---------------------------------------------------------------------------
+ * Batched 2D solves: many independent grids of uneven sizes, each with its own
+ * H0 (and D for the step model), advanced together by one kernel launch per
+ * PT iteration with per-instance convergence flags.  No reference
+ * counterpart (the reference solves one grid per run); the per-instance
+ * algorithm is that of ptd_solve (FP64, DF64) or its FP32_DC form.
+ * Constraint: itmax is a multiple of nchk. */
+typedef struct ptd_batch_params {
+    int32_t ninst;       /* number of instances */
+    int32_t model;       /* PTD_MODEL_* */
+    double lx, ly;       /* domain lengths (shared) */
+    double dt;
+    int32_t nt, itmax, nchk, precision;
+    double tol, cfl, resc, D;
+    int32_t norm, flags;
+    int32_t dc_max_outer, pad0;
+    double dc_inner_rtol;
+    int32_t reserved[8];
+} ptd_batch_params;
+
+typedef struct ptd_batch ptd_batch;
+
+/* Defaults of the 2D script for `model` (lx = ly = 10, dt = 0.2, nt = 5, ...). */
+PTD_API int ptd_batch_params_init(ptd_batch_params* p, int32_t ninst, int32_t model);
+/* nx[i], ny[i]: cells of instance i (including boundary cells). */
+PTD_API int ptd_batch_create(ptd_batch** b, const ptd_batch_params* p, const int32_t* nx, const int32_t* ny);
+/* H[i] in: H0 of instance i, out: H after nt steps (nx[i]*ny[i], x fastest; host
+ * or device).  D[i]: step-model diffusivity or NULL.  iters: ninst*nt PT
+ * iterations (FP32_DC: inner FP32 iterations), instance-major.  err_last
+ * (nullable, ninst): last residual norm of each instance.  n_done: ninst. */
+PTD_API int ptd_batch_solve(ptd_batch* b, double* const* H, const double* const* D, int32_t* iters,
+                            double* err_last, int32_t* n_done);
+/* Autotuner: times every (warps per CTA, rows per y chunk) launch shape of the
+ * batched kernel on the batch's own instances and keeps the fastest. */
+PTD_API int ptd_batch_tune(ptd_batch* b, int32_t* warps, int32_t* chunk, float* us_per_iteration);
+PTD_API int ptd_batch_counters(ptd_batch* b, int64_t* kernel_launches, int64_t* pt_iterations);
+PTD_API void ptd_batch_destroy(ptd_batch* b);
+
+/* ---------------------------------------------------------------------------
+ * Discrete adjoint (3D, D = H^3 or D = exp(m) H^3).  No reference counterpart
+ * (the reference has no adjoint).  ptd_adj_forward solves p->nt implicit steps
+ * from H0 (m: the log-coefficient field, model PTD_MODEL_NONLIN_EXPM), keeps
+ * one FP64 checkpoint of H per physical step and returns
+ * L = 1/2 sum_inner (H^nt - Ht)^2 (and H^nt when HN != NULL);
+ * ptd_adj_gradient then returns dL/dm and dL/dH0 (every cell, each nullable)
+ * by solving the transposed linearised PT system of every step backwards. */
+typedef struct ptd_adj ptd_adj;
+PTD_API int ptd_adj_create(ptd_adj** a, const ptd_params* p);
+PTD_API int ptd_adj_forward(ptd_adj* a, const double* H0, const double* m, const double* Ht, double* loss,
+                            double* HN, int32_t* iters_per_step);
+PTD_API int ptd_adj_gradient(ptd_adj* a, double* grad_m, double* grad_H0, int32_t* adj_iters_per_step);
+PTD_API int ptd_adj_counters(ptd_adj* a, int64_t* kernel_launches, int64_t* pt_iterations);
+PTD_API void ptd_adj_destroy(ptd_adj* a);
 
 PTD_API const char* ptd_strerror(int status);
 PTD_API const char* ptd_last_error(void);   /* detail of the last failure on this thread */

@@ -88,7 +88,7 @@ extern "C" int ptd_params_init(ptd_params* p, int32_t ndim, int32_t model)
 {
     if (!p) return fail(PTD_EINVAL, "ptd_params_init: p is NULL");
     if (ndim < 1 || ndim > 3) return fail(PTD_EINVAL, "ptd_params_init: ndim must be 1, 2 or 3");
-    if (model < PTD_MODEL_LIN || model > PTD_MODEL_NONLIN)
+    if (model < PTD_MODEL_LIN || model > PTD_MODEL_NONLIN_EXPM)
         return fail(PTD_EINVAL, "ptd_params_init: unknown model %d", model);
     std::memset(p, 0, sizeof(*p));
     p->ndim = ndim;
@@ -106,7 +106,7 @@ extern "C" int ptd_params_init(ptd_params* p, int32_t ndim, int32_t model)
     p->tol = 1e-8;
     if (ndim == 1) p->cfl = model == PTD_MODEL_NONLIN ? 1.0 : 0.99;
     else p->cfl = 1.0 / std::sqrt((double)ndim);
-    p->resc = (model == PTD_MODEL_NONLIN && ndim > 1) ? 1.0 / 1.2 : 1.0;
+    p->resc = (model >= PTD_MODEL_NONLIN && ndim > 1) ? 1.0 / 1.2 : 1.0;
     p->D = 1.0;
     p->resid_mode = PTD_RESID_MIXED;
     p->norm = PTD_NORM_RMS;
@@ -117,8 +117,10 @@ int ptd::validate(const ptd_params* p)
 {
     if (!p) return fail(PTD_EINVAL, "params is NULL");
     if (p->ndim < 1 || p->ndim > 3) return fail(PTD_EINVAL, "ndim must be 1, 2 or 3 (got %d)", p->ndim);
-    if (p->model < PTD_MODEL_LIN || p->model > PTD_MODEL_NONLIN)
+    if (p->model < PTD_MODEL_LIN || p->model > PTD_MODEL_NONLIN_EXPM)
         return fail(PTD_EINVAL, "unknown model %d", p->model);
+    if (p->model == PTD_MODEL_NONLIN_EXPM && p->precision == PTD_PREC_FP32_DC)
+        return fail(PTD_EINVAL, "the exp(m) H^3 model runs in FP64 or DF64");
     const int n[3] = {p->nx, p->ny, p->nz};
     for (int d = 0; d < 3; ++d) {
         if (d < p->ndim && n[d] < 3)
@@ -137,7 +139,7 @@ int ptd::validate(const ptd_params* p)
     if (!(p->tol >= 0.0)) return fail(PTD_EINVAL, "tol must be >= 0");
     if (!(p->cfl > 0.0) || !std::isfinite(p->cfl)) return fail(PTD_EINVAL, "cfl must be > 0");
     if (!(p->resc > 0.0) || !std::isfinite(p->resc)) return fail(PTD_EINVAL, "resc must be > 0");
-    if (p->model != PTD_MODEL_NONLIN && (!(p->D > 0.0) || !std::isfinite(p->D)))
+    if (p->model < PTD_MODEL_NONLIN && (!(p->D > 0.0) || !std::isfinite(p->D)))
         return fail(PTD_EINVAL, "D must be > 0");
     if (p->precision != PTD_PREC_FP64 && p->precision != PTD_PREC_FP32_DC && p->precision != PTD_PREC_DF64)
         return fail(PTD_EINVAL, "unknown precision %d", p->precision);
@@ -187,7 +189,7 @@ void ptd::derive(const ptd_params& p, Derived& dv)
     } else {
         dv.k1 = 1.0 / (dv.vpdt * L * p.resc);
         dv.k2 = L * p.resc / dv.vpdt;
-        kappa = 0.125;
+        kappa = p.model == PTD_MODEL_NONLIN_EXPM ? 0.0625 : 0.125;
     }
     for (int d = 0; d < 3; ++d) dv.sig[d] = d < p.ndim ? kappa / (dv.h[d] * dv.h[d]) : 0.0;
     dv.A = L * L / p.dt;
@@ -411,8 +413,9 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
     if (!rc) rc = alloc((void**)&c->Hold, bytes);
     for (int d = 0; d < p->ndim && !rc; ++d)
         for (int q = 0; q < 2 && !rc; ++q) rc = alloc((void**)&c->W[d][q], bytes);
-    if (!rc && p->model == PTD_MODEL_LINSTEP) rc = alloc((void**)&c->D, bytes);
-    if (!rc && c->df64) rc = alloc((void**)&c->stage, bytes);
+    if (!rc && (p->model == PTD_MODEL_LINSTEP || p->model == PTD_MODEL_NONLIN_EXPM))
+        rc = alloc((void**)&c->D, bytes);
+    if (!rc && (c->df64 || p->model == PTD_MODEL_NONLIN_EXPM)) rc = alloc((void**)&c->stage, bytes);
     if (!rc) rc = alloc((void**)&c->st, sizeof(DevState));
     if (!rc) rc = alloc((void**)&c->zero_flag, sizeof(int));
     c->errcap = (p->nchk <= p->itmax ? p->itmax / p->nchk : 0) + 2;
@@ -481,6 +484,7 @@ extern "C" int ptd_set_state(ptd_ctx* c, const double* H, const double* D)
     if (!c) return fail(PTD_EINVAL, "ctx is NULL");
     if (!H) return fail(PTD_EINVAL, "H is NULL");
     if (c->p.model == PTD_MODEL_LINSTEP && !D) return fail(PTD_EINVAL, "the step model needs D");
+    if (c->p.model == PTD_MODEL_NONLIN_EXPM && !D) return fail(PTD_EINVAL, "the exp(m) H^3 model needs m (in D)");
     const size_t bytes = (size_t)c->nfield * sizeof(double);
     // padding stays zero: clear whole buffers first
     double* Hdst = c->df64 ? c->stage : c->H[0];
@@ -496,6 +500,13 @@ extern "C" int ptd_set_state(ptd_ctx* c, const double* H, const double* D)
     for (int d = 0; d < 3; ++d)
         for (int q = 0; q < 2; ++q)
             if (c->W[d][q]) CK(cudaMemsetAsync(c->W[d][q], 0, bytes, c->stream));
+    if (c->p.model == PTD_MODEL_NONLIN_EXPM) {
+        CK(cudaMemsetAsync(c->stage, 0, bytes, c->stream));
+        rc = copy_field_in(*c, c->stage, D, c->stream);
+        if (rc) return rc;
+        CK(launch_expm(c->stage, c->D, c->nfield, c->df64, c->stream));
+        c->launches += 1;
+    }
     if (c->p.model == PTD_MODEL_LINSTEP) {
         double* Ddst = c->df64 ? c->stage : c->D;
         CK(cudaMemsetAsync(Ddst, 0, bytes, c->stream));
@@ -654,4 +665,16 @@ extern "C" int ptd_solve(ptd_ctx* c, double* H, const double* D, int32_t* iters_
     rc = ptd_get_state(c, H);
     if (rc) return rc;
     return rs;
+}
+
+int ptd::ctx_current_f64(ptd_ctx* c, double* dst)
+{
+    const double* src = c->dc ? dc_current(c->dc) : c->H[c->cur];
+    if (c->df64) {
+        CK(launch_from_df64(src, dst, c->nfield, c->stream));
+        c->launches += 1;
+    } else {
+        CK(cudaMemcpyAsync(dst, src, (size_t)c->nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return PTD_OK;
 }

@@ -1,0 +1,1083 @@
+// ptd_batch.cu -- many independent 2D solves of uneven grid sizes, each with
+// its own initial condition and D field, advanced together.
+//
+// No reference counterpart (the reference solves one grid per process); the
+// per-instance algorithm is the reference's (scripts/diff_2D_linstep.jl and
+// siblings) or the FP32 + FP64 defect correction of ptd_dc.cu.
+//
+// Layout: every field of every instance lives in one concatenated device
+// buffer (instance i at element offset off_i, row pitch a multiple of 32).
+// One kernel launch per PT iteration covers the whole batch: a work table
+// maps each CTA to (instance, x tile block, y chunk), the CTA loads its
+// instance's arguments from a device table and runs the same kernel body as
+// the one-grid solver.  Each instance has its own control block (check
+// accumulator, done flag, iteration counter); CTAs of a finished instance
+// return at entry, so a CUDA graph holding nchk iterations + the batched judge
+// is replayed until every instance has stopped, with no host round trip per
+// check and no instance waiting for another.
+//
+// FP32_DC: the inexact-Newton state machine of ptd_dc.cu runs per instance on
+// the device (forcing term, FP32-floor-aware inner target, backtracking), so
+// instances that need different numbers of outer corrections also proceed
+// independently; the host only replays graphs until all have finished.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "ptd_dc_body.cuh"
+#include "ptd_internal.h"
+#include "ptd_pt_body.cuh"
+
+namespace ptd {
+
+enum { PH_START = 0, PH_INNER = 1, PH_BACKTRACK = 2, PH_CONVERGED = 3, PH_CAPPED = 4, PH_NAN = 5 };
+
+// Per-instance control block of the batched defect correction.
+struct BDev {
+    int done;        // inner solve finished (or not running)
+    int nchecks;
+    int iter;        // inner iterations of the current inner solve
+    int best_at;
+    double acc;      // inner residual accumulator
+    double err;
+    double best;
+    double target;
+    double outer_acc;            // FP64 residual accumulator
+    unsigned long long hmax_bits;
+    double err_ref;  // residual norm of the last accepted state
+    double a_last;   // factor of the last correction applied
+    double a_next;   // factor the next apply uses
+    int phase;
+    int nhalf;
+    int outer;
+    int total_inner;
+    // constants
+    double norm_den;
+    double cond_scale;   // dt * sum_d 4/dx_d^2
+    double dconst;       // Dmax of the linear models
+};
+
+// ---------------------------------------------------------------------------
+template <class N, int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) pt2d_batch_kernel(const PTArgs* __restrict__ tab,
+                                                         const int4* __restrict__ work, int chunk)
+{
+    const int4 w = work[blockIdx.x];
+    const PTArgs a = tab[w.x];
+    if (step_done(a.done)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    pt2d_body<N, MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    if (CHECK) block_reduce_residual(a, part, pmax);
+}
+
+__global__ void judge_batch_kernel(DevState* st, int ninst, int nchk, int itmax, double tol,
+                                   const double* norm_den, int norm_max)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    DevState& s = st[i];
+    if (s.done) return;
+    const double acc = s.acc;
+    s.acc = 0.0;
+    const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den[i]);
+    s.nchecks += 1;
+    s.iter += nchk;
+    s.err = err;
+    if (!(err > tol)) s.done = (err != err) ? DONE_NAN : DONE_CONVERGED;
+    else if (s.iter + nchk > itmax) s.done = DONE_CAP;
+}
+
+__global__ void reset_batch_kernel(DevState* st, int ninst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    st[i].done = DONE_RUNNING;
+    st[i].nchecks = 0;
+    st[i].iter = 0;
+    st[i].acc = 0.0;
+    st[i].err = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+template <int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) dc2d_batch_kernel(const DcArgs* __restrict__ tab,
+                                                         const int4* __restrict__ work, int chunk)
+{
+    const int4 w = work[blockIdx.x];
+    const DcArgs a = tab[w.x];
+    if (dc_done(a.done)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    dc2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+}
+
+__global__ void inner_judge_batch_kernel(BDev* st, int ninst, int nchk, int itmax, int norm_max, int stall)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    BDev& s = st[i];
+    if (s.done) return;
+    const double acc = s.acc;
+    s.acc = 0.0;
+    const double err = norm_max ? acc : sqrt(acc) / sqrt(s.norm_den);
+    s.err = err;
+    s.nchecks += 1;
+    s.iter += nchk;
+    if (err < 0.95 * s.best) {
+        s.best = err;
+        s.best_at = s.nchecks;
+    }
+    if (!(err > s.target)) s.done = 1;
+    else if (s.iter + nchk > itmax) s.done = 1;
+    else if (s.nchecks - s.best_at >= stall) s.done = 1;   // FP32 floor reached
+}
+
+// FP64 residual of each unfinished instance over one chunk of its inner
+// cells (cwork: {instance, first inner cell, count}); writes r as FP32.
+template <int MODEL>
+__global__ void __launch_bounds__(256) resid64_batch_kernel(const PTArgs* __restrict__ tab, BDev* st,
+                                                            float* const* rf, const int4* __restrict__ cwork)
+{
+    const int4 w = cwork[blockIdx.x];
+    const int inst = w.x;
+    if (st[inst].phase >= PH_CONVERGED) return;
+    const PTArgs a = tab[inst];
+    const double* Hp = static_cast<const double*>(a.Hin);
+    const double* Hold = a.Hold ? static_cast<const double*>(a.Hold) : Hp;
+    const double* Dp = static_cast<const double*>(a.D);
+    float* r_out = rf[inst];
+    const long long nix = a.nx - 2;
+    double part = 0.0;
+    unsigned long long pmax = 0ull, hm = 0ull;
+    for (int t = threadIdx.x; t < w.z; t += blockDim.x) {
+        const long long cell = (long long)w.y + t;
+        const long long ix = 1 + cell % nix, iy = 1 + cell / nix;
+        const long long c = iy * a.sy + ix;
+        const long long stp[2] = {1, a.sy};
+        const double H = Hp[c];
+        double div = 0.0;
+        for (int d = 0; d < 2; ++d) {
+            const double HR = Hp[c + stp[d]], HL = Hp[c - stp[d]];
+            double uR, uL;
+            if (MODEL == LIN) {
+                uR = HR - H;
+                uL = H - HL;
+            } else if (MODEL == LINSTEP) {
+                uR = (Dp[c] + Dp[c + stp[d]]) * (HR - H);
+                uL = (Dp[c - stp[d]] + Dp[c]) * (H - HL);
+            } else {
+                const double sR = H + HR, sL = HL + H;
+                uR = sR * sR * sR * (HR - H);
+                uL = sL * sL * sL * (H - HL);
+            }
+            div = fma(uR - uL, a.sig[d], div);
+        }
+        const double r = fma(-(H - Hold[c]), a.rdt, div);
+        r_out[c] = (float)r;
+        accumulate_residual(r, part, pmax);
+        const unsigned long long hb = (unsigned long long)__double_as_longlong(H) & 0x7fffffffffffffffull;
+        hm = hb > hm ? hb : hm;
+    }
+    hm = warp_max_u64(hm);
+    if ((threadIdx.x & 31) == 0 && hm) atomicMax(&st[inst].hmax_bits, hm);
+    block_reduce_residual(&st[inst].outer_acc, a.norm_max, part, pmax);
+}
+
+// Per-instance inexact-Newton state machine (see ptd_dc.cu).
+__global__ void outer_judge_batch_kernel(BDev* st, int ninst, int norm_max, double tol, double rtol,
+                                         int max_outer, int itmax, int nonlin)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    BDev& s = st[i];
+    if (s.phase >= PH_CONVERGED) return;
+    const double acc = s.outer_acc;
+    s.outer_acc = 0.0;
+    const double err = norm_max ? acc : sqrt(acc) / sqrt(s.norm_den);
+    const double hmax = __longlong_as_double((long long)s.hmax_bits);
+    s.hmax_bits = 0ull;
+    double eta = 0.1;
+    if (s.phase == PH_START) {
+        s.outer = 0;
+        s.total_inner = 0;
+        s.nhalf = 0;
+    } else {
+        if (s.phase == PH_INNER) s.total_inner += s.iter;
+        if (!(err < s.err_ref) && s.nhalf < 4) {   // also catches NaN
+            s.phase = PH_BACKTRACK;
+            s.a_next = -0.5 * s.a_last;
+            s.a_last *= 0.5;
+            s.nhalf += 1;
+            s.done = 1;
+            return;
+        }
+        s.outer += 1;
+        const double q = err / s.err_ref;
+        eta = fmin(0.5, fmax(rtol, 0.9 * q * q));
+    }
+    s.err_ref = err;
+    s.nhalf = 0;
+    s.done = 1;
+    if (!(err > tol)) {
+        s.phase = (err != err) ? PH_NAN : PH_CONVERGED;
+        return;
+    }
+    if (s.outer >= max_outer || s.total_inner >= itmax) {
+        s.phase = PH_CAPPED;
+        return;
+    }
+    const double dmax = nonlin ? hmax * hmax * hmax : s.dconst;
+    const double floor = fmin(0.5, 0.5 * 5.96e-8 * (1.0 + s.cond_scale * dmax));
+    s.target = fmax(fmax(eta, floor) * err, 0.25 * tol);
+    s.phase = PH_INNER;
+    s.a_last = 1.0;
+    s.a_next = 1.0;
+    s.done = 0;
+    s.nchecks = 0;
+    s.iter = 0;
+    s.best = err;
+    s.best_at = 0;
+    s.acc = 0.0;
+}
+
+__global__ void start_batch_kernel(BDev* st, int ninst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    st[i].phase = PH_START;
+    st[i].done = 1;
+    st[i].outer_acc = 0.0;
+    st[i].hmax_bits = 0ull;
+    st[i].acc = 0.0;
+}
+
+// H += a * delta (a from the instance's phase), refresh Hf; zero the
+// correction state for the next inner solve.
+__global__ void __launch_bounds__(256) apply_batch_kernel(const DcArgs* __restrict__ tab0, const BDev* st,
+                                                          const int4* __restrict__ fwork, double* const* Hs,
+                                                          const int* cur_parity)
+{
+    const int4 w = fwork[blockIdx.x];
+    const int inst = w.x;
+    const BDev& s = st[inst];
+    double a;
+    if (s.phase == PH_INNER) a = 1.0;
+    else if (s.phase == PH_BACKTRACK) a = s.a_next;
+    else return;
+    const DcArgs& t = tab0[inst];
+    const float* delta = cur_parity[inst] ? t.dout : t.din;
+    double* H = Hs[inst];
+    float* Hf = const_cast<float*>(t.Hf);
+    for (int k = threadIdx.x; k < w.z; k += blockDim.x) {
+        const long long e = (long long)w.y + k;
+        const double h = fma(a, (double)delta[e], H[e]);
+        H[e] = h;
+        Hf[e] = __double2float_rn(h);
+    }
+}
+
+// Zero the correction state (delta and its fluxes, both parities) of the
+// instances about to start an inner solve.
+__global__ void __launch_bounds__(256) zero_batch_kernel(const DcArgs* __restrict__ tab0, const BDev* st,
+                                                         const int4* __restrict__ fwork, int ndim)
+{
+    const int4 w = fwork[blockIdx.x];
+    const int inst = w.x;
+    if (st[inst].phase != PH_INNER || st[inst].iter != 0) return;
+    const DcArgs& t = tab0[inst];
+    float* ptrs[2 + 2 * 3];
+    int np = 0;
+    ptrs[np++] = const_cast<float*>(t.din);
+    ptrs[np++] = t.dout;
+    for (int d = 0; d < ndim; ++d) {
+        ptrs[np++] = const_cast<float*>(t.win[d]);
+        ptrs[np++] = t.wout[d];
+    }
+    for (int k = threadIdx.x; k < w.z; k += blockDim.x) {
+        const long long e = (long long)w.y + k;
+        for (int q = 0; q < np; ++q) ptrs[q][e] = 0.0f;
+    }
+}
+
+__global__ void set_done_batch_kernel(BDev* st, int ninst, int v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ninst) st[i].done = v;
+}
+
+__global__ void parity_batch_kernel(const BDev* st, int* cur_parity, int ninst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    if (st[i].phase == PH_INNER) cur_parity[i] = st[i].iter & 1;
+}
+
+__global__ void tofloat_batch_kernel(const double* src, float* dst, long long n)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x)
+        dst[t] = __double2float_rn(src[t]);
+}
+
+// ---------------------------------------------------------------------------
+#define BCK(call)                                                 \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);       \
+    } while (0)
+
+struct Inst {
+    int nx, ny;
+    long long sy, nfield, off;
+    Derived dv;
+    ptd_params p;   // one-grid view of the instance
+};
+
+}  // namespace ptd
+
+using namespace ptd;
+
+struct ptd_batch {
+    ptd_batch_params bp;
+    int ninst = 0;
+    int model = 0;
+    bool df64 = false, dc = false;
+    std::vector<Inst> inst;
+    long long total = 0;       // elements of one concatenated field
+    cudaStream_t s = nullptr;
+    LaunchCfg cfg;
+    // plain PT (FP64 / DF64)
+    void* H[2] = {nullptr, nullptr};
+    void* Hold = nullptr;
+    void* W[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    void* D = nullptr;
+    double* stage = nullptr;
+    DevState* st = nullptr;
+    DevState* h_st = nullptr;
+    double* norm_den = nullptr;
+    PTArgs* tab[2] = {nullptr, nullptr};
+    // FP32 DC
+    double* H64 = nullptr;
+    double* Hold64 = nullptr;
+    double* D64 = nullptr;
+    float* Hf = nullptr;
+    float* Df = nullptr;
+    float* rf = nullptr;
+    float* d[2] = {nullptr, nullptr};
+    float* w32[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    BDev* bst = nullptr;
+    BDev* h_bst = nullptr;
+    DcArgs* dtab[2] = {nullptr, nullptr};
+    PTArgs* rtab = nullptr;
+    float** rf_ptrs = nullptr;
+    double** H_ptrs = nullptr;
+    int* cur_parity = nullptr;
+    int4* cwork = nullptr;
+    int ncwork = 0;
+    int4* fwork = nullptr;
+    int nfwork = 0;
+    // common
+    int4* work = nullptr;
+    int nwork = 0;
+    int nchk = 10;
+    int stall = 10;
+    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    int kernels_per_graph = 0;
+    long long launches = 0, iterations = 0;
+};
+
+namespace {
+
+int bfail(int status, const char* msg) { return set_error(status, msg); }
+
+template <class T>
+int balloc(T** p, size_t bytes)
+{
+    cudaError_t e = cudaMalloc((void**)p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(e == cudaErrorMemoryAllocation ? PTD_ENOMEM : PTD_ECUDA, "batch: cudaMalloc failed");
+    }
+    return PTD_OK;
+}
+
+cudaError_t launch_pt_batch(ptd_batch* b, int par, bool check)
+{
+    const dim3 blk(32, b->cfg.warps2d);
+    const bool c = check;
+    const PTArgs* t = b->tab[par];
+#define PTB(NT, M)                                                                                           \
+    (c ? pt2d_batch_kernel<NT, M, true><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)                \
+       : pt2d_batch_kernel<NT, M, false><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d))
+    if (b->df64) {
+        if (b->model == LIN) PTB(DF64, LIN);
+        else if (b->model == LINSTEP) PTB(DF64, LINSTEP);
+        else PTB(DF64, NONLIN);
+    } else {
+        if (b->model == LIN) PTB(F64, LIN);
+        else if (b->model == LINSTEP) PTB(F64, LINSTEP);
+        else PTB(F64, NONLIN);
+    }
+#undef PTB
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dc_batch(ptd_batch* b, int par, bool check)
+{
+    const dim3 blk(32, b->cfg.warps2d);
+    const DcArgs* t = b->dtab[par];
+#define DCB(M)                                                                                                 \
+    (check ? dc2d_batch_kernel<M, true><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)                 \
+           : dc2d_batch_kernel<M, false><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d))
+    if (b->model == LIN) DCB(LIN);
+    else if (b->model == LINSTEP) DCB(LINSTEP);
+    else DCB(NONLIN);
+#undef DCB
+    return cudaGetLastError();
+}
+
+void build_work(ptd_batch* b, std::vector<int4>& work)
+{
+    work.clear();
+    const int W = b->cfg.warps2d, ch = b->cfg.chunk2d;
+    for (int i = 0; i < b->ninst; ++i) {
+        const int tiles = (b->inst[i].nx - 2 + 30) / 31;
+        const int bx = (tiles + W - 1) / W;
+        const int by = (b->inst[i].ny - 2 + ch - 1) / ch;
+        for (int y = 0; y < by; ++y)
+            for (int x = 0; x < bx; ++x) work.push_back(make_int4(i, x, y, 0));
+    }
+}
+
+int upload_work(ptd_batch* b)
+{
+    std::vector<int4> work;
+    build_work(b, work);
+    if (b->work) cudaFree(b->work);
+    b->work = nullptr;
+    int rc = balloc(&b->work, work.size() * sizeof(int4));
+    if (rc) return rc;
+    BCK(cudaMemcpy(b->work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b->nwork = (int)work.size();
+    return PTD_OK;
+}
+
+int capture(ptd_batch* b)
+{
+    for (int q = 0; q < 2; ++q) {
+        if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
+        b->g[q] = nullptr;
+        cudaGraph_t gr = nullptr;
+        BCK(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
+        cudaError_t err = cudaSuccess;
+        int par = q, nk = 0;
+        for (int it = 0; it < b->nchk && err == cudaSuccess; ++it) {
+            const bool check = it == b->nchk - 1;
+            err = b->dc ? launch_dc_batch(b, par, check) : launch_pt_batch(b, par, check);
+            par ^= 1;
+            ++nk;
+        }
+        if (err == cudaSuccess) {
+            const int tb = 128, nb = (b->ninst + tb - 1) / tb;
+            if (b->dc)
+                inner_judge_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, b->ninst, b->nchk, b->bp.itmax,
+                                                              b->bp.norm == PTD_NORM_MAX, b->stall);
+            else
+                judge_batch_kernel<<<nb, tb, 0, b->s>>>(b->st, b->ninst, b->nchk, b->bp.itmax, b->bp.tol,
+                                                        b->norm_den, b->bp.norm == PTD_NORM_MAX);
+            err = cudaGetLastError();
+            ++nk;
+        }
+        cudaError_t e2 = cudaStreamEndCapture(b->s, &gr);
+        if (err != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return cuda_fail(err, "batch capture");
+        }
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+        cudaError_t e3 = cudaGraphInstantiate(&b->g[q], gr, 0);
+        cudaGraphDestroy(gr);
+        if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+        b->kernels_per_graph = nk;
+    }
+    return PTD_OK;
+}
+
+void one_grid_params(const ptd_batch_params& bp, int nx, int ny, ptd_params& p)
+{
+    std::memset(&p, 0, sizeof(p));
+    p.ndim = 2;
+    p.model = bp.model;
+    p.nx = nx;
+    p.ny = ny;
+    p.nz = 1;
+    p.lx = bp.lx;
+    p.ly = bp.ly;
+    p.lz = 1.0;
+    p.dt = bp.dt;
+    p.nt = bp.nt;
+    p.itmax = bp.itmax;
+    p.nchk = bp.nchk;
+    p.precision = bp.precision;
+    p.tol = bp.tol;
+    p.cfl = bp.cfl;
+    p.resc = bp.resc;
+    p.D = bp.D;
+    p.norm = bp.norm;
+}
+
+int fill_tables(ptd_batch* b)
+{
+    const int n = b->ninst;
+    if (!b->dc) {
+        std::vector<PTArgs> t[2] = {std::vector<PTArgs>(n), std::vector<PTArgs>(n)};
+        std::vector<double> nd(n);
+        const size_t es = sizeof(double);   // bytes per element (double or float2)
+        for (int i = 0; i < n; ++i) {
+            const Inst& I = b->inst[i];
+            nd[i] = I.dv.norm_den;
+            for (int q = 0; q < 2; ++q) {
+                PTArgs& a = t[q][i];
+                fill_args(I.p, I.dv, a);
+                a.sy = I.sy;
+                a.sz = I.nfield;
+                auto at = [&](void* base) -> char* { return (char*)base + (size_t)I.off * es; };
+                a.Hin = at(b->H[q]);
+                a.Hout = at(b->H[q ^ 1]);
+                a.Hold = at(b->Hold);
+                for (int d = 0; d < 3; ++d) {
+                    a.win[d] = at(b->W[d < 2 ? d : 0][q]);
+                    a.wout[d] = at(b->W[d < 2 ? d : 0][q ^ 1]);
+                }
+                a.D = b->D ? at(b->D) : nullptr;
+                a.done = &b->st[i].done;
+                a.acc = &b->st[i].acc;
+            }
+        }
+        for (int q = 0; q < 2; ++q)
+            BCK(cudaMemcpy(b->tab[q], t[q].data(), n * sizeof(PTArgs), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(b->norm_den, nd.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        return PTD_OK;
+    }
+    std::vector<DcArgs> t[2] = {std::vector<DcArgs>(n), std::vector<DcArgs>(n)};
+    std::vector<PTArgs> r(n);
+    std::vector<float*> rp(n);
+    std::vector<double*> hp(n);
+    std::vector<BDev> bd(n);
+    for (int i = 0; i < n; ++i) {
+        const Inst& I = b->inst[i];
+        for (int q = 0; q < 2; ++q) {
+            DcArgs& a = t[q][i];
+            std::memset(&a, 0, sizeof(a));
+            a.nx = I.nx;
+            a.ny = I.ny;
+            a.nz = 1;
+            a.sy = I.sy;
+            a.sz = I.nfield;
+            a.rdt = (float)I.dv.rdt;
+            for (int d = 0; d < 3; ++d) a.sig[d] = (float)I.dv.sig[d];
+            a.c_lin = (float)I.dv.c_lin;
+            a.e_lin = (float)I.dv.e_lin;
+            a.f = fparams(I.dv);
+            a.din = b->d[q] + I.off;
+            a.dout = b->d[q ^ 1] + I.off;
+            for (int d = 0; d < 3; ++d) {
+                a.win[d] = b->w32[d < 2 ? d : 0][q] + I.off;
+                a.wout[d] = b->w32[d < 2 ? d : 0][q ^ 1] + I.off;
+            }
+            a.Hf = b->Hf + I.off;
+            a.Df = b->Df ? b->Df + I.off : nullptr;
+            a.r = b->rf + I.off;
+            a.done = &b->bst[i].done;
+            a.acc = &b->bst[i].acc;
+            a.norm_max = b->bp.norm == PTD_NORM_MAX;
+        }
+        PTArgs& a = r[i];
+        fill_args(I.p, I.dv, a);
+        a.sy = I.sy;
+        a.sz = I.nfield;
+        a.Hin = b->H64 + I.off;
+        a.Hold = b->Hold64 + I.off;
+        a.D = b->D64 ? b->D64 + I.off : nullptr;
+        rp[i] = b->rf + I.off;
+        hp[i] = b->H64 + I.off;
+        std::memset(&bd[i], 0, sizeof(BDev));
+        bd[i].norm_den = I.dv.norm_den;
+        double cs = 0.0;
+        for (int d = 0; d < 2; ++d) cs += 4.0 / (I.dv.h[d] * I.dv.h[d]);
+        bd[i].cond_scale = cs * b->bp.dt;
+        bd[i].dconst = b->bp.D;
+        bd[i].done = 1;
+        bd[i].phase = PH_CONVERGED;
+    }
+    for (int q = 0; q < 2; ++q)
+        BCK(cudaMemcpy(b->dtab[q], t[q].data(), n * sizeof(DcArgs), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->rtab, r.data(), n * sizeof(PTArgs), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->rf_ptrs, rp.data(), n * sizeof(float*), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->H_ptrs, hp.data(), n * sizeof(double*), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->bst, bd.data(), n * sizeof(BDev), cudaMemcpyHostToDevice));
+    // cell work (inner cells, residual) and field work (whole fields, apply)
+    std::vector<int4> cw, fw;
+    const int CH = 2048;
+    for (int i = 0; i < n; ++i) {
+        const Inst& I = b->inst[i];
+        const long long cells = (long long)(I.nx - 2) * (I.ny - 2);
+        for (long long s0 = 0; s0 < cells; s0 += CH)
+            cw.push_back(make_int4(i, (int)s0, (int)std::min<long long>(CH, cells - s0), 0));
+        for (long long s0 = 0; s0 < I.nfield; s0 += CH)
+            fw.push_back(make_int4(i, (int)s0, (int)std::min<long long>(CH, I.nfield - s0), 0));
+    }
+    int rc = balloc(&b->cwork, cw.size() * sizeof(int4));
+    if (!rc) rc = balloc(&b->fwork, fw.size() * sizeof(int4));
+    if (rc) return rc;
+    BCK(cudaMemcpy(b->cwork, cw.data(), cw.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->fwork, fw.data(), fw.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b->ncwork = (int)cw.size();
+    b->nfwork = (int)fw.size();
+    return PTD_OK;
+}
+
+void free_batch(ptd_batch* b)
+{
+    if (!b) return;
+    if (b->s) cudaStreamSynchronize(b->s);
+    for (int q = 0; q < 2; ++q)
+        if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
+    void* ptrs[] = {b->H[0], b->H[1], b->Hold, b->W[0][0], b->W[0][1], b->W[1][0], b->W[1][1], b->D,
+                    b->stage, b->st, b->norm_den, b->tab[0], b->tab[1], b->H64, b->Hold64, b->D64, b->Hf,
+                    b->Df, b->rf, b->d[0], b->d[1], b->w32[0][0], b->w32[0][1], b->w32[1][0], b->w32[1][1],
+                    b->bst, b->dtab[0], b->dtab[1], b->rtab, b->rf_ptrs, b->H_ptrs, b->cur_parity,
+                    b->cwork, b->fwork, b->work};
+    for (void* p : ptrs) cudaFree(p);
+    if (b->h_st) cudaFreeHost(b->h_st);
+    if (b->h_bst) cudaFreeHost(b->h_bst);
+    if (b->s) cudaStreamDestroy(b->s);
+    delete b;
+}
+
+// Upload instance fields: src[i] (nx_i*ny_i doubles, host or device) into
+// the concatenated padded field dst (FP64).
+int upload(ptd_batch* b, double* dst, const double* const* src)
+{
+    for (int i = 0; i < b->ninst; ++i) {
+        const Inst& I = b->inst[i];
+        const size_t w = (size_t)I.nx * sizeof(double);
+        BCK(cudaMemcpy2DAsync(dst + I.off, (size_t)I.sy * sizeof(double), src[i], w, w, I.ny, cudaMemcpyDefault,
+                              b->s));
+    }
+    return PTD_OK;
+}
+
+int download(ptd_batch* b, double* const* dst, const double* src)
+{
+    for (int i = 0; i < b->ninst; ++i) {
+        const Inst& I = b->inst[i];
+        const size_t w = (size_t)I.nx * sizeof(double);
+        BCK(cudaMemcpy2DAsync(dst[i], w, src + I.off, (size_t)I.sy * sizeof(double), w, I.ny, cudaMemcpyDefault,
+                              b->s));
+    }
+    return PTD_OK;
+}
+
+}  // namespace
+
+extern "C" int ptd_batch_params_init(ptd_batch_params* p, int32_t ninst, int32_t model)
+{
+    if (!p) return bfail(PTD_EINVAL, "ptd_batch_params_init: p is NULL");
+    if (ninst < 1) return bfail(PTD_EINVAL, "ninst must be >= 1");
+    ptd_params q;
+    int rc = ptd_params_init(&q, 2, model);
+    if (rc) return rc;
+    std::memset(p, 0, sizeof(*p));
+    p->ninst = ninst;
+    p->model = model;
+    p->lx = q.lx;
+    p->ly = q.ly;
+    p->dt = q.dt;
+    p->nt = q.nt;
+    p->itmax = q.itmax;
+    p->nchk = q.nchk;
+    p->precision = PTD_PREC_FP64;
+    p->tol = q.tol;
+    p->cfl = q.cfl;
+    p->resc = q.resc;
+    p->D = q.D;
+    p->norm = PTD_NORM_RMS;
+    return PTD_OK;
+}
+
+extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, const int32_t* nx, const int32_t* ny)
+{
+    if (!out) return bfail(PTD_EINVAL, "ptd_batch_create: out is NULL");
+    *out = nullptr;
+    if (!p || !nx || !ny) return bfail(PTD_EINVAL, "ptd_batch_create: NULL argument");
+    if (p->ninst < 1) return bfail(PTD_EINVAL, "ninst must be >= 1");
+    if (p->nchk < 1 || p->itmax < p->nchk || p->itmax % p->nchk)
+        return bfail(PTD_EINVAL, "batch: itmax must be a positive multiple of nchk");
+    for (int k = 0; k < 8; ++k)
+        if (p->reserved[k]) return bfail(PTD_EINVAL, "reserved fields must be zero");
+    ptd_batch* b = new (std::nothrow) ptd_batch();
+    if (!b) return bfail(PTD_ENOMEM, "batch: host allocation failed");
+    b->bp = *p;
+    b->ninst = p->ninst;
+    b->model = p->model;
+    b->df64 = p->precision == PTD_PREC_DF64;
+    b->dc = p->precision == PTD_PREC_FP32_DC;
+    b->inst.resize(b->ninst);
+    long long off = 0;
+    int rc = PTD_OK;
+    for (int i = 0; i < b->ninst && !rc; ++i) {
+        Inst& I = b->inst[i];
+        one_grid_params(*p, nx[i], ny[i], I.p);
+        rc = validate(&I.p);
+        if (rc) break;
+        derive(I.p, I.dv);
+        I.nx = nx[i];
+        I.ny = ny[i];
+        I.sy = ((nx[i] + 31) / 32) * 32;
+        I.nfield = I.sy * ny[i];
+        I.off = off;
+        off += ((I.nfield + 63) / 64) * 64;
+    }
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    b->total = off;
+    {
+        ptd_params q = b->inst[0].p;
+        int nmax = 0;
+        for (auto& I : b->inst) nmax = std::max(nmax, std::max(I.nx, I.ny));
+        q.nx = q.ny = nmax;
+        b->cfg = tuned_config(q);
+        b->cfg.chunk2d = 32;
+        b->stall = std::max(10, (2 * nmax + 49) / 50);
+    }
+    b->nchk = b->dc ? std::max(1, std::min(p->nchk, 50)) : p->nchk;
+    if (b->dc && p->itmax % b->nchk) b->nchk = p->nchk;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return cuda_fail(e, "cudaStreamCreateWithFlags");
+    }
+    const size_t db = (size_t)b->total * sizeof(double), fb = (size_t)b->total * sizeof(float);
+    const int n = b->ninst;
+    if (!b->dc) {
+        for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->H[q], db);
+        if (!rc) rc = balloc(&b->Hold, db);
+        for (int d = 0; d < 2 && !rc; ++d)
+            for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->W[d][q], db);
+        if (!rc && p->model == PTD_MODEL_LINSTEP) rc = balloc(&b->D, db);
+        if (!rc && b->df64) rc = balloc(&b->stage, db);
+        if (!rc) rc = balloc(&b->st, n * sizeof(DevState));
+        if (!rc) rc = balloc(&b->norm_den, n * sizeof(double));
+        for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->tab[q], n * sizeof(PTArgs));
+        if (!rc && cudaMallocHost((void**)&b->h_st, n * sizeof(DevState)) != cudaSuccess)
+            rc = bfail(PTD_ENOMEM, "batch: cudaMallocHost failed");
+        if (!rc) {
+            e = cudaMemset(b->st, 0, n * sizeof(DevState));
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemset");
+        }
+    } else {
+        if (!rc) rc = balloc(&b->H64, db);
+        if (!rc) rc = balloc(&b->Hold64, db);
+        if (!rc && p->model == PTD_MODEL_LINSTEP) rc = balloc(&b->D64, db);
+        if (!rc) rc = balloc(&b->Hf, fb);
+        if (!rc && p->model == PTD_MODEL_LINSTEP) rc = balloc(&b->Df, fb);
+        if (!rc) rc = balloc(&b->rf, fb);
+        for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->d[q], fb);
+        for (int d = 0; d < 2 && !rc; ++d)
+            for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->w32[d][q], fb);
+        if (!rc) rc = balloc(&b->bst, n * sizeof(BDev));
+        for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->dtab[q], n * sizeof(DcArgs));
+        if (!rc) rc = balloc(&b->rtab, n * sizeof(PTArgs));
+        if (!rc) rc = balloc(&b->rf_ptrs, n * sizeof(float*));
+        if (!rc) rc = balloc(&b->H_ptrs, n * sizeof(double*));
+        if (!rc) rc = balloc(&b->cur_parity, n * sizeof(int));
+        if (!rc && cudaMallocHost((void**)&b->h_bst, n * sizeof(BDev)) != cudaSuccess)
+            rc = bfail(PTD_ENOMEM, "batch: cudaMallocHost failed");
+    }
+    if (!rc) {
+        void* zs[] = {b->H[0], b->H[1], b->Hold, b->W[0][0], b->W[0][1], b->W[1][0], b->W[1][1], b->D,
+                      b->H64, b->Hold64, b->D64};
+        for (void* z : zs)
+            if (z && cudaMemset(z, 0, db) != cudaSuccess) rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
+        float* zf[] = {b->Hf, b->Df, b->rf, b->d[0], b->d[1], b->w32[0][0], b->w32[0][1], b->w32[1][0],
+                       b->w32[1][1]};
+        for (float* z : zf)
+            if (z && cudaMemset(z, 0, fb) != cudaSuccess) rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
+    }
+    if (!rc) rc = fill_tables(b);
+    if (!rc) rc = upload_work(b);
+    if (!rc) rc = capture(b);
+    if (rc) {
+        free_batch(b);
+        return rc;
+    }
+    *out = b;
+    return PTD_OK;
+}
+
+extern "C" void ptd_batch_destroy(ptd_batch* b) { free_batch(b); }
+
+extern "C" int ptd_batch_counters(ptd_batch* b, int64_t* launches, int64_t* iterations)
+{
+    if (!b) return bfail(PTD_EINVAL, "batch is NULL");
+    if (launches) *launches = b->launches;
+    if (iterations) *iterations = b->iterations;
+    return PTD_OK;
+}
+
+static int batch_read_states(ptd_batch* b)
+{
+    if (b->dc) BCK(cudaMemcpyAsync(b->h_bst, b->bst, b->ninst * sizeof(BDev), cudaMemcpyDeviceToHost, b->s));
+    else BCK(cudaMemcpyAsync(b->h_st, b->st, b->ninst * sizeof(DevState), cudaMemcpyDeviceToHost, b->s));
+    BCK(cudaStreamSynchronize(b->s));
+    return PTD_OK;
+}
+
+// Plain PT: one physical step of every instance.
+static int batch_pt_step(ptd_batch* b, int32_t* iters, double* err_last, int* nan_any)
+{
+    const int n = b->ninst, tb = 128, nb = (n + tb - 1) / tb;
+    reset_batch_kernel<<<nb, tb, 0, b->s>>>(b->st, n);
+    BCK(cudaGetLastError());
+    b->launches += 1;
+    const long long blocks_max = b->bp.itmax / b->nchk;
+    long long launched = 0, batch = 1;
+    while (launched < blocks_max) {
+        const long long k = std::min(batch, blocks_max - launched);
+        for (long long j = 0; j < k; ++j) {
+            BCK(cudaGraphLaunch(b->g[(int)(((launched + j) * b->nchk) & 1)], b->s));
+            b->launches += b->kernels_per_graph;
+        }
+        launched += k;
+        int rc = batch_read_states(b);
+        if (rc) return rc;
+        bool all = true;
+        for (int i = 0; i < n; ++i) all = all && b->h_st[i].done != DONE_RUNNING;
+        if (all) break;
+        batch = std::min<long long>(batch * 2, 64);
+    }
+    // bring every instance back to parity 0, then Hold <- H
+    const size_t es = sizeof(double);
+    for (int i = 0; i < n; ++i) {
+        const DevState& s = b->h_st[i];
+        iters[i] = s.iter;
+        b->iterations += s.iter;
+        if (err_last) err_last[i] = s.err;
+        if (s.done == DONE_NAN) *nan_any = 1;
+        if (s.iter & 1) {
+            const Inst& I = b->inst[i];
+            const size_t bytes = (size_t)I.nfield * es, o = (size_t)I.off * es;
+            BCK(cudaMemcpyAsync((char*)b->H[0] + o, (char*)b->H[1] + o, bytes, cudaMemcpyDeviceToDevice, b->s));
+            for (int d = 0; d < 2; ++d)
+                BCK(cudaMemcpyAsync((char*)b->W[d][0] + o, (char*)b->W[d][1] + o, bytes, cudaMemcpyDeviceToDevice,
+                                    b->s));
+        }
+    }
+    BCK(cudaMemcpyAsync(b->Hold, b->H[0], (size_t)b->total * es, cudaMemcpyDeviceToDevice, b->s));
+    return PTD_OK;
+}
+
+static int batch_residual(ptd_batch* b)
+{
+    if (b->model == LIN) resid64_batch_kernel<LIN><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork);
+    else if (b->model == LINSTEP)
+        resid64_batch_kernel<LINSTEP><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork);
+    else resid64_batch_kernel<NONLIN><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork);
+    BCK(cudaGetLastError());
+    const int n = b->ninst, tb = 128, nb = (n + tb - 1) / tb;
+    const double rtol = b->bp.dc_inner_rtol > 0.0 ? b->bp.dc_inner_rtol : 1e-3;
+    const int max_outer = b->bp.dc_max_outer > 0 ? b->bp.dc_max_outer : 30;
+    outer_judge_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, n, b->bp.norm == PTD_NORM_MAX, b->bp.tol, rtol, max_outer,
+                                                   b->bp.itmax, b->model == NONLIN);
+    BCK(cudaGetLastError());
+    b->launches += 2;
+    return PTD_OK;
+}
+
+// FP32 defect correction: one physical step of every instance.
+static int batch_dc_step(ptd_batch* b, int32_t* iters, double* err_last, int* nan_any, int* capped_any)
+{
+    const int n = b->ninst, tb = 128, nb = (n + tb - 1) / tb;
+    start_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, n);
+    BCK(cudaGetLastError());
+    int rc = batch_residual(b);
+    if (rc) return rc;
+    for (int round = 0; round < 4 * 64; ++round) {
+        rc = batch_read_states(b);
+        if (rc) return rc;
+        bool all_fin = true, any_inner = false;
+        for (int i = 0; i < n; ++i) {
+            all_fin = all_fin && b->h_bst[i].phase >= PH_CONVERGED;
+            any_inner = any_inner || b->h_bst[i].phase == PH_INNER;
+        }
+        if (all_fin) break;
+        if (any_inner) {
+            zero_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->dtab[0], b->bst, b->fwork, 2);
+            BCK(cudaGetLastError());
+            b->launches += 1;
+            long long launched = 0, batch = 1;
+            const long long blocks_max = b->bp.itmax / b->nchk;
+            while (launched < blocks_max) {
+                const long long k = std::min(batch, blocks_max - launched);
+                for (long long j = 0; j < k; ++j) {
+                    BCK(cudaGraphLaunch(b->g[(int)(((launched + j) * b->nchk) & 1)], b->s));
+                    b->launches += b->kernels_per_graph;
+                }
+                launched += k;
+                rc = batch_read_states(b);
+                if (rc) return rc;
+                bool all = true;
+                for (int i = 0; i < n; ++i) all = all && b->h_bst[i].done;
+                if (all) break;
+                batch = std::min<long long>(batch * 2, 32);
+            }
+            for (int i = 0; i < n; ++i)
+                if (b->h_bst[i].phase == PH_INNER) b->iterations += b->h_bst[i].iter;
+            parity_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, b->cur_parity, n);
+            BCK(cudaGetLastError());
+        }
+        apply_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->dtab[0], b->bst, b->fwork, b->H_ptrs, b->cur_parity);
+        BCK(cudaGetLastError());
+        b->launches += 2;
+        rc = batch_residual(b);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < n; ++i) {
+        const BDev& s = b->h_bst[i];
+        iters[i] = s.total_inner;
+        if (err_last) err_last[i] = s.err_ref;
+        if (s.phase == PH_NAN) *nan_any = 1;
+        if (s.phase == PH_CAPPED || s.phase < PH_CONVERGED) *capped_any = 1;
+    }
+    BCK(cudaMemcpyAsync(b->Hold64, b->H64, (size_t)b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->s));
+    return PTD_OK;
+}
+
+extern "C" int ptd_batch_solve(ptd_batch* b, double* const* H, const double* const* D, int32_t* iters,
+                               double* err_last, int32_t* n_done)
+{
+    if (!b) return bfail(PTD_EINVAL, "batch is NULL");
+    if (!H || !iters) return bfail(PTD_EINVAL, "ptd_batch_solve: H and iters are required");
+    if (b->model == PTD_MODEL_LINSTEP && !D) return bfail(PTD_EINVAL, "the step model needs D");
+    for (int i = 0; i < b->ninst; ++i)
+        if (!H[i] || (b->model == PTD_MODEL_LINSTEP && !D[i])) return bfail(PTD_EINVAL, "NULL instance field");
+    const size_t db = (size_t)b->total * sizeof(double);
+    int rc;
+    const int n = b->ninst;
+    if (!b->dc) {
+        double* h0 = b->df64 ? b->stage : (double*)b->H[0];
+        BCK(cudaMemsetAsync(h0, 0, db, b->s));
+        if ((rc = upload(b, h0, H))) return rc;
+        if (b->df64) BCK(launch_to_df64(h0, b->H[0], b->total, b->s));
+        BCK(cudaMemcpyAsync(b->H[1], b->H[0], db, cudaMemcpyDeviceToDevice, b->s));
+        BCK(cudaMemcpyAsync(b->Hold, b->H[0], db, cudaMemcpyDeviceToDevice, b->s));
+        for (int d = 0; d < 2; ++d)
+            for (int q = 0; q < 2; ++q) BCK(cudaMemsetAsync(b->W[d][q], 0, db, b->s));
+        if (b->D) {
+            double* d0 = b->df64 ? b->stage : (double*)b->D;
+            BCK(cudaMemsetAsync(d0, 0, db, b->s));
+            if ((rc = upload(b, d0, D))) return rc;
+            if (b->df64) BCK(launch_to_df64(d0, b->D, b->total, b->s));
+        }
+    } else {
+        BCK(cudaMemsetAsync(b->H64, 0, db, b->s));
+        if ((rc = upload(b, b->H64, H))) return rc;
+        BCK(cudaMemcpyAsync(b->Hold64, b->H64, db, cudaMemcpyDeviceToDevice, b->s));
+        tofloat_batch_kernel<<<152 * 8, 256, 0, b->s>>>(b->H64, b->Hf, b->total);
+        BCK(cudaGetLastError());
+        if (b->D64) {
+            BCK(cudaMemsetAsync(b->D64, 0, db, b->s));
+            if ((rc = upload(b, b->D64, D))) return rc;
+            tofloat_batch_kernel<<<152 * 8, 256, 0, b->s>>>(b->D64, b->Df, b->total);
+            BCK(cudaGetLastError());
+        }
+        BCK(cudaMemsetAsync(b->rf, 0, (size_t)b->total * sizeof(float), b->s));
+        BCK(cudaMemsetAsync(b->cur_parity, 0, n * sizeof(int), b->s));
+    }
+    std::vector<int32_t> it(n);
+    int nan_any = 0, capped_any = 0;
+    for (int step = 0; step < b->bp.nt; ++step) {
+        rc = b->dc ? batch_dc_step(b, it.data(), err_last, &nan_any, &capped_any)
+                   : batch_pt_step(b, it.data(), err_last, &nan_any);
+        if (rc) return rc;
+        for (int i = 0; i < n; ++i) iters[(size_t)i * b->bp.nt + step] = it[i];
+        if (nan_any) break;
+    }
+    if (!b->dc && b->df64) {
+        BCK(launch_from_df64(b->H[0], b->stage, b->total, b->s));
+        rc = download(b, H, b->stage);
+    } else {
+        rc = download(b, H, b->dc ? b->H64 : (double*)b->H[0]);
+    }
+    if (rc) return rc;
+    BCK(cudaStreamSynchronize(b->s));
+    if (n_done) *n_done = n;
+    if (nan_any) return bfail(PTD_ENAN, "an instance's residual is NaN");
+    if ((b->bp.flags & PTD_FLAG_STRICT) && capped_any) return bfail(PTD_ENOTCONV, "an instance did not converge");
+    return PTD_OK;
+}
+
+// Autotuner: time each (warps per block, rows per y chunk) candidate on the
+// current state with a few plain iterations, keep the fastest, re-capture.
+extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_out, float* us_out)
+{
+    if (!b) return bfail(PTD_EINVAL, "batch is NULL");
+    const int Ws[] = {2, 4, 8};
+    const int Cs[] = {16, 32, 64, 128};
+    float best = 1e30f;
+    LaunchCfg keep = b->cfg, bestc = b->cfg;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    // plain iterations on the current fields with every instance's flag cleared
+    // (the fields are zero after ptd_batch_create; ptd_batch_solve uploads its
+    // own state afterwards)
+    if (b->dc) {
+        set_done_batch_kernel<<<(b->ninst + 127) / 128, 128, 0, b->s>>>(b->bst, b->ninst, 0);
+        BCK(cudaGetLastError());
+    } else {
+        BCK(cudaMemsetAsync(b->st, 0, b->ninst * sizeof(DevState), b->s));
+    }
+    for (int W : Ws)
+        for (int C : Cs) {
+            b->cfg.warps2d = W;
+            b->cfg.chunk2d = C;
+            int rc = upload_work(b);
+            if (rc) return rc;
+            for (int rep = 0; rep < 2; ++rep) {
+                BCK(cudaEventRecord(e0, b->s));
+                for (int it = 0; it < 6; ++it)
+                    BCK(b->dc ? launch_dc_batch(b, it & 1, false) : launch_pt_batch(b, it & 1, false));
+                BCK(cudaEventRecord(e1, b->s));
+                BCK(cudaEventSynchronize(e1));
+            }
+            float ms = 0.0f;
+            BCK(cudaEventElapsedTime(&ms, e0, e1));
+            b->launches += 12;
+            if (ms < best) {
+                best = ms;
+                bestc = b->cfg;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (b->dc) {
+        set_done_batch_kernel<<<(b->ninst + 127) / 128, 128, 0, b->s>>>(b->bst, b->ninst, 1);
+        BCK(cudaGetLastError());
+    }
+    (void)keep;
+    b->cfg = bestc;
+    int rc = upload_work(b);
+    if (!rc) rc = capture(b);
+    if (rc) return rc;
+    if (warps_out) *warps_out = bestc.warps2d;
+    if (chunk_out) *chunk_out = bestc.chunk2d;
+    if (us_out) *us_out = best * 1000.0f / 6.0f;
+    return PTD_OK;
+}

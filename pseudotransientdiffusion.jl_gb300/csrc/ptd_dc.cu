@@ -28,108 +28,17 @@
 #include <new>
 
 #include "ptd_internal.h"
+#include "ptd_dc_body.cuh"
 
 namespace ptd {
 
-struct DcArgs {
-    int nx, ny, nz;
-    long long sy, sz;
-    float rdt;
-    float sig[3];
-    float c_lin, e_lin;
-    FParams f;
-    const float* din;     // correction delta (iteration k)
-    float* dout;          // correction delta (iteration k+1)
-    const float* win[3];
-    float* wout[3];
-    const float* Hf;      // FP32 copy of H (linearisation point)
-    const float* Df;      // LINSTEP: FP32 copy of D
-    const float* r;       // FP32 copy of the FP64 residual
-    const int* done;
-    double* acc;
-    int norm_max;
-};
-
-// Control block of the inner solve (device), see DevState in ptd_kernels.h.
-struct DcDev {
-    int done;
-    int nchecks;
-    int iter;
-    int best_at;       // check index of the smallest inner err so far
-    double acc;        // inner residual accumulator
-    double err;        // last inner err
-    double best;       // smallest inner err so far
-    double target;     // inner stopping threshold
-    double outer_acc;  // FP64 residual accumulator
-    double outer_err;  // FP64 residual norm
-    unsigned long long hmax_bits;  // max |H| over the grid (bit pattern), for the FP32 floor
-};
-
-// One face of the linearised flux (scaled like ptd_device.cuh):
-// u = K_f (d_R - d_L) [+ 3 s^2 (h_R - h_L) (d_L + d_R)],  w <- w - c (w + u).
-template <int MODEL, bool U>
-__device__ __forceinline__ float face32(const DcArgs& a, float dL, float dR, float hL, float hR, float DL,
-                                        float DR, float w, float& u)
-{
-    const float gd = dR - dL;
-    float uu, c;
-    if (MODEL == LIN) {
-        uu = gd;
-        c = a.c_lin;
-    } else if (MODEL == LINSTEP) {
-        uu = (DL + DR) * gd;
-        c = a.c_lin;
-    } else {
-        const float s = hL + hR;
-        const float s2 = s * s;
-        uu = s2 * s * gd;
-        uu = fmaf(3.0f * s2 * (hR - hL), dL + dR, uu);
-        c = nonlin_face_c(a.f, s);
-    }
-    if (U) u = uu;
-    return fmaf(-c, w + uu, w);
-}
-
-template <int MODEL>
-__device__ __forceinline__ float cell_e32(const DcArgs& a, float h, float dmax)
-{
-    if (MODEL == LIN) return a.e_lin;
-    if (MODEL == LINSTEP) return linstep_cell_e(a.f, dmax);
-    return nonlin_cell_e(a.f, h);
-}
-
-__device__ __forceinline__ bool dc_done(const int* done) { return __ldcg(done) != 0; }
-
-// ---------------------------------------------------------------------------
 template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) dc1d_kernel(DcArgs a)
 {
     if (dc_done(a.done)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nx = a.nx;
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    if (i < nx) {
-        const float dc = a.din[i], hc = a.Hf[i];
-        const float Dc = MODEL == LINSTEP ? a.Df[i] : 0.0f;
-        float wr = 0.0f, ur = 0.0f, Dr = 0.0f;
-        if (i <= nx - 2) {
-            Dr = MODEL == LINSTEP ? a.Df[i + 1] : 0.0f;
-            wr = face32<MODEL, CHECK>(a, dc, a.din[i + 1], hc, a.Hf[i + 1], Dc, Dr, a.win[0][i], ur);
-            a.wout[0][i] = wr;
-        }
-        if (i >= 1 && i <= nx - 2) {
-            const float Dl = MODEL == LINSTEP ? a.Df[i - 1] : 0.0f;
-            float ul = 0.0f;
-            const float wl = face32<MODEL, CHECK>(a, a.din[i - 1], dc, a.Hf[i - 1], hc, Dl, Dc, a.win[0][i - 1], ul);
-            const float rr = a.r[i];
-            const float e = cell_e32<MODEL>(a, hc, fmaxf(fmaxf(Dl, Dr), Dc));
-            const float div = (wr - wl) * a.sig[0];
-            const float dn = fmaf(-e, fmaf(dc, a.rdt, div - rr), dc);
-            a.dout[i] = dn;
-            if (CHECK) accumulate_residual((double)fmaf(-dn, a.rdt, rr + (ur - ul) * a.sig[0]), part, pmax);
-        }
-    }
+    dc1d_body<MODEL, CHECK>(a, blockIdx.x, part, pmax);
     if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
@@ -137,70 +46,9 @@ template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) dc2d_kernel(DcArgs a, int chunk)
 {
     if (dc_done(a.done)) return;
-    const int lane = threadIdx.x;
-    const int tile = blockIdx.x * blockDim.y + threadIdx.y;
-    const int i = 31 * tile + lane;
-    const int nx = a.nx, ny = a.ny;
-    const int j0 = 1 + blockIdx.y * chunk;
-    const int j1 = min(j0 + chunk, ny - 1);
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    if ((31 * tile < nx - 1) && (j0 < j1)) {
-        const int ic = min(i, nx - 1);
-        const bool xface = i <= nx - 2;
-        const bool upd = i >= 1 && i <= nx - 2 && lane >= 1;
-        const bool own_x = xface && (lane >= 1 || tile == 0);
-        const long long sy = a.sy;
-        long long idx = (long long)j0 * sy + ic;
-        float dc = a.din[idx], hc = a.Hf[idx];
-        float Dc = MODEL == LINSTEP ? a.Df[idx] : 0.0f, Db = 0.0f;
-        float wyb = 0.0f, uyb = 0.0f;
-        if (upd) {
-            Db = MODEL == LINSTEP ? a.Df[idx - sy] : 0.0f;
-            wyb = face32<MODEL, CHECK>(a, a.din[idx - sy], dc, a.Hf[idx - sy], hc, Db, Dc, a.win[1][idx - sy], uyb);
-            if (j0 == 1) a.wout[1][idx - sy] = wyb;
-        }
-        for (int j = j0; j < j1; ++j, idx += sy) {
-            const float dn = a.din[idx + sy], hn = a.Hf[idx + sy];
-            const float wx = a.win[0][idx], wy = a.win[1][idx], rr = a.r[idx];
-            const float Dn = MODEL == LINSTEP ? a.Df[idx + sy] : 0.0f;
-            float dr = __shfl_down_sync(FULL, dc, 1);
-            float hr = __shfl_down_sync(FULL, hc, 1);
-            float Dr = MODEL == LINSTEP ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
-            if (lane == 31) {
-                const bool ok = ic + 1 < nx;
-                dr = ok ? a.din[idx + 1] : dc;
-                hr = ok ? a.Hf[idx + 1] : hc;
-                if (MODEL == LINSTEP) Dr = ok ? a.Df[idx + 1] : Dc;
-            }
-            float ux = 0.0f, uy = 0.0f, wxn = 0.0f, wyn = 0.0f;
-            if (xface) wxn = face32<MODEL, CHECK>(a, dc, dr, hc, hr, Dc, Dr, wx, ux);
-            if (upd) wyn = face32<MODEL, CHECK>(a, dc, dn, hc, hn, Dc, Dn, wy, uy);
-            const float wxl = __shfl_up_sync(FULL, wxn, 1);
-            const float uxl = CHECK ? __shfl_up_sync(FULL, ux, 1) : 0.0f;
-            const float Dl = MODEL == LINSTEP ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
-            if (own_x) a.wout[0][idx] = wxn;
-            if (upd) {
-                a.wout[1][idx] = wyn;
-                const float e = cell_e32<MODEL>(a, hc, fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Db)), Dn));
-                const float div = fmaf(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]);
-                const float dnew = fmaf(-e, fmaf(dc, a.rdt, div - rr), dc);
-                a.dout[idx] = dnew;
-                if (CHECK) {
-                    const float divu = fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]);
-                    accumulate_residual((double)fmaf(-dnew, a.rdt, rr + divu), part, pmax);
-                }
-            }
-            dc = dn;
-            hc = hn;
-            wyb = wyn;
-            uyb = uy;
-            if (MODEL == LINSTEP) {
-                Db = Dc;
-                Dc = Dn;
-            }
-        }
-    }
+    dc2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
     if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
@@ -208,107 +56,9 @@ template <int MODEL, bool CHECK, int R>
 __global__ void __launch_bounds__(32 * R) dc3d_kernel(DcArgs a, int chunk)
 {
     if (dc_done(a.done)) return;
-    __shared__ float sd[2][R][32];
-    __shared__ float sh[2][R][32];
-    __shared__ float sw[2][R][32];
-    __shared__ float su[CHECK ? 2 : 1][CHECK ? R : 1][32];
-    __shared__ float sD[MODEL == LINSTEP ? 2 : 1][MODEL == LINSTEP ? R : 1][32];
-    const int lane = threadIdx.x, r = threadIdx.y;
-    const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const int i = 31 * blockIdx.x + lane;
-    const int j = (R - 1) * blockIdx.y + r;
-    const int k0 = 1 + blockIdx.z * chunk;
-    const int k1 = min(k0 + chunk, nz - 1);
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    if (k0 < k1) {
-        const int ic = min(i, nx - 1), jc = min(j, ny - 1);
-        const bool inner_x = i >= 1 && i <= nx - 2, inner_y = j >= 1 && j <= ny - 2;
-        const bool xface = i <= nx - 2 && inner_y && r >= 1;
-        const bool yface = j <= ny - 2 && inner_x;
-        const bool upd = inner_x && inner_y && lane >= 1 && r >= 1;
-        const bool own_x = xface && (lane >= 1 || blockIdx.x == 0);
-        const bool own_y = yface && lane >= 1 && (r >= 1 || blockIdx.y == 0);
-        const bool top = r == R - 1, up_ok = jc + 1 < ny;
-        const long long sy = a.sy, sz = a.sz;
-        long long idx = (long long)k0 * sz + (long long)jc * sy + ic;
-        float dc = a.din[idx], hc = a.Hf[idx];
-        float Dc = MODEL == LINSTEP ? a.Df[idx] : 0.0f, Db = 0.0f;
-        float wzb = 0.0f, uzb = 0.0f;
-        if (upd) {
-            Db = MODEL == LINSTEP ? a.Df[idx - sz] : 0.0f;
-            wzb = face32<MODEL, CHECK>(a, a.din[idx - sz], dc, a.Hf[idx - sz], hc, Db, Dc, a.win[2][idx - sz], uzb);
-            if (k0 == 1) a.wout[2][idx - sz] = wzb;
-        }
-        int p = 0;
-        sd[0][r][lane] = dc;
-        sh[0][r][lane] = hc;
-        if (MODEL == LINSTEP) sD[0][r][lane] = Dc;
-        __syncthreads();
-        for (int k = k0; k < k1; ++k, idx += sz) {
-            const float dn = a.din[idx + sz], hn = a.Hf[idx + sz];
-            const float wx = a.win[0][idx], wy = a.win[1][idx], wz = a.win[2][idx], rr = a.r[idx];
-            const float Dn = MODEL == LINSTEP ? a.Df[idx + sz] : 0.0f;
-            float du, hu, Du = 0.0f;
-            if (!top) {
-                du = sd[p][r + 1][lane];
-                hu = sh[p][r + 1][lane];
-                if (MODEL == LINSTEP) Du = sD[p][r + 1][lane];
-            } else {
-                du = up_ok ? a.din[idx + sy] : dc;
-                hu = up_ok ? a.Hf[idx + sy] : hc;
-                if (MODEL == LINSTEP) Du = up_ok ? a.Df[idx + sy] : Dc;
-            }
-            const float Dd = (MODEL == LINSTEP && r >= 1) ? sD[p][r - 1][lane] : 0.0f;
-            float dr = __shfl_down_sync(FULL, dc, 1);
-            float hr = __shfl_down_sync(FULL, hc, 1);
-            float Dr = MODEL == LINSTEP ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
-            if (lane == 31) {
-                const bool ok = ic + 1 < nx;
-                dr = ok ? a.din[idx + 1] : dc;
-                hr = ok ? a.Hf[idx + 1] : hc;
-                if (MODEL == LINSTEP) Dr = ok ? a.Df[idx + 1] : Dc;
-            }
-            float ux = 0.0f, uy = 0.0f, uz = 0.0f, wxn = 0.0f, wyn = 0.0f, wzn = 0.0f;
-            if (xface) wxn = face32<MODEL, CHECK>(a, dc, dr, hc, hr, Dc, Dr, wx, ux);
-            if (yface) wyn = face32<MODEL, CHECK>(a, dc, du, hc, hu, Dc, Du, wy, uy);
-            if (upd) wzn = face32<MODEL, CHECK>(a, dc, dn, hc, hn, Dc, Dn, wz, uz);
-            if (own_x) a.wout[0][idx] = wxn;
-            if (own_y) a.wout[1][idx] = wyn;
-            if (upd) a.wout[2][idx] = wzn;
-            const float wxl = __shfl_up_sync(FULL, wxn, 1);
-            const float uxl = CHECK ? __shfl_up_sync(FULL, ux, 1) : 0.0f;
-            const float Dl = MODEL == LINSTEP ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
-            sw[p][r][lane] = wyn;
-            if (CHECK) su[p][r][lane] = uy;
-            sd[p ^ 1][r][lane] = dn;
-            sh[p ^ 1][r][lane] = hn;
-            if (MODEL == LINSTEP) sD[p ^ 1][r][lane] = Dn;
-            __syncthreads();
-            if (upd) {
-                const float wyb = sw[p][r - 1][lane];
-                const float e = cell_e32<MODEL>(
-                    a, hc, fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Du)), fmaxf(fmaxf(Dd, Db), Dn)));
-                const float div = fmaf(wzn - wzb, a.sig[2], fmaf(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]));
-                const float dnew = fmaf(-e, fmaf(dc, a.rdt, div - rr), dc);
-                a.dout[idx] = dnew;
-                if (CHECK) {
-                    const float uyb = su[p][r - 1][lane];
-                    const float divu = fmaf(uz - uzb, a.sig[2], fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]));
-                    accumulate_residual((double)fmaf(-dnew, a.rdt, rr + divu), part, pmax);
-                }
-            }
-            dc = dn;
-            hc = hn;
-            wzb = wzn;
-            uzb = uz;
-            if (MODEL == LINSTEP) {
-                Db = Dc;
-                Dc = Dn;
-            }
-            p ^= 1;
-        }
-    }
+    dc3d_body<MODEL, CHECK, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, chunk, part, pmax);
     if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 

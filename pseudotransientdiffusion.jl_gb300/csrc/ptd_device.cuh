@@ -27,7 +27,7 @@
 
 namespace ptd {
 
-enum { LIN = 0, LINSTEP = 1, NONLIN = 2 };
+enum { LIN = 0, LINSTEP = 1, NONLIN = 2, NONLIN_EXPM = 3 };
 
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -112,10 +112,10 @@ __device__ __forceinline__ float fsqrt(float x)
 // NONLIN face: c = 1/(1+theta), theta = L*Resc/(Vpdtau*Re_f),
 // Re_f = pi + sqrt(pi^2 + L^2/(D_f dt)), D_f = ((h_L+h_R)/2)^3
 // (scripts/diff_2D_nonlin.jl:145-151).  D_f -> 0 gives Re_f -> inf, c -> 1.
-__device__ __forceinline__ float nonlin_face_c(const FParams& a, float hsum)
+__device__ __forceinline__ float nonlin_face_c(const FParams& a, float hsum, float efac = 1.0f)
 {
     float m = 0.5f * hsum;
-    float df = m * m * m;
+    float df = efac * m * m * m;
     float re = a.fpi + fsqrt(a.fpi2 + a.fA * frcp(df));
     float th = a.fk2 * frcp(re);
     return frcp(1.0f + th);
@@ -124,12 +124,15 @@ __device__ __forceinline__ float nonlin_face_c(const FParams& a, float hsum)
 // NONLIN cell: e = 1/(1/dtau + 1/dt) with
 // 1/dtau = H^3 Re / (Vpdtau L Resc) = (pi H^3 + sqrt(pi^2 H^6 + L^2 H^3/dt)) * k1
 // (scripts/diff_2D_nonlin.jl:149,152); finite for H^3 -> 0 (e -> dt).
-__device__ __forceinline__ float nonlin_cell_e(const FParams& a, float h)
+__device__ __forceinline__ float nonlin_cell_e(const FParams& a, float h, float efac = 1.0f)
 {
-    float h3 = h * h * h;
+    float h3 = efac * h * h * h;
     float inv = (a.fpi * h3 + fsqrt(a.fpi2 * h3 * h3 + a.fA * h3)) * a.fk1;
     return frcp(inv + a.frdt);
 }
+
+// (NONLIN_EXPM: D = exp(m) H^3 -- efac = exp(m) at the cell, the arithmetic
+// mean of exp(m) at a face.)
 
 // LINSTEP cell: 1/dtau = maxloc(D) * Re / (Vpdtau L) (compute_iter_params!,
 // scripts/diff_2D_linstep.jl:18-21).

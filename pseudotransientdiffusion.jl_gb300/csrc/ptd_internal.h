@@ -38,6 +38,12 @@ LaunchCfg tuned_config(const ptd_params& p);
 int copy_field_in(const ptd_ctx_base& g, double* dst, const double* src, cudaStream_t s);
 int copy_field_out(const ptd_ctx_base& g, double* dst, const double* src, cudaStream_t s);
 
+// The current H of a one-grid context as an FP64 padded field (device to
+// device; converts DF64).  ptd_api.cu.
+int ctx_current_f64(ptd_ctx* c, double* dst);
+// dst += src over n elements.  ptd_pt.cu.
+cudaError_t add_fields(double* dst, const double* src, long long n, cudaStream_t s);
+
 // FP32 + FP64 defect correction (ptd_dc.cu).
 struct DcState;
 int dc_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cudaStream_t s, DcState** out);

@@ -35,6 +35,7 @@ cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, bool df6
                       cudaStream_t s);
 cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, bool df64, cudaStream_t s);
 cudaError_t launch_to_df64(const double* src, void* dst, long long n, cudaStream_t s);
+cudaError_t launch_expm(const double* m, void* E, long long n, bool df64, cudaStream_t s);
 cudaError_t launch_from_df64(const void* src, double* dst, long long n, cudaStream_t s);
 cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
                          double norm_den, int norm_max, cudaStream_t s);

@@ -9,6 +9,9 @@ from . import _abi, scripts
 from ._abi import PtdError, PtdParams
 from .scripts import SCRIPTS, Script, initial_condition, step_field
 from .solvers import Result, Solver, make_params, run_script
+from .batch import BatchSolver, batch_instances, batch_params
+from .adjoint import AdjointSolver, misfit_function
 
 __all__ = ["_abi", "scripts", "PtdError", "PtdParams", "SCRIPTS", "Script", "initial_condition",
-           "step_field", "Result", "Solver", "make_params", "run_script"]
+           "step_field", "Result", "Solver", "make_params", "run_script", "BatchSolver", "batch_instances",
+           "batch_params", "AdjointSolver", "misfit_function"]

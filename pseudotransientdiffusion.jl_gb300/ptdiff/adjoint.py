@@ -1,0 +1,128 @@
+"""Gradients of an L2 misfit through the implicit PT solve (libptd.so
+``ptd_adj_*``), and their torch.autograd binding.
+
+``AdjointSolver(params)`` wraps one ``ptd_adj`` context (3D, D = exp(m) H^3 or
+D = H^3): ``forward(H0, m, Ht)`` runs ``params.nt`` implicit steps keeping one
+checkpoint per step and returns L = 1/2 sum_inner (H^nt - Ht)^2;
+``gradient()`` returns (dL/dm, dL/dH0).  ``DiffusionMisfit`` is the
+torch.autograd.Function over the same calls (the Python counterpart of the
+Julia ChainRulesCore rrule in julia/PTDiffusion.jl).  No reference counterpart.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+
+_bound = False
+
+
+def _lib():
+    global _bound
+    L = _abi.lib()
+    if not _bound:
+        vp, ip, dp = C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_double)
+        L.ptd_adj_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(_abi.PtdParams)]
+        L.ptd_adj_create.restype = C.c_int
+        L.ptd_adj_forward.argtypes = [vp, vp, vp, vp, dp, vp, ip]
+        L.ptd_adj_forward.restype = C.c_int
+        L.ptd_adj_gradient.argtypes = [vp, vp, vp, ip]
+        L.ptd_adj_gradient.restype = C.c_int
+        L.ptd_adj_counters.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.ptd_adj_counters.restype = C.c_int
+        L.ptd_adj_destroy.argtypes = [vp]
+        L.ptd_adj_destroy.restype = None
+        _bound = True
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return C.c_void_p(a.ctypes.data)
+
+
+class AdjointSolver:
+    def __init__(self, params: _abi.PtdParams):
+        self.params = params
+        self.shape = (params.nx, params.ny, params.nz)
+        self._h = C.c_void_p()
+        _abi.check(_lib().ptd_adj_create(C.byref(self._h), C.byref(params)), "ptd_adj_create")
+
+    def close(self):
+        if self._h:
+            _lib().ptd_adj_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _f(self, a):
+        if a is None:
+            return None
+        if hasattr(a, "data_ptr"):
+            return a.contiguous()
+        return np.asfortranarray(a, dtype=np.float64)
+
+    def forward(self, H0, m, Ht, want_HN=False):
+        H0, m, Ht = self._f(H0), self._f(m), self._f(Ht)
+        loss = C.c_double(0.0)
+        HN = np.zeros(self.shape, dtype=np.float64, order="F") if want_HN else None
+        iters = np.zeros(max(self.params.nt, 1), dtype=np.int32)
+        _abi.check(_lib().ptd_adj_forward(self._h, _ptr(H0), _ptr(m), _ptr(Ht), C.byref(loss), _ptr(HN),
+                                          iters.ctypes.data_as(C.POINTER(C.c_int32))), "ptd_adj_forward")
+        self.forward_iters = iters[: self.params.nt].copy()
+        return (loss.value, HN) if want_HN else loss.value
+
+    def gradient(self, want_m=True, want_H0=True):
+        gm = np.zeros(self.shape, dtype=np.float64, order="F") if want_m else None
+        gh = np.zeros(self.shape, dtype=np.float64, order="F") if want_H0 else None
+        iters = np.zeros(max(self.params.nt, 1), dtype=np.int32)
+        _abi.check(_lib().ptd_adj_gradient(self._h, _ptr(gm), _ptr(gh),
+                                           iters.ctypes.data_as(C.POINTER(C.c_int32))), "ptd_adj_gradient")
+        self.adjoint_iters = iters[: self.params.nt].copy()
+        return gm, gh
+
+    def counters(self):
+        l, it = C.c_int64(0), C.c_int64(0)
+        _abi.check(_lib().ptd_adj_counters(self._h, C.byref(l), C.byref(it)), "ptd_adj_counters")
+        return l.value, it.value
+
+
+def misfit_function():
+    """torch.autograd.Function computing L(m, H0) = 1/2 ||H^nt(m, H0) - Ht||^2
+    with the library's forward and adjoint (float64 tensors, x fastest,
+    shape (nz, ny, nx) in torch's C order)."""
+    import torch
+
+    class DiffusionMisfit(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, m, H0, Ht, solver):
+            def host(t):
+                return np.asfortranarray(t.detach().cpu().numpy().transpose(2, 1, 0))
+
+            loss = solver.forward(host(H0), host(m), host(Ht))
+            ctx.solver = solver
+            ctx.dev = m.device
+            return torch.tensor(loss, dtype=torch.float64, device=m.device)
+
+        @staticmethod
+        def backward(ctx, gout):
+            gm, gh = ctx.solver.gradient()
+            t = lambda a: torch.from_numpy(np.ascontiguousarray(a.transpose(2, 1, 0))).to(ctx.dev)
+            return gout * t(gm), gout * t(gh), None, None
+
+    return DiffusionMisfit

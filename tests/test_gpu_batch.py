@@ -1,0 +1,69 @@
+"""Batched solves (ptd_batch_*): every instance must match the one-grid
+oracle run of its own problem -- equal PT iteration counts and relative L2
+error <= 1e-10 for FP64/DF64; the converged-to-tol bound for FP32_DC."""
+import numpy as np
+import pytest
+
+import ptdiff
+from oracle import oracle as O
+from ptdiff import scripts as S
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def oracle_instance(model, H0, D, **kw):
+    base = S.SCRIPTS["diff_2D_linstep" if model == S.LINSTEP else "diff_2D_nonlin"
+                     if model == S.NONLIN else "diff_2D_lin"]
+    s = base.with_(**kw)
+    return O.solve(s, H0, D)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "df64", "fp32_dc"])
+@pytest.mark.parametrize("model", [S.LINSTEP, S.NONLIN])
+def test_batch_matches_oracle(prec, model):
+    sizes, Hs, Ds = ptdiff.batch_instances(7, seed=3, nmin=12, nmax=90)
+    Hs0 = [H.copy(order="F") for H in Hs]
+    if model != S.LINSTEP:
+        Ds = None
+    nt = 2
+    p = ptdiff.batch_params(len(sizes), model=model, precision=prec, nt=nt,
+                            resc=(1 / 1.2 if model == S.NONLIN else 1.0))
+    with ptdiff.BatchSolver(p, sizes, sizes) as b:
+        iters, err = b.solve(Hs, Ds)
+        launches, its = b.counters()
+    assert launches > 0 and its > 0
+    for k in range(len(sizes)):
+        Hr, it_r, _, st = oracle_instance(model, Hs0[k], None if Ds is None else Ds[k], ttot=0.2 * nt,
+                                          resc=p.resc)
+        assert st == 0
+        if prec == "fp32_dc":
+            rms = float(np.sqrt(np.mean(np.square(Hr))))
+            Ht, _, _, _ = oracle_instance(model, Hs0[k], None if Ds is None else Ds[k], ttot=0.2 * nt,
+                                          resc=p.resc, tol=1e-11)
+            assert rel_l2(Hs[k], Ht) <= 2 * 0.2 * 1e-8 / rms
+            assert err[k] <= 1e-8
+        else:
+            assert list(iters[k]) == list(it_r)
+            assert rel_l2(Hs[k], Hr) <= 1e-10
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_dc"])
+def test_batch_autotuner(prec):
+    sizes, Hs, Ds = ptdiff.batch_instances(5, seed=4, nmin=40, nmax=200)
+    Hs0 = [H.copy(order="F") for H in Hs]
+    p = ptdiff.batch_params(len(sizes), model=S.LINSTEP, precision=prec, nt=1)
+    with ptdiff.BatchSolver(p, sizes, sizes) as b:
+        w, c, us = b.tune()
+        assert w in (2, 4, 8) and c in (16, 32, 64, 128) and us > 0
+        iters, err = b.solve(Hs, Ds)
+    for k in range(len(sizes)):
+        Hr, it_r, _, _ = oracle_instance(S.LINSTEP, Hs0[k], Ds[k], ttot=0.2)
+        if prec == "fp64":
+            assert list(iters[k]) == list(it_r)
+            assert rel_l2(Hs[k], Hr) <= 1e-10
+        else:
+            assert err[k] <= 1e-8

@@ -76,19 +76,24 @@ def test_golden_cases(name, prec):
     assert rel_l2(got, ref) <= RTOL_FP64
 
 
+# DF64 holds H with a 48-bit significand: one unit in the last place of H moves
+# the residual by ~2^-48 |H| (1/dt + sum_d 4 sigma_d K), which reaches tol on
+# fine 1D/2D grids (1D nx >= 2048, 2D >= 1024^2); the DF64 cases stay below.
+LIMITS = {"fp64": {1: 2048, 2: 256, 3: 126}, "df64": {1: 1024, 2: 256, 3: 126}}
+
+
 def _count_cases():
-    limits = {1: 2048, 2: 256, 3: 126}
     out = []
-    for key, rows in COUNTS.items():
-        s = S.SCRIPTS[COUNT_SCRIPTS[key]]
-        for row in rows:
-            if row[0] <= limits[s.ndim]:
-                out.append((key, tuple(row)))
+    for prec in PRECS:
+        for key, rows in COUNTS.items():
+            s = S.SCRIPTS[COUNT_SCRIPTS[key]]
+            for row in rows:
+                if row[0] <= LIMITS[prec][s.ndim]:
+                    out.append((key, tuple(row), prec))
     return out
 
 
-@pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("key,row", _count_cases())
+@pytest.mark.parametrize("key,row,prec", _count_cases())
 def test_published_iteration_counts(key, row, prec):
     s = S.SCRIPTS[COUNT_SCRIPTS[key]]
     shape = row[: s.ndim]

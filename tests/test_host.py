@@ -50,6 +50,39 @@ def test_params_layout_matches_c(tmp_path):
         assert getattr(_abi.PtdParams, f).offset == off, f
 
 
+def test_batch_params_layout_matches_c(tmp_path):
+    from ptdiff.batch import PtdBatchParams
+
+    fields = [f for f, _ in PtdBatchParams._fields_]
+    src = tmp_path / "blayout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/ptd.h"',
+             'int main(void){', 'printf("%zu\\n", sizeof(ptd_batch_params));']
+    lines += [f'printf("%zu\\n", offsetof(ptd_batch_params, {f}));' for f in fields]
+    lines += ['return 0;}']
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "blayout"
+    subprocess.run(["gcc", "-std=c11", "-o", str(exe), str(src)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                           check=True).stdout.split()]
+    assert vals[0] == C.sizeof(PtdBatchParams)
+    for f, off in zip(fields, vals[1:]):
+        assert getattr(PtdBatchParams, f).offset == off, f
+
+
+def test_batch_create_rejects_invalid_params():
+    from ptdiff import batch as B
+
+    p = B.batch_params(2, precision="fp64")
+    p.itmax = 95   # not a multiple of nchk
+    h = C.c_void_p()
+    n = (C.c_int32 * 2)(32, 40)
+    assert B._lib().ptd_batch_create(C.byref(h), C.byref(p), n, n) == _abi.PTD_EINVAL
+    assert "multiple of nchk" in _abi.last_error()
+    p = B.batch_params(2, precision="fp64")
+    n2 = (C.c_int32 * 2)(32, 2)
+    assert B._lib().ptd_batch_create(C.byref(h), C.byref(p), n2, n2) == _abi.PTD_EINVAL
+
+
 @pytest.mark.parametrize("ndim,model", [(1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2), (3, 0), (3, 1), (3, 2)])
 def test_params_init_matches_scripts(ndim, model):
     p = _abi.PtdParams()
