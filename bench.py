@@ -219,6 +219,52 @@ def run_reference(args, world, rank, pg):
     return 0
 
 
+def run_batch(args, world, rank, local, pg):
+    """The batched 2D step-diffusion workload: 256 instances, sides log-uniform
+    in [128, 1024] (seeded), FP32 + FP64 defect correction, tol 1e-8; the
+    instances are sharded over the ranks by cell count (no collective on the
+    data path).  Metric: instances solved per second (one physical step)."""
+    import torch
+
+    import ptdiff
+    from ptdiff import dist as PD
+
+    torch.cuda.set_device(local)
+    n = 256
+    sizes, Hs, Ds = ptdiff.batch_instances(n, seed=0)
+    mine = PD.shard_by_cells([int(s) ** 2 for s in sizes], world)[rank]
+    sz = [int(sizes[i]) for i in mine]
+    p = ptdiff.batch_params(len(mine), model=1, precision=args.precision if args.precision != "fp64" else "fp32_dc",
+                            nt=1)
+    b = ptdiff.BatchSolver(p, sz, sz)
+    w, c, us = b.tune()
+    for _ in range(args.warmup):
+        b.solve([Hs[i].copy(order="F") for i in mine], [Ds[i] for i in mine])
+    barrier(pg)
+    l0, i0 = b.counters()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        iters, err = b.solve([Hs[i].copy(order="F") for i in mine], [Ds[i] for i in mine])
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    l1, i1 = b.counters()
+    b.close()
+    t_max = reduce_max(pg, dt)
+    total = reduce_sum(pg, len(mine) * args.steps)
+    if rank == 0:
+        print(json.dumps({"metric": "batch instances per second (one implicit step to tol)",
+                          "value": round(total / t_max, 3), "unit": "instances/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": round(t_max / args.steps * 1e3, 3), "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner + f64 outer",
+                          "data": "synthetic", "config": {"workload": "batch_linstep_256", "instances": n,
+                                                          "sides": "log-uniform 128..1024, seed 0",
+                                                          "tuned": {"warps": w, "chunk": c, "us_per_iter": us}},
+                          "gpu_launches": int(l1 - l0), "inner_iterations": int(i1 - i0),
+                          "max_err_last": float(max(err))}), flush=True)
+    return 0
+
+
 def run_ours(args, world, rank, local, pg):
     import torch
 
@@ -398,6 +444,8 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args, world, rank, pg)
+        if args.workload == "batch_linstep_256":
+            return run_batch(args, world, rank, local, pg)
         return run_ours(args, world, rank, local, pg)
     finally:
         if pg is not None:

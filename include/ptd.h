@@ -84,7 +84,9 @@ enum { PTD_RESID_MIXED = 0, PTD_RESID_CONSISTENT = 1 };
 enum { PTD_NORM_RMS = 0, PTD_NORM_MAX = 1 };
 
 /* Flags */
-#define PTD_FLAG_STRICT 0x1 /* return PTD_ENOTCONV when a step stops at itmax */
+#define PTD_FLAG_STRICT 0x1   /* return PTD_ENOTCONV when a step stops at itmax */
+#define PTD_FLAG_AUTOTUNE 0x2 /* ptd_create times every launch shape of the fused kernel (2D: warps per CTA
+                                 x rows per y march; 3D: z-march length x warps per CTA) and keeps the fastest */
 
 typedef struct ptd_params {
     int32_t ndim;        /* 1, 2, 3 */
@@ -142,6 +144,9 @@ PTD_API int ptd_step(ptd_ctx* ctx, int32_t nsteps, int32_t* iters_per_step, doub
 PTD_API int ptd_iterate(ptd_ctx* ctx, int32_t niter);  /* niter PT iterations, no checks (perf protocol,
                                                   scripts/diff_3D/diff_3D_nonlin_perf.jl:97-105) */
 PTD_API int ptd_get_state(ptd_ctx* ctx, double* H);    /* H out */
+
+/* Launch shape in use: {warps per 2D CTA, rows per 2D y march, warps per 3D CTA, planes per 3D z march}. */
+PTD_API int ptd_launch_config(ptd_ctx* ctx, int32_t cfg[4]);
 
 /* The context's CUDA stream (cudaStream_t) and a device synchronize of it. */
 PTD_API void* ptd_stream(ptd_ctx* ctx);

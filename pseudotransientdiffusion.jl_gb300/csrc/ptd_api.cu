@@ -146,7 +146,7 @@ int ptd::validate(const ptd_params* p)
     if (p->resid_mode != PTD_RESID_MIXED && p->resid_mode != PTD_RESID_CONSISTENT)
         return fail(PTD_EINVAL, "unknown resid_mode %d", p->resid_mode);
     if (p->norm != PTD_NORM_RMS && p->norm != PTD_NORM_MAX) return fail(PTD_EINVAL, "unknown norm %d", p->norm);
-    if (p->flags & ~PTD_FLAG_STRICT) return fail(PTD_EINVAL, "unknown flags 0x%x", p->flags);
+    if (p->flags & ~(PTD_FLAG_STRICT | PTD_FLAG_AUTOTUNE)) return fail(PTD_EINVAL, "unknown flags 0x%x", p->flags);
     for (int k = 0; k < 8; ++k)
         if (p->reserved[k]) return fail(PTD_EINVAL, "reserved fields must be zero");
     return PTD_OK;
@@ -351,6 +351,80 @@ static int capture_plain(ptd_ctx* c, int parity, cudaGraphExec_t* out)
     return PTD_OK;
 }
 
+__global__ void fill_one_kernel(double* a, long long n, int df64)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        if (df64) reinterpret_cast<float2*>(a)[t] = make_float2(1.0f, 0.0f);
+        else a[t] = 1.0;
+    }
+}
+
+// Autotuner: on a synthetic state (H = 1, zero fluxes) time every launch
+// shape of the fused kernel -- 2D: warps per CTA x rows per y march; 3D: z
+// march length x warps per CTA -- and keep the fastest.
+static int autotune(ptd_ctx* c)
+{
+    const bool d3 = c->p.ndim == 3;
+    std::vector<LaunchCfg> cands;
+    if (d3) {
+        for (int rows : {8, 16})
+            for (int ch : {16, 32, 64, 128, 256}) {
+                LaunchCfg k = c->cfg;
+                k.rows3d = rows;
+                k.chunk3d = ch;
+                cands.push_back(k);
+            }
+    } else {
+        for (int w : {2, 4, 8})
+            for (int ch : {16, 32, 64, 128}) {
+                LaunchCfg k = c->cfg;
+                k.warps2d = w;
+                k.chunk2d = ch;
+                cands.push_back(k);
+            }
+    }
+    for (double* f : {c->H[0], c->H[1], c->Hold}) {
+        fill_one_kernel<<<152 * 8, 256, 0, c->stream>>>(f, c->nfield, c->df64 ? 1 : 0);
+        CK(cudaGetLastError());
+    }
+    if (c->D) {
+        fill_one_kernel<<<152 * 8, 256, 0, c->stream>>>(c->D, c->nfield, c->df64 ? 1 : 0);
+        CK(cudaGetLastError());
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    LaunchCfg bestc = c->cfg;
+    for (const LaunchCfg& k : cands) {
+        c->cfg = k;
+        int par = 0;
+        for (int rep = 0; rep < 2; ++rep) {
+            CK(cudaEventRecord(e0, c->stream));
+            for (int it = 0; it < 4; ++it) {
+                PTArgs a;
+                args_for(c, par, c->zero_flag, a);
+                CK(launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream));
+                par ^= 1;
+            }
+            CK(cudaEventRecord(e1, c->stream));
+            CK(cudaEventSynchronize(e1));
+        }
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        c->launches += 8;
+        if (ms < best) {
+            best = ms;
+            bestc = k;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->cfg = bestc;
+    return PTD_OK;
+}
+
 static void free_ctx(ptd_ctx* c)
 {
     if (!c) return;
@@ -441,6 +515,7 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
             return rc;
         }
     } else {
+        if ((p->flags & PTD_FLAG_AUTOTUNE) && p->ndim > 1) rc = autotune(c);
         for (int q = 0; q < 2 && !rc; ++q) {
             if (p->nchk <= p->itmax) rc = capture_block(c, q, &c->gblock[q]);
             if (!rc) rc = capture_plain(c, q, &c->gplain[q]);
@@ -457,6 +532,16 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
 extern "C" void ptd_destroy(ptd_ctx* c) { free_ctx(c); }
 
 extern "C" void* ptd_stream(ptd_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int ptd_launch_config(ptd_ctx* c, int32_t cfg[4])
+{
+    if (!c || !cfg) return fail(PTD_EINVAL, "ptd_launch_config: NULL argument");
+    cfg[0] = c->cfg.warps2d;
+    cfg[1] = c->cfg.chunk2d;
+    cfg[2] = c->cfg.rows3d;
+    cfg[3] = c->cfg.chunk3d;
+    return PTD_OK;
+}
 
 extern "C" int ptd_sync(ptd_ctx* c)
 {

@@ -1031,7 +1031,7 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
     const int Ws[] = {2, 4, 8};
     const int Cs[] = {16, 32, 64, 128};
     float best = 1e30f;
-    LaunchCfg keep = b->cfg, bestc = b->cfg;
+    LaunchCfg bestc = b->cfg;
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
@@ -1071,7 +1071,6 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
         set_done_batch_kernel<<<(b->ninst + 127) / 128, 128, 0, b->s>>>(b->bst, b->ninst, 1);
         BCK(cudaGetLastError());
     }
-    (void)keep;
     b->cfg = bestc;
     int rc = upload_work(b);
     if (!rc) rc = capture(b);

@@ -14,11 +14,29 @@ LaunchCfg tuned_config(const ptd_params& p)
         while (chunk > 16 && (long long)bx * ((p.ny - 2 + chunk - 1) / chunk) < 152 * 8) chunk /= 2;
         c.chunk2d = chunk;
     } else if (p.ndim == 3) {
+        // 512-thread CTAs, 3 resident per SM at <= 40 registers: 456 slots.
+        // Take the longest z march whose CTA count fills the slots in whole
+        // waves to >= 90 % (wave quantization), else the best filling one.
         const int rows = 16;
+        const long long slots = 152 * 3;
         const long long bxy = (long long)((p.nx - 2 + 30) / 31) * ((p.ny - 2 + rows - 2) / (rows - 1));
-        int chunk = 256;
-        while (chunk > 16 && bxy * ((p.nz - 2 + chunk - 1) / chunk) < 152 * 4) chunk /= 2;
-        c.chunk3d = chunk;
+        int best = 16;
+        double best_eff = -1.0;
+        for (int chunk = 512; chunk >= 16; chunk /= 2) {
+            const long long nb = bxy * ((p.nz - 2 + chunk - 1) / chunk);
+            const long long waves = (nb + slots - 1) / slots;
+            const double eff = (double)nb / (double)(waves * slots);
+            if (nb >= slots && eff >= 0.9) {
+                best = chunk;
+                best_eff = 2.0;
+                break;
+            }
+            if (eff > best_eff) {
+                best_eff = eff;
+                best = chunk;
+            }
+        }
+        c.chunk3d = best;
         c.rows3d = rows;
     }
     return c;

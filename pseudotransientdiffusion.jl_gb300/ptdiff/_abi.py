@@ -21,6 +21,7 @@ PREC_FP64, PREC_FP32_DC, PREC_DF64 = 0, 1, 2
 RESID_MIXED, RESID_CONSISTENT = 0, 1
 NORM_RMS, NORM_MAX = 0, 1
 FLAG_STRICT = 0x1
+FLAG_AUTOTUNE = 0x2
 
 
 class PtdParams(C.Structure):
@@ -76,6 +77,7 @@ def lib():
         "ptd_stream": (C.c_void_p, [vp]),
         "ptd_sync": (C.c_int, [vp]),
         "ptd_counters": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+        "ptd_launch_config": (C.c_int, [vp, C.POINTER(C.c_int32)]),
         "ptd_destroy": (None, [vp]),
         "ptd_strerror": (C.c_char_p, [C.c_int]),
         "ptd_last_error": (C.c_char_p, []),

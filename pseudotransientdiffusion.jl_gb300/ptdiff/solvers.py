@@ -26,7 +26,7 @@ PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC, "df64": _abi
 
 def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=None,
                 precision="fp64", resid="mixed", norm="rms", norm_len=0.0, strict=False,
-                dc_max_outer=0, dc_inner_rtol=0.0) -> _abi.PtdParams:
+                autotune=False, dc_max_outer=0, dc_inner_rtol=0.0) -> _abi.PtdParams:
     """ptd_params for a script at a grid shape (x fastest)."""
     p = _abi.PtdParams()
     _abi.check(_abi.lib().ptd_params_init(C.byref(p), script.ndim, script.model), "ptd_params_init")
@@ -46,7 +46,7 @@ def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=No
     p.resid_mode = {"mixed": _abi.RESID_MIXED, "consistent": _abi.RESID_CONSISTENT}[resid]
     p.norm = {"rms": _abi.NORM_RMS, "max": _abi.NORM_MAX}[norm]
     p.norm_len = norm_len
-    p.flags = _abi.FLAG_STRICT if strict else 0
+    p.flags = (_abi.FLAG_STRICT if strict else 0) | (_abi.FLAG_AUTOTUNE if autotune else 0)
     p.dc_max_outer = dc_max_outer
     p.dc_inner_rtol = dc_inner_rtol
     return p
@@ -153,6 +153,11 @@ class Solver:
         l, it = C.c_int64(0), C.c_int64(0)
         _abi.check(_abi.lib().ptd_counters(self._h, C.byref(l), C.byref(it)), "ptd_counters")
         return l.value, it.value
+
+    def launch_config(self):
+        cfg = (C.c_int32 * 4)()
+        _abi.check(_abi.lib().ptd_launch_config(self._h, cfg), "ptd_launch_config")
+        return {"warps2d": cfg[0], "chunk2d": cfg[1], "rows3d": cfg[2], "chunk3d": cfg[3]}
 
 
 @dataclass

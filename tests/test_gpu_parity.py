@@ -201,3 +201,20 @@ def test_iterate_matches_oracle_iterations(prec):
     q = [np.zeros_like(Hr) for _ in range(3)]
     O.iterate(s, Hr, H0.copy(order="F"), q, 77)
     assert rel_l2(H, Hr) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("name,shape", [("diff_2D_nonlin", (130, 97)), ("diff_3D_linstep_multixpu", (40, 36, 50))])
+def test_autotuned_launch_shape_gives_the_same_solution(name, shape, prec):
+    s = S.SCRIPTS[name]
+    D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
+    H0 = S.initial_condition(s, *shape)
+    H = np.array(H0, order="F", copy=True)
+    with ptdiff.Solver(ptdiff.make_params(s, shape, precision=prec, autotune=True)) as sol:
+        cfg = sol.launch_config()
+        iters, _, st = sol.solve(H, D)
+    assert cfg["warps2d"] in (2, 4, 8) and cfg["chunk2d"] in (16, 32, 64, 128)
+    assert cfg["rows3d"] in (8, 16) and cfg["chunk3d"] in (16, 32, 64, 128, 256, 512)
+    Hr, iters_r, _, _ = O.solve(s, H0, D)
+    assert st == 0 and list(iters) == list(iters_r)
+    assert rel_l2(H, Hr) <= RTOL_FP64
