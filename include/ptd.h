@@ -212,6 +212,30 @@ PTD_API int ptd_adj_gradient(ptd_adj* a, double* grad_m, double* grad_H0, int32_
 PTD_API int ptd_adj_counters(ptd_adj* a, int64_t* kernel_launches, int64_t* pt_iterations);
 PTD_API void ptd_adj_destroy(ptd_adj* a);
 
+/* ---------------------------------------------------------------------------
+ * ptd_solve_2d_noalloc: the 2D FP64 solve of ptd_solve for callers that cannot
+ * allocate GPU memory when they need a solve (a host framework whose memory
+ * pool already owns the device, code running while such an allocator holds
+ * its lock, drivers that must not grow their footprint after start-up).  It
+ * has no counterpart in the reference.  It runs the fused FP64 PT kernel on
+ * the caller's device buffers and takes all scratch from one fixed device
+ * array compiled into the library (24 MiB, held on every GPU that loads the
+ * library until the process exits); it calls no cudaMalloc/cudaFree, creates
+ * no stream or graph and launches on `stream` (a cudaStream_t, NULL = legacy
+ * default stream).
+ *   p      2D, PTD_PREC_FP64, models LIN/LINSTEP/NONLIN, mixed residual;
+ *          nx*ny <= PTD_NOALLOC_MAX_CELLS, else PTD_EINVAL.
+ *   H      device memory, nx*ny doubles, x fastest: in H0, out H after p->nt steps.
+ *   D      device memory (LINSTEP) or NULL.
+ *   iters_per_step  host, p->nt entries (nullable).
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Every call uses the same array: calls that overlap on the GPU (from two
+ * streams or two threads) race and must be serialised by the caller. */
+#define PTD_NOALLOC_MAX_CELLS 524288
+PTD_API int ptd_solve_2d_noalloc(const ptd_params* p, double* H, const double* D, void* stream,
+                                 int32_t* iters_per_step);
+
 PTD_API const char* ptd_strerror(int status);
 PTD_API const char* ptd_last_error(void);   /* detail of the last failure on this thread */
 PTD_API int ptd_abi_version(void);
