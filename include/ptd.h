@@ -139,6 +139,11 @@ PTD_API int ptd_solve(ptd_ctx* ctx, double* H, const double* D, int32_t* iters_p
 /* Resident-state interface (the same loop split in pieces; used for timing
  * and by callers that keep H on the device between calls). */
 PTD_API int ptd_set_state(ptd_ctx* ctx, const double* H, const double* D); /* H and Hold <- H, fluxes <- 0 */
+/* H <- H, Hold <- Hold (NULL: H), fluxes <- 0.  With H = 0 and Hold = Heq, one
+ * step of dt = theta_kin is the reference's steady reaction-diffusion solve
+ * (scripts/diff_2D_react.jl:15-72: Heq/theta_kin in place of Hold/dt, Da in
+ * place of Re, one PT loop). */
+PTD_API int ptd_set_state2(ptd_ctx* ctx, const double* H, const double* Hold, const double* D);
 PTD_API int ptd_step(ptd_ctx* ctx, int32_t nsteps, int32_t* iters_per_step, double* err_hist,
              int32_t err_cap, int32_t* n_err);                       /* nsteps physical steps */
 PTD_API int ptd_iterate(ptd_ctx* ctx, int32_t niter);  /* niter PT iterations, no checks (perf protocol,

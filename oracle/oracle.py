@@ -49,6 +49,8 @@ def lib():
         ip = C.POINTER(C.c_int32)
         L.ora_solve.argtypes = [C.POINTER(OraParams), dp, dp, ip, dp, C.c_int32, ip]
         L.ora_solve.restype = C.c_int
+        L.ora_solve2.argtypes = [C.POINTER(OraParams), dp, dp, dp, ip, dp, C.c_int32, ip]
+        L.ora_solve2.restype = C.c_int
         L.ora_iterate.argtypes = [C.POINTER(OraParams), dp, dp, dp, dp, dp, dp, C.c_int32]
         L.ora_iterate.restype = C.c_int
         L.ora_residual_norm.argtypes = [C.POINTER(OraParams), dp, dp, dp, dp]
@@ -78,17 +80,19 @@ def params(script, shape, *, nt=None, itmax=None, nout=None, resid=0, norm=0, nt
 
 
 def solve(script, H0, D=None, *, nt=None, itmax=None, nout=None, resid=0, norm=0, nthreads=0,
-          errcap=100000, norm_len=0.0):
-    """Run the reference algorithm on the CPU.  Returns (H, iters_per_step, errhist, status)."""
+          errcap=100000, norm_len=0.0, Hold0=None):
+    """Run the reference algorithm on the CPU.  Returns (H, iters_per_step, errhist, status).
+    Hold0: the first step's previous state (default H0; the reaction scripts use H0 = 0, Hold0 = Heq)."""
     H = np.array(H0, dtype=np.float64, order="F", copy=True)
+    Ho = None if Hold0 is None else np.array(Hold0, dtype=np.float64, order="F", copy=True)
     p = params(script, H.shape, nt=nt, itmax=itmax, nout=nout, resid=resid, norm=norm,
                nthreads=nthreads, norm_len=norm_len)
     Dv = None if D is None else np.asfortranarray(D, dtype=np.float64)
     iters = np.zeros(max(p.nt, 1), dtype=np.int32)
     eh = np.zeros(errcap, dtype=np.float64)
     ne = C.c_int32(0)
-    st = lib().ora_solve(C.byref(p), _dptr(H), _dptr(Dv),
-                         iters.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(eh), errcap, C.byref(ne))
+    st = lib().ora_solve2(C.byref(p), _dptr(H), _dptr(Ho), _dptr(Dv),
+                          iters.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(eh), errcap, C.byref(ne))
     return H, iters[: p.nt].copy(), eh[: min(ne.value, errcap)].copy(), st
 
 

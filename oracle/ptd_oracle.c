@@ -284,6 +284,12 @@ static void step_dtau(const octx* c, const double* Df, double* dtau_arr)
 int ora_solve(const ora_params* p, double* H, const double* Dfield, int32_t* iters,
               double* errhist, int32_t errcap, int32_t* nerr)
 {
+    return ora_solve2(p, H, NULL, Dfield, iters, errhist, errcap, nerr);
+}
+
+int ora_solve2(const ora_params* p, double* H, const double* Hold0, const double* Dfield, int32_t* iters,
+               double* errhist, int32_t errcap, int32_t* nerr)
+{
     octx c;
     if (setup(&c, p) || !H || !iters || p->nt < 0 || p->nout < 1) return 1;
     if ((p->model == 1 || p->model == 3) && !Dfield) return 1;
@@ -298,7 +304,7 @@ int ora_solve(const ora_params* p, double* H, const double* Dfield, int32_t* ite
     }
     double* q[3] = {buf, buf + N, buf + 2 * N};
     double* q2[3] = {buf + 3 * N, buf + 4 * N, buf + 5 * N};
-    memcpy(Hold, H, sizeof(double) * N);
+    memcpy(Hold, Hold0 ? Hold0 : H, sizeof(double) * N);
     if (p->model == 1) step_dtau(&c, Dfield, dtau_arr);
     if (p->model == 3) {
         for (long i = 0; i < N; ++i) dtau_arr[i] = exp(Dfield[i]);

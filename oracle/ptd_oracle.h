@@ -58,6 +58,12 @@ typedef struct ora_params {
 int ora_solve(const ora_params* p, double* H, const double* Dfield, int32_t* iters,
               double* errhist, int32_t errcap, int32_t* nerr);
 
+/* As ora_solve with the first step's previous state Hold0 given separately
+ * (NULL: H).  The reaction scripts (scripts/diff_{1D,2D}_react.jl) are one
+ * step with dt = theta_kin, H = 0 and Hold0 = Heq. */
+int ora_solve2(const ora_params* p, double* H, const double* Hold0, const double* Dfield, int32_t* iters,
+               double* errhist, int32_t errcap, int32_t* nerr);
+
 /* Run exactly `niter` PT iterations of one physical step (no residual checks),
  * starting from H with damped fluxes q (3 arrays of nx*ny*nz, face between
  * cell c and c+stride stored at c; zero on the first call).  Used as the timed

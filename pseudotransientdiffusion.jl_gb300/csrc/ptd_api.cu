@@ -566,6 +566,11 @@ extern "C" int ptd_counters(ptd_ctx* c, int64_t* launches, int64_t* iters)
 
 extern "C" int ptd_set_state(ptd_ctx* c, const double* H, const double* D)
 {
+    return ptd_set_state2(c, H, nullptr, D);
+}
+
+extern "C" int ptd_set_state2(ptd_ctx* c, const double* H, const double* Hold, const double* D)
+{
     if (!c) return fail(PTD_EINVAL, "ctx is NULL");
     if (!H) return fail(PTD_EINVAL, "H is NULL");
     if (c->p.model == PTD_MODEL_LINSTEP && !D) return fail(PTD_EINVAL, "the step model needs D");
@@ -581,7 +586,19 @@ extern "C" int ptd_set_state(ptd_ctx* c, const double* H, const double* D)
         c->launches += 1;
     }
     CK(cudaMemcpyAsync(c->H[1], c->H[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->Hold, c->H[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if (Hold) {
+        // a separate previous state (e.g. the reaction form: H from 0, Hold = Heq)
+        double* Odst = c->df64 ? c->stage : c->Hold;
+        CK(cudaMemsetAsync(Odst, 0, bytes, c->stream));
+        rc = copy_field_in(*c, Odst, Hold, c->stream);
+        if (rc) return rc;
+        if (c->df64) {
+            CK(launch_to_df64(c->stage, c->Hold, c->nfield, c->stream));
+            c->launches += 1;
+        }
+    } else {
+        CK(cudaMemcpyAsync(c->Hold, c->H[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    }
     for (int d = 0; d < 3; ++d)
         for (int q = 0; q < 2; ++q)
             if (c->W[d][q]) CK(cudaMemsetAsync(c->W[d][q], 0, bytes, c->stream));

@@ -71,6 +71,7 @@ def lib():
         "ptd_create": (C.c_int, [C.POINTER(C.c_void_p), pp]),
         "ptd_solve": (C.c_int, [vp, vp, vp, ip, dp, C.c_int32, ip]),
         "ptd_set_state": (C.c_int, [vp, vp, vp]),
+        "ptd_set_state2": (C.c_int, [vp, vp, vp, vp]),
         "ptd_step": (C.c_int, [vp, C.c_int32, ip, dp, C.c_int32, ip]),
         "ptd_iterate": (C.c_int, [vp, C.c_int32]),
         "ptd_get_state": (C.c_int, [vp, vp]),

@@ -61,6 +61,7 @@ class Script:
     ic: str = "linrange"      # "linrange" (xc = LinRange) or "xg" (ImplicitGlobalGrid x_g)
     shift: float = 0.0        # H0 = shift + exp(-r^2) (the reference uses 0)
     dirichlet: float | None = None  # boundary cells set to this value (None: keep H0 there)
+    react: bool = False       # reaction form: H starts at 0, Hold = Heq = H0, dt = theta_kin
     default_n: int = 512
     extra: dict = field(default_factory=dict)
 
@@ -96,6 +97,10 @@ SCRIPTS = {
                itmax=1000, nout=2000, recip=True, ic="xg", default_n=64),
         Script("diff_3D_nonlin_perf", 3, NONLIN, cfl=_S3, resc=1.0 / 1.2, ttot=0.4,
                itmax=1000, nout=2000, recip=True, ic="linrange", default_n=64),
+        # steady diffusion-reaction (scripts/diff_1D_react.jl:31-57, diff_2D_react.jl:33-60):
+        # theta_kin = 0.1 plays dt, Heq = H0 plays Hold, H starts at 0, one PT loop
+        Script("diff_1D_react", 1, LIN, lx=20.0, cfl=0.99, D=1.0, dt=0.1, ttot=0.1, react=True),
+        Script("diff_2D_react", 2, LIN, cfl=_S2, D=1.0, dt=0.1, ttot=0.1, react=True),
     ]
 }
 

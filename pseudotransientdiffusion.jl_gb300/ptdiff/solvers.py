@@ -103,12 +103,17 @@ class Solver:
             raise ValueError(f"{name}: expected x-fastest (Fortran-ordered) storage")
         return a
 
-    def solve(self, H, D=None, err_cap: int = 100000, raise_on_nan: bool = True):
+    def solve(self, H, D=None, err_cap: int = 100000, raise_on_nan: bool = True, Hold=None):
         """Solve nt steps in place on H (numpy Fortran array or device tensor).
+        Hold: the first step's previous state (default H).
         Returns (iters_per_step, errhist, status)."""
         H = self._check_array(H, "H")
         if D is not None:
             D = self._check_array(D, "D")
+        if Hold is not None:
+            Hold = self._check_array(Hold, "Hold")
+            _abi.check(_abi.lib().ptd_set_state2(self._h, _ptr(H), _ptr(Hold), _ptr(D)), "ptd_set_state2")
+            return self._step_and_get(H, err_cap, raise_on_nan)
         nt = max(self.params.nt, 1)
         iters = np.zeros(nt, dtype=np.int32)
         eh = np.zeros(max(err_cap, 1), dtype=np.float64)
@@ -117,6 +122,18 @@ class Solver:
                                   eh.ctypes.data_as(C.POINTER(C.c_double)), err_cap, C.byref(ne))
         if st not in (_abi.PTD_OK, _abi.PTD_ENAN, _abi.PTD_ENOTCONV) or (st == _abi.PTD_ENAN and raise_on_nan):
             _abi.check(st, "ptd_solve")
+        return iters[: self.params.nt].copy(), eh[: min(ne.value, err_cap)].copy(), st
+
+    def _step_and_get(self, H, err_cap, raise_on_nan):
+        nt = max(self.params.nt, 1)
+        iters = np.zeros(nt, dtype=np.int32)
+        eh = np.zeros(max(err_cap, 1), dtype=np.float64)
+        ne = C.c_int32(0)
+        st = _abi.lib().ptd_step(self._h, self.params.nt, iters.ctypes.data_as(C.POINTER(C.c_int32)),
+                                 eh.ctypes.data_as(C.POINTER(C.c_double)), err_cap, C.byref(ne))
+        if st not in (_abi.PTD_OK, _abi.PTD_ENAN, _abi.PTD_ENOTCONV) or (st == _abi.PTD_ENAN and raise_on_nan):
+            _abi.check(st, "ptd_step")
+        _abi.check(_abi.lib().ptd_get_state(self._h, _ptr(H)), "ptd_get_state")
         return iters[: self.params.nt].copy(), eh[: min(ne.value, err_cap)].copy(), st
 
     def set_state(self, H, D=None):
@@ -198,7 +215,12 @@ def run_script(name: str, nx: int | None = None, ny: int | None = None, nz: int 
     D = step_field(s, *shape) if s.model == LINSTEP else None
     params = make_params(s, shape, precision=precision, **overrides)
     with Solver(params) as sol:
-        iters, eh, st = sol.solve(H, D)
+        if s.react:
+            Heq = H
+            H = np.zeros_like(Heq, order="F")
+            iters, eh, st = sol.solve(H, D, Hold=Heq)
+        else:
+            iters, eh, st = sol.solve(H, D)
     lengths = (s.lx, s.ly, s.lz)
     coords = tuple(cell_centres(lengths[d], shape[d]) for d in range(s.ndim))
     res = Result(coords, H, iters, eh, st)

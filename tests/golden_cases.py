@@ -12,10 +12,12 @@ GOLDEN_CASES = {
     "diff_1D_lin": 64,
     "diff_1D_linstep": 64,
     "diff_1D_nonlin": 64,
+    "diff_1D_react": 64,
     "diff_2D_lin": 64,
     "diff_2D_linstep": 64,
     "diff_2D_nonlin": 64,
     "diff_2D_nonlin_perf": 64,
+    "diff_2D_react": 64,
     "diff_3D_lin_multixpu": 32,
     "diff_3D_linstep_multixpu": 32,
     "diff_3D_nonlin_multixpu": 32,
@@ -30,6 +32,17 @@ COUNT_SCRIPTS = {
     "3D_lin": "diff_3D_lin_multixpu", "3D_linstep": "diff_3D_linstep_multixpu",
     "3D_nonlin": "diff_3D_nonlin_multixpu",
 }
+
+
+def start_fields(s, shape):
+    """(H, Hold) the script starts from: H0 twice, or for the reaction scripts
+    H = 0 and Hold = Heq = H0 (scripts/diff_1D_react.jl:45-47)."""
+    from ptdiff.scripts import initial_condition
+
+    H0 = initial_condition(s, *shape)
+    if s.react:
+        return np.zeros_like(H0, order="F"), H0
+    return H0, None
 
 
 def load_reftests():

@@ -7,7 +7,7 @@ import pytest
 
 import ptdiff
 from golden_cases import (COUNT_SCRIPTS, GOLDEN_CASES, golden_array, load_counts, load_reftests,
-                          multirank_norm_len, reference_isapprox, sample)
+                          multirank_norm_len, reference_isapprox, sample, start_fields)
 from oracle import oracle as O
 from ptdiff import _abi
 from ptdiff import scripts as S
@@ -24,10 +24,12 @@ def rel_l2(a, b):
 
 
 def gpu_solve(s, shape, D=None, H0=None, **kw):
-    H = S.initial_condition(s, *shape) if H0 is None else np.array(H0, order="F", copy=True)
+    H, Hold = start_fields(s, shape)
+    if H0 is not None:
+        H = np.array(H0, order="F", copy=True)
     p = ptdiff.make_params(s, shape, **kw)
     with ptdiff.Solver(p) as sol:
-        iters, eh, st = sol.solve(H, D, raise_on_nan=False)
+        iters, eh, st = sol.solve(H, D, raise_on_nan=False, Hold=Hold)
     return H, iters, eh, st
 
 
@@ -47,9 +49,9 @@ def oracle_kw(kw):
 
 def compare(s, shape, **kw):
     D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
-    H0 = S.initial_condition(s, *shape)
+    H0, Hold0 = start_fields(s, shape)
     H, iters, eh, st = gpu_solve(s, shape, D, **kw)
-    Hr, iters_r, eh_r, st_r = O.solve(s, H0, D, **oracle_kw(kw))
+    Hr, iters_r, eh_r, st_r = O.solve(s, H0, D, Hold0=Hold0, **oracle_kw(kw))
     assert st == 0 and st_r == 0
     assert list(iters) == list(iters_r)
     assert rel_l2(H, Hr) <= RTOL_FP64

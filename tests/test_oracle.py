@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from golden_cases import (COUNT_SCRIPTS, GOLDEN_CASES, golden_array, load_counts, load_reftests,
-                          multirank_norm_len, reference_isapprox, sample)
+                          multirank_norm_len, reference_isapprox, sample, start_fields)
 from oracle import oracle as O
 from ptdiff import scripts as S
 
@@ -23,9 +23,9 @@ def test_oracle_matches_golden(name):
     n = GOLDEN_CASES[name]
     s = S.SCRIPTS[name]
     shape = (n,) * s.ndim
-    H0 = S.initial_condition(s, *shape)
+    H0, Hold0 = start_fields(s, shape)
     D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
-    H, iters, _, st = O.solve(s, H0, D)
+    H, iters, _, st = O.solve(s, H0, D, Hold0=Hold0)
     assert st == 0
     got = sample(H, n, s.ndim)
     ref = golden_array(REF[name])
