@@ -1,7 +1,7 @@
 """Benchmark of the accelerated PT diffusion solver (T_eff, the reference's metric).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload 2d_nonlin_4096]
-                    [--precision fp64|fp32_dc] [--impl ours|reference]
+                    [--precision fp64|dfh|df64|fp32_dc] [--impl ours|reference]
 
 Workload (default): 2D nonlinear diffusion D = H^3 on 4096^2 cells, 10x10
 domain, H0 = 1 + exp(-r^2), H = 1 on the boundary, dt = 0.2, tol = 1e-8,
@@ -23,6 +23,9 @@ scripts/diff_3D/diff_3D_nonlin_perf.jl:114), in GB/s (1e9 bytes).
 * ``roofline``: the fused PT kernel alone (fixed iterations, the reference's
   perf protocol, scripts/diff_3D/diff_3D_nonlin_perf.jl:97-105), A_eff per
   launch over the mean launch time, against the measured HBM copy bandwidth.
+* ``dfh`` / ``df64``: the same K steps with double-float arithmetic on the
+  FP32 pipe (DFH: H kept in FP64; DF64: every value a double-float, 3D only),
+  with their iteration counts and distance to the FP64 solution.
 * ``cpu_baseline`` / ``--impl reference``: the CPU restatement of the
   reference (oracle/, OpenMP on all host cores; the reference's own Julia
   Threads backend cannot run here: no Julia) on a bounded sample of the same
@@ -328,31 +331,39 @@ def run_ours(args, world, rank, local, pg):
     traffic = profile_traffic(args.workload)
     sol.close()
 
-    # ---- the same FP64-accuracy iteration with double-float arithmetic (FP32 pipe)
-    df = None
-    if args.precision == "fp64" and not args.no_df64:
-        pdf = ptdiff.make_params(s, shape, nt=1, precision="df64")
-        sdf = ptdiff.Solver(pdf)
-        t_df, df_iters, _, _ = timed_steps(sdf, args.steps)
-        H_df = sdf.get_state()
-        ext_df = torch.cuda.ExternalStream(sdf.stream)
-        sdf.iterate(8)
-        sdf.sync()
+    # ---- the same FP64-accuracy iteration with double-float arithmetic on the
+    # FP32 pipe: DFH (FP64 H, double-float fluxes) everywhere; DF64 (every value
+    # a double-float) in 3D only -- its 48-bit H cannot reach tol on the fine 2D
+    # grid and would run to itmax
+    def alt_precision(prec):
+        pa = ptdiff.make_params(s, shape, nt=1, precision=prec)
+        sa = ptdiff.Solver(pa)
+        t_a, a_iters, _, _ = timed_steps(sa, args.steps)
+        H_a = sa.get_state()
+        ext_a = torch.cuda.ExternalStream(sa.stream)
+        sa.iterate(8)
+        sa.sync()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(ext_df)
-        sdf.iterate(nfix)
-        f1.record(ext_df)
+        f0.record(ext_a)
+        sa.iterate(nfix)
+        f1.record(ext_a)
         f1.synchronize()
-        t_launch_df = f0.elapsed_time(f1) / 1e3 / nfix
-        sdf.close()
-        t_df = reduce_max(pg, t_df)
-        df = {"value": round(reduce_sum(pg, A * sum(df_iters)) / t_df / 1e9, 2), "unit": "GB/s",
-              "ms_per_step": round(t_df / args.steps * 1e3, 3), "pt_iterations_per_step": df_iters,
-              "same_iterations_as_fp64": df_iters == step_iters,
-              "rel_l2_vs_fp64": float(np.linalg.norm(H_df - H_fp64) / np.linalg.norm(H_fp64)),
-              "kernel_achieved": round(A / t_launch_df / 1e9, 1),
-              "kernel_frac": round(A / t_launch_df / 1e9 / peak, 4),
-              "launch_us": round(t_launch_df * 1e6, 2)}
+        t_launch_a = f0.elapsed_time(f1) / 1e3 / nfix
+        sa.close()
+        t_a = reduce_max(pg, t_a)
+        return {"value": round(reduce_sum(pg, A * sum(a_iters)) / t_a / 1e9, 2), "unit": "GB/s",
+                "ms_per_step": round(t_a / args.steps * 1e3, 3), "pt_iterations_per_step": a_iters,
+                "same_iterations_as_fp64": a_iters == step_iters,
+                "rel_l2_vs_fp64": float(np.linalg.norm(H_a - H_fp64) / np.linalg.norm(H_fp64)),
+                "kernel_achieved": round(A / t_launch_a / 1e9, 1),
+                "kernel_frac": round(A / t_launch_a / 1e9 / peak, 4),
+                "launch_us": round(t_launch_a * 1e6, 2)}
+
+    alts = {}
+    if args.precision == "fp64" and not args.no_df64:
+        alts["dfh"] = alt_precision("dfh")
+        if s.ndim == 3:
+            alts["df64"] = alt_precision("df64")
 
     # ---- time to tol: FP32 iterations + FP64 defect correction, same K steps from H0
     ttt = None
@@ -400,7 +411,8 @@ def run_ours(args, world, rank, local, pg):
         "ms_per_step": round(t_max / max(args.steps, 1) * 1e3, 3),
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": round(value / pub, 3) if pub else None,
-        "dtype": {"fp64": "f64", "df64": "df64 (f32x2)", "fp32_dc": "f32 inner + f64 outer"}[args.precision],
+        "dtype": {"fp64": "f64", "df64": "df64 (f32x2)", "dfh": "f64 state, df64 (f32x2) arithmetic",
+                  "fp32_dc": "f32 inner + f64 outer"}[args.precision],
         "data": "synthetic",
         "config": {"workload": args.workload, "shape": list(shape), "precision": args.precision,
                    "nchk": s.nout, "tol": s.tol, "dt": s.dt, "step": "one physical time step to tol",
@@ -417,7 +429,8 @@ def run_ours(args, world, rank, local, pg):
         "clocks": clk,
         "pt_iterations_per_step": step_iters,
         "time_to_tol": ttt,
-        "df64": df,
+        "dfh": alts.get("dfh"),
+        "df64": alts.get("df64"),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -430,13 +443,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="2d_nonlin_4096")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "fp32_dc"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "dfh", "fp32_dc"])
     ap.add_argument("--n", type=int, default=0, help="override the grid size (testing)")
     ap.add_argument("--fixed-iters", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-dc", action="store_true", help="skip the FP32+DC time-to-tol comparison")
-    ap.add_argument("--no-df64", action="store_true", help="skip the double-float run")
+    ap.add_argument("--no-df64", action="store_true", help="skip the double-float (DFH, DF64) runs")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

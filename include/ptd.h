@@ -71,8 +71,15 @@ enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL
  *  DF64     the FP64 form with every value held as a double-float (two
  *           FP32 numbers, ~48-bit significand, 8 bytes like a double) and
  *           computed on the FP32 pipe; same iterations and iteration counts
- *           as FP64, H within ~1e-13 relative of it. */
-enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2 };
+ *           as FP64, H within ~1e-13 relative of it.  The 48-bit H limits
+ *           the attainable residual on fine 1D/2D grids (1D nx >= 2048,
+ *           2D >= 1024^2 at tol 1e-8).
+ *  DFH      DF64 arithmetic on an FP64 state: H and Hold are doubles (the
+ *           differences of H values and the H update in FP64, 4 FP64
+ *           operations per cell in 2D, 5 in 3D), fluxes and D double-floats.
+ *           Reaches tol wherever FP64 does.  Single grids only (not the
+ *           batch or the adjoint). */
+enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH = 3 };
 
 /* Residual used for the stopping test.  MIXED is the reference's: the
  * undamped flux from the H the fluxes of that iteration were computed on, the

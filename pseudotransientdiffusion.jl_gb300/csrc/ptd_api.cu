@@ -141,7 +141,8 @@ int ptd::validate(const ptd_params* p)
     if (!(p->resc > 0.0) || !std::isfinite(p->resc)) return fail(PTD_EINVAL, "resc must be > 0");
     if (p->model < PTD_MODEL_NONLIN && (!(p->D > 0.0) || !std::isfinite(p->D)))
         return fail(PTD_EINVAL, "D must be > 0");
-    if (p->precision != PTD_PREC_FP64 && p->precision != PTD_PREC_FP32_DC && p->precision != PTD_PREC_DF64)
+    if (p->precision != PTD_PREC_FP64 && p->precision != PTD_PREC_FP32_DC && p->precision != PTD_PREC_DF64 &&
+        p->precision != PTD_PREC_DFH)
         return fail(PTD_EINVAL, "unknown precision %d", p->precision);
     if (p->resid_mode != PTD_RESID_MIXED && p->resid_mode != PTD_RESID_CONSISTENT)
         return fail(PTD_EINVAL, "unknown resid_mode %d", p->resid_mode);
@@ -267,7 +268,9 @@ struct ptd_ctx : ptd_ctx_base {
     long long launches = 0, iterations = 0;
     int kernels_per_block = 0;
     DcState* dc = nullptr;        // FP32 defect-correction resources
-    bool df64 = false;            // fields hold double-floats (PTD_PREC_DF64)
+    bool df64 = false;            // H and Hold hold double-floats (PTD_PREC_DF64)
+    bool ddf = false;             // D and the fluxes hold double-floats (PTD_PREC_DF64, PTD_PREC_DFH)
+    int num = NUM_F64;            // number type of the PT kernels
     double* stage = nullptr;      // DF64: FP64 staging field for the host boundary
 };
 
@@ -301,11 +304,11 @@ static int capture_block(ptd_ctx* c, int parity, cudaGraphExec_t* out)
         args_for(c, par, &c->st->done, a);
         const bool check = it == nchk - 1;
         if (check && c->p.resid_mode == PTD_RESID_CONSISTENT) {
-            err = launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream);
-            if (err == cudaSuccess) err = launch_resid_consistent(a, c->p.ndim, c->p.model, c->df64, c->stream);
+            err = launch_pt(a, c->p.ndim, c->p.model, false, c->num, c->cfg, c->stream);
+            if (err == cudaSuccess) err = launch_resid_consistent(a, c->p.ndim, c->p.model, c->num, c->stream);
             nk += 2;
         } else {
-            err = launch_pt(a, c->p.ndim, c->p.model, check, c->df64, c->cfg, c->stream);
+            err = launch_pt(a, c->p.ndim, c->p.model, check, c->num, c->cfg, c->stream);
             nk += 1;
         }
         par ^= 1;
@@ -336,7 +339,7 @@ static int capture_plain(ptd_ctx* c, int parity, cudaGraphExec_t* out)
     for (int it = 0; it < c->plain_len && err == cudaSuccess; ++it) {
         PTArgs a;
         args_for(c, par, c->zero_flag, a);
-        err = launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream);
+        err = launch_pt(a, c->p.ndim, c->p.model, false, c->num, c->cfg, c->stream);
         par ^= 1;
     }
     cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
@@ -389,7 +392,7 @@ static int autotune(ptd_ctx* c)
         CK(cudaGetLastError());
     }
     if (c->D) {
-        fill_one_kernel<<<152 * 8, 256, 0, c->stream>>>(c->D, c->nfield, c->df64 ? 1 : 0);
+        fill_one_kernel<<<152 * 8, 256, 0, c->stream>>>(c->D, c->nfield, c->ddf ? 1 : 0);
         CK(cudaGetLastError());
     }
     cudaEvent_t e0, e1;
@@ -405,7 +408,7 @@ static int autotune(ptd_ctx* c)
             for (int it = 0; it < 4; ++it) {
                 PTArgs a;
                 args_for(c, par, c->zero_flag, a);
-                CK(launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream));
+                CK(launch_pt(a, c->p.ndim, c->p.model, false, c->num, c->cfg, c->stream));
                 par ^= 1;
             }
             CK(cudaEventRecord(e1, c->stream));
@@ -467,6 +470,8 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
     c->nfield = c->sz * p->nz;
     c->cfg = tuned_config(*p);
     c->df64 = p->precision == PTD_PREC_DF64;
+    c->ddf = c->df64 || p->precision == PTD_PREC_DFH;
+    c->num = c->df64 ? NUM_DF64 : (p->precision == PTD_PREC_DFH ? NUM_DFH : NUM_F64);
     const size_t bytes = (size_t)c->nfield * sizeof(double);
     auto alloc = [&](void** ptr, size_t n) -> int {
         cudaError_t e = cudaMalloc(ptr, n);
@@ -489,7 +494,7 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
         for (int q = 0; q < 2 && !rc; ++q) rc = alloc((void**)&c->W[d][q], bytes);
     if (!rc && (p->model == PTD_MODEL_LINSTEP || p->model == PTD_MODEL_NONLIN_EXPM))
         rc = alloc((void**)&c->D, bytes);
-    if (!rc && (c->df64 || p->model == PTD_MODEL_NONLIN_EXPM)) rc = alloc((void**)&c->stage, bytes);
+    if (!rc && (c->ddf || p->model == PTD_MODEL_NONLIN_EXPM)) rc = alloc((void**)&c->stage, bytes);
     if (!rc) rc = alloc((void**)&c->st, sizeof(DevState));
     if (!rc) rc = alloc((void**)&c->zero_flag, sizeof(int));
     c->errcap = (p->nchk <= p->itmax ? p->itmax / p->nchk : 0) + 2;
@@ -606,15 +611,15 @@ extern "C" int ptd_set_state2(ptd_ctx* c, const double* H, const double* Hold, c
         CK(cudaMemsetAsync(c->stage, 0, bytes, c->stream));
         rc = copy_field_in(*c, c->stage, D, c->stream);
         if (rc) return rc;
-        CK(launch_expm(c->stage, c->D, c->nfield, c->df64, c->stream));
+        CK(launch_expm(c->stage, c->D, c->nfield, c->ddf, c->stream));
         c->launches += 1;
     }
     if (c->p.model == PTD_MODEL_LINSTEP) {
-        double* Ddst = c->df64 ? c->stage : c->D;
+        double* Ddst = c->ddf ? c->stage : c->D;
         CK(cudaMemsetAsync(Ddst, 0, bytes, c->stream));
         rc = copy_field_in(*c, Ddst, D, c->stream);
         if (rc) return rc;
-        if (c->df64) {
+        if (c->ddf) {
             CK(launch_to_df64(c->stage, c->D, c->nfield, c->stream));
             c->launches += 1;
         }
@@ -659,7 +664,7 @@ static int run_plain(ptd_ctx* c, long long n)
     for (; n > 0; --n) {
         PTArgs a;
         args_for(c, c->cur, c->zero_flag, a);
-        CK(launch_pt(a, c->p.ndim, c->p.model, false, c->df64, c->cfg, c->stream));
+        CK(launch_pt(a, c->p.ndim, c->p.model, false, c->num, c->cfg, c->stream));
         c->launches += 1;
         c->iterations += 1;
         c->cur ^= 1;

@@ -31,9 +31,12 @@ struct LaunchCfg {
     int rows3d = 16;    // warps (y rows) per 3D block (8 or 16)
 };
 
-cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, bool df64, const LaunchCfg& cfg,
+// number types of the PT kernels (ptd_num.cuh)
+enum { NUM_F64 = 0, NUM_DF64 = 1, NUM_DFH = 2 };
+
+cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, int num, const LaunchCfg& cfg,
                       cudaStream_t s);
-cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, bool df64, cudaStream_t s);
+cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, int num, cudaStream_t s);
 cudaError_t launch_to_df64(const double* src, void* dst, long long n, cudaStream_t s);
 cudaError_t launch_expm(const double* m, void* E, long long n, bool df64, cudaStream_t s);
 cudaError_t launch_from_df64(const void* src, double* dst, long long n, cudaStream_t s);

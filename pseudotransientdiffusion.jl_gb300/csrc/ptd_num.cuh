@@ -1,9 +1,12 @@
-// ptd_num.cuh -- the two FP64-accuracy number types of the PT kernels.
+// ptd_num.cuh -- the FP64-accuracy number types of the PT kernels.
 //
 // F64   native IEEE double: every operation on the FP64 pipe.
 // DF64  double-float (float2 {hi, lo}, value hi + lo, |lo| <= ulp(hi)/2):
 //       ~48-bit significand carried entirely on the FP32 pipe with
 //       error-free transformations (Knuth two-sum, FMA two-product).
+// DFH   DF64 arithmetic on an FP64 state: H and Hold are IEEE doubles, the
+//       fluxes and D double-floats.  Only the operations that need H's full
+//       53 bits run on the FP64 pipe (below).
 //
 // GB300 executes FP64 at ~1/72 of its FP32 rate (measured: 0.50 T DFMA/s
 // against 36.5 T FFMA/s), so a PT iteration done in native FP64 is bound by
@@ -38,6 +41,19 @@ struct F64 {
     __device__ static __forceinline__ T zero() { return 0.0; }
     __device__ static __forceinline__ T shfl_down(T v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
     __device__ static __forceinline__ T shfl_up(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+    // the H interface (see DFH): H values are plain T here
+    using HV = T;
+    using HS = T;
+    __device__ static __forceinline__ HV ldh(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
+    __device__ static __forceinline__ HS ldo(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
+    __device__ static __forceinline__ void sth(void* p, long long i, HS v) { static_cast<T*>(p)[i] = v; }
+    __device__ static __forceinline__ float hf(HV h) { return d2f_bits(h); }
+    __device__ static __forceinline__ HV shfl_down_h(HV v, int d) { return shfl_down(v, d); }
+    __device__ static __forceinline__ T hdiff(HV r, HV l) { return r - l; }
+    __device__ static __forceinline__ T hsum(HV l, HV r) { return l + r; }
+    __device__ static __forceinline__ T hdo(HV h, HS o) { return h - o; }
+    __device__ static __forceinline__ T hdn(HS h, HS o) { return h - o; }
+    __device__ static __forceinline__ HS hstep(HV h, T rp, float e) { return fma(-f2d_bits(e), rp, h); }
 };
 
 struct DF64 {
@@ -89,6 +105,77 @@ struct DF64 {
     __device__ static __forceinline__ T shfl_up(T v, int d)
     {
         return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+    }
+    using HV = T;
+    using HS = T;
+    __device__ static __forceinline__ HV ldh(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
+    __device__ static __forceinline__ HS ldo(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
+    __device__ static __forceinline__ void sth(void* p, long long i, HS v) { static_cast<T*>(p)[i] = v; }
+    __device__ static __forceinline__ float hf(HV h) { return h.x; }
+    __device__ static __forceinline__ HV shfl_down_h(HV v, int d) { return shfl_down(v, d); }
+    __device__ static __forceinline__ T hdiff(HV r, HV l) { return sub(r, l); }
+    __device__ static __forceinline__ T hsum(HV l, HV r) { return add(l, r); }
+    __device__ static __forceinline__ T hdo(HV h, HS o) { return sub(h, o); }
+    __device__ static __forceinline__ T hdn(HS h, HS o) { return sub(h, o); }
+    __device__ static __forceinline__ HS hstep(HV h, T rp, float e) { return sub(h, mulf(rp, e)); }
+};
+
+// A double as a double-float, with integer operations only (the hardware
+// f64 -> f32 conversion issues on the FP64 pipe): hi = x truncated to 24
+// significant bits, lo = the remainder truncated to 24 bits, so
+// |x - (hi + lo)| < 2^-47 |x| and |lo| < ulp(hi).  For 2^-126 <= |x| < 2^-74
+// the remainder is dropped (absolute error < 2^-97), below 2^-126 the result
+// is 0; Inf stays Inf and NaN NaN (in hi).
+__device__ __forceinline__ float2 split_bits(double x)
+{
+    const unsigned hi32 = (unsigned)__double2hiint(x);
+    const unsigned lo32 = (unsigned)__double2loint(x);
+    const unsigned sign = hi32 & 0x80000000u;
+    const int E = (int)((hi32 >> 20) & 0x7ffu);
+    const int ef = E - 896;   // biased float exponent of x
+    unsigned h = sign | ((unsigned)ef << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+    h = ef <= 0 ? sign : h;
+    const bool nan = E == 0x7ff && ((hi32 & 0xfffffu) | lo32) != 0u;
+    h = ef >= 255 ? (sign | 0x7f800000u | (nan ? 0x400000u : 0u)) : h;
+    // remainder: the low 29 significand bits, worth m29 * 2^(E - 1075)
+    const int es = E - 948;   // biased float exponent of 2^(E - 1075)
+    const float m29 = __uint2float_rz(lo32 & 0x1fffffffu);
+    float l = __fmul_rn(m29, __uint_as_float((unsigned)max(es, 1) << 23));
+    l = (es >= 1 && ef < 255) ? l : 0.0f;
+    return make_float2(__uint_as_float(h), __uint_as_float(__float_as_uint(l) | sign));
+}
+
+struct DFH : DF64 {
+    // H in registers: the double and its double-float split (taken once per load)
+    struct HV {
+        double d;
+        float2 f;
+    };
+    using HS = double;   // H as stored
+    __device__ static __forceinline__ HV ldh(const void* p, long long i)
+    {
+        const double d = static_cast<const double*>(p)[i];
+        return HV{d, split_bits(d)};
+    }
+    __device__ static __forceinline__ HS ldo(const void* p, long long i) { return static_cast<const double*>(p)[i]; }
+    __device__ static __forceinline__ void sth(void* p, long long i, HS v) { static_cast<double*>(p)[i] = v; }
+    __device__ static __forceinline__ float hf(const HV& h) { return h.f.x; }
+    __device__ static __forceinline__ HV shfl_down_h(const HV& v, int d)
+    {
+        return HV{__shfl_down_sync(0xffffffffu, v.d, d), shfl_down(v.f, d)};
+    }
+    // differences of H values, whose absolute accuracy sets the attainable
+    // residual, are taken in FP64 (exact for close values) and then split
+    __device__ static __forceinline__ T hdiff(const HV& r, const HV& l) { return split_bits(r.d - l.d); }
+    __device__ static __forceinline__ T hsum(const HV& l, const HV& r) { return add(l.f, r.f); }
+    __device__ static __forceinline__ T hdo(const HV& h, HS o) { return split_bits(h.d - o); }
+    __device__ static __forceinline__ T hdn(HS h, HS o) { return split_bits(h - o); }
+    // H - e*Rp: the increment needs only FP32 accuracy (it vanishes at the
+    // fixed point, so its rounding does not move the solution); the
+    // accumulation into H is FP64
+    __device__ static __forceinline__ HS hstep(const HV& h, T rp, float e)
+    {
+        return h.d - f2d_bits(__fmul_rn(e, rp.x));
     }
 };
 

@@ -1,6 +1,7 @@
 // ptd_pt.cu -- fused PT-iteration kernels (one launch per iteration), generic
-// over the number type: F64 (native FP64) and DF64 (double-float on the FP32
-// pipe, same 8 bytes per value), see ptd_num.cuh.
+// over the number type: F64 (native FP64), DF64 (double-float on the FP32
+// pipe, same 8 bytes per value) and DFH (DF64 arithmetic on an FP64 H), see
+// ptd_num.cuh.
 //
 // One launch computes, for every face, the damped flux of iteration k+1 from
 // H^k and the flux of iteration k, and for every inner cell H^{k+1} from those
@@ -65,6 +66,7 @@ template <class N, int MODEL>
 __global__ void __launch_bounds__(256) resid_consistent_kernel(PTArgs a, int ndim)
 {
     using T = typename N::T;
+    using HV = typename N::HV;
     if (step_done(a.done)) return;
     const long long ninner_x = a.nx - 2;
     const long long ninner_y = ndim > 1 ? a.ny - 2 : 1;
@@ -80,22 +82,22 @@ __global__ void __launch_bounds__(256) resid_consistent_kernel(PTArgs a, int ndi
         const long long iz = ndim > 2 ? 1 + rest / ninner_y : 0;
         const long long c = iz * a.sz + iy * a.sy + ix;
         const long long stp[3] = {1, a.sy, a.sz};
-        const T H = ld<N>(a.Hout, c);
+        const HV H = N::ldh(a.Hout, c);
         T div = N::zero();
         for (int d = 0; d < ndim; ++d) {
-            const T HR = ld<N>(a.Hout, c + stp[d]), HL = ld<N>(a.Hout, c - stp[d]);
+            const HV HR = N::ldh(a.Hout, c + stp[d]), HL = N::ldh(a.Hout, c - stp[d]);
             T uR, uL;
             if (MODEL == LIN) {
-                uR = N::sub(HR, H);
-                uL = N::sub(H, HL);
+                uR = N::hdiff(HR, H);
+                uL = N::hdiff(H, HL);
             } else if (MODEL == LINSTEP) {
                 const T Dc = ld<N>(a.D, c);
-                uR = N::mul(N::add(Dc, ld<N>(a.D, c + stp[d])), N::sub(HR, H));
-                uL = N::mul(N::add(ld<N>(a.D, c - stp[d]), Dc), N::sub(H, HL));
+                uR = N::mul(N::add(Dc, ld<N>(a.D, c + stp[d])), N::hdiff(HR, H));
+                uL = N::mul(N::add(ld<N>(a.D, c - stp[d]), Dc), N::hdiff(H, HL));
             } else {
-                const T sR = N::add(H, HR), sL = N::add(HL, H);
-                uR = N::mul(N::mul(N::mul(sR, sR), sR), N::sub(HR, H));
-                uL = N::mul(N::mul(N::mul(sL, sL), sL), N::sub(H, HL));
+                const T sR = N::hsum(H, HR), sL = N::hsum(HL, H);
+                uR = N::mul(N::mul(N::mul(sR, sR), sR), N::hdiff(HR, H));
+                uL = N::mul(N::mul(N::mul(sL, sL), sL), N::hdiff(H, HL));
                 if (MODEL == NONLIN_EXPM) {
                     const T Ec = ld<N>(a.D, c);
                     uR = N::mul(uR, N::add(Ec, ld<N>(a.D, c + stp[d])));
@@ -104,7 +106,7 @@ __global__ void __launch_bounds__(256) resid_consistent_kernel(PTArgs a, int ndi
             }
             div = N::mad(N::sub(uR, uL), cst<N>(a, d), div);
         }
-        const T r = N::sub(div, N::mul(N::sub(H, ld<N>(a.Hold, c)), cst<N>(a, 3)));
+        const T r = N::sub(div, N::mul(N::hdo(H, N::ldo(a.Hold, c)), cst<N>(a, 3)));
         accumulate_residual(N::to_d(r), part, pmax);
     }
     block_reduce_residual(a, part, pmax);
@@ -210,26 +212,29 @@ static cudaError_t launch_type(const PTArgs& a, int ndim, int model, bool check,
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, bool df64, const LaunchCfg& cfg,
+cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, int num, const LaunchCfg& cfg,
                       cudaStream_t s)
 {
-    return df64 ? launch_type<DF64>(a, ndim, model, check, cfg, s) : launch_type<F64>(a, ndim, model, check, cfg, s);
+    if (num == NUM_DF64) return launch_type<DF64>(a, ndim, model, check, cfg, s);
+    if (num == NUM_DFH) return launch_type<DFH>(a, ndim, model, check, cfg, s);
+    return launch_type<F64>(a, ndim, model, check, cfg, s);
 }
 
-cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, bool df64, cudaStream_t s)
+template <class N>
+static void resid_consistent_type(const PTArgs& a, int ndim, int model, cudaStream_t s)
 {
     const int bs = 256, nb = 152 * 8;
-    if (df64) {
-        if (model == LIN) resid_consistent_kernel<DF64, LIN><<<nb, bs, 0, s>>>(a, ndim);
-        else if (model == LINSTEP) resid_consistent_kernel<DF64, LINSTEP><<<nb, bs, 0, s>>>(a, ndim);
-        else if (model == NONLIN) resid_consistent_kernel<DF64, NONLIN><<<nb, bs, 0, s>>>(a, ndim);
-        else resid_consistent_kernel<DF64, NONLIN_EXPM><<<nb, bs, 0, s>>>(a, ndim);
-    } else {
-        if (model == LIN) resid_consistent_kernel<F64, LIN><<<nb, bs, 0, s>>>(a, ndim);
-        else if (model == LINSTEP) resid_consistent_kernel<F64, LINSTEP><<<nb, bs, 0, s>>>(a, ndim);
-        else if (model == NONLIN) resid_consistent_kernel<F64, NONLIN><<<nb, bs, 0, s>>>(a, ndim);
-        else resid_consistent_kernel<F64, NONLIN_EXPM><<<nb, bs, 0, s>>>(a, ndim);
-    }
+    if (model == LIN) resid_consistent_kernel<N, LIN><<<nb, bs, 0, s>>>(a, ndim);
+    else if (model == LINSTEP) resid_consistent_kernel<N, LINSTEP><<<nb, bs, 0, s>>>(a, ndim);
+    else if (model == NONLIN) resid_consistent_kernel<N, NONLIN><<<nb, bs, 0, s>>>(a, ndim);
+    else resid_consistent_kernel<N, NONLIN_EXPM><<<nb, bs, 0, s>>>(a, ndim);
+}
+
+cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, int num, cudaStream_t s)
+{
+    if (num == NUM_DF64) resid_consistent_type<DF64>(a, ndim, model, s);
+    else if (num == NUM_DFH) resid_consistent_type<DFH>(a, ndim, model, s);
+    else resid_consistent_type<F64>(a, ndim, model, s);
     return cudaGetLastError();
 }
 

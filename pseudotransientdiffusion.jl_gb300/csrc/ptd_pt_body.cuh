@@ -1,5 +1,5 @@
 // ptd_pt_body.cuh -- bodies of the fused PT-iteration kernels, generic over
-// the number type (F64, DF64) and callable with explicit tile indices, so the
+// the number type (F64, DF64, DFH) and callable with explicit tile indices, so the
 // same code serves one grid (ptd_pt.cu) and a batch of grids (ptd_batch.cu).
 // See ptd_pt.cu for the algorithm and the tiling.
 #pragma once
@@ -27,12 +27,12 @@ __device__ __forceinline__ void st(void* p, long long i, typename N::T v)
 
 // One face: new scaled flux, and u = K_f * g (undamped flux) when U.
 template <class N, int MODEL, bool U>
-__device__ __forceinline__ typename N::T face_t(const PTArgs& a, typename N::T HL, typename N::T HR, float hsum,
-                                                typename N::T DL, typename N::T DR, typename N::T w,
-                                                typename N::T& u)
+__device__ __forceinline__ typename N::T face_t(const PTArgs& a, const typename N::HV& HL,
+                                                const typename N::HV& HR, float hsum, typename N::T DL,
+                                                typename N::T DR, typename N::T w, typename N::T& u)
 {
     using T = typename N::T;
-    const T g = N::sub(HR, HL);
+    const T g = N::hdiff(HR, HL);
     if (MODEL == LIN) {
         if (U) u = g;
         return nmadf(N(), a.fc_lin, N::add(g, w), w);
@@ -43,11 +43,11 @@ __device__ __forceinline__ typename N::T face_t(const PTArgs& a, typename N::T H
         K = N::add(DL, DR);
         c = a.fc_lin;
     } else if (MODEL == NONLIN) {
-        const T s = N::add(HL, HR);
+        const T s = N::hsum(HL, HR);
         K = N::mul(N::mul(s, s), s);
         c = nonlin_face_c(a.f, hsum);
     } else {   // NONLIN_EXPM: D holds exp(m); K = (E_L + E_R) s^3, kappa = 1/16
-        const T s = N::add(HL, HR);
+        const T s = N::hsum(HL, HR);
         const T e2 = N::add(DL, DR);
         K = N::mul(N::mul(N::mul(s, s), s), e2);
         c = nonlin_face_c(a.f, hsum, 0.5f * N::lo_f(e2));
@@ -74,6 +74,11 @@ __device__ __forceinline__ float2 cst<DF64>(const PTArgs& a, int which)
 {
     return which < 3 ? a.sig_df[which] : a.rdt_df;
 }
+template <>
+__device__ __forceinline__ float2 cst<DFH>(const PTArgs& a, int which)
+{
+    return which < 3 ? a.sig_df[which] : a.rdt_df;
+}
 
 template <int MODEL>
 struct ModelTraits {
@@ -91,11 +96,11 @@ __device__ __forceinline__ float cell_e(const PTArgs& a, float h, float dmax)
 
 // H_new = H - e*((H - Hold)/dt + div)
 template <class N>
-__device__ __forceinline__ typename N::T h_update(const PTArgs& a, typename N::T Hc, typename N::T Ho,
-                                                  typename N::T div, float e)
+__device__ __forceinline__ typename N::HS h_update(const PTArgs& a, const typename N::HV& Hc, typename N::HS Ho,
+                                                   typename N::T div, float e)
 {
-    const typename N::T Rp = N::mad(N::sub(Hc, Ho), cst<N>(a, 3), div);
-    return nmadf(N(), e, Rp, Hc);
+    const typename N::T Rp = N::mad(N::hdo(Hc, Ho), cst<N>(a, 3), div);
+    return N::hstep(Hc, Rp, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -104,33 +109,35 @@ template <class N, int MODEL, bool CHECK>
 __device__ __forceinline__ void pt1d_body(const PTArgs& a, int bx, double& part, unsigned long long& pmax)
 {
     using T = typename N::T;
+    using HV = typename N::HV;
+    using HS = typename N::HS;
     const int i = bx * blockDim.x + threadIdx.x;
     const int nx = a.nx;
     if (i < nx) {
-        const T Hc = ld<N>(a.Hin, i);
-        const float hc = N::lo_f(Hc);
+        const HV Hc = N::ldh(a.Hin, i);
+        const float hc = N::hf(Hc);
         constexpr bool HASD = ModelTraits<MODEL>::hasd;
         const T Dc = HASD ? ld<N>(a.D, i) : N::zero();
         T wr = N::zero(), ur = N::zero(), Dr = N::zero();
         if (i <= nx - 2) {
-            const T Hr = ld<N>(a.Hin, i + 1);
+            const HV Hr = N::ldh(a.Hin, i + 1);
             if (HASD) Dr = ld<N>(a.D, i + 1);
-            wr = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + N::lo_f(Hr), Dc, Dr, ld<N>(a.win[0], i), ur);
+            wr = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + N::hf(Hr), Dc, Dr, ld<N>(a.win[0], i), ur);
             st<N>(a.wout[0], i, wr);
         }
         if (i >= 1 && i <= nx - 2) {
-            const T Hl = ld<N>(a.Hin, i - 1);
+            const HV Hl = N::ldh(a.Hin, i - 1);
             const T Dl = HASD ? ld<N>(a.D, i - 1) : N::zero();
             T ul = N::zero();
-            const T wl = face_t<N, MODEL, CHECK>(a, Hl, Hc, N::lo_f(Hl) + hc, Dl, Dc, ld<N>(a.win[0], i - 1), ul);
-            const T Ho = ld<N>(a.Hold, i);
+            const T wl = face_t<N, MODEL, CHECK>(a, Hl, Hc, N::hf(Hl) + hc, Dl, Dc, ld<N>(a.win[0], i - 1), ul);
+            const HS Ho = N::ldo(a.Hold, i);
             const T div = N::mul(N::sub(wr, wl), cst<N>(a, 0));
             const float e = cell_e<MODEL>(a, hc, MODEL == NONLIN_EXPM ? N::lo_f(Dc)
                                                  : fmaxf(fmaxf(N::lo_f(Dl), N::lo_f(Dr)), N::lo_f(Dc)));
-            const T Hn = h_update<N>(a, Hc, Ho, div, e);
-            st<N>(a.Hout, i, Hn);
+            const HS Hn = h_update<N>(a, Hc, Ho, div, e);
+            N::sth(a.Hout, i, Hn);
             if (CHECK) {
-                const T r = N::sub(N::mul(N::sub(ur, ul), cst<N>(a, 0)), N::mul(N::sub(Hn, Ho), cst<N>(a, 3)));
+                const T r = N::sub(N::mul(N::sub(ur, ul), cst<N>(a, 0)), N::mul(N::hdn(Hn, Ho), cst<N>(a, 3)));
                 accumulate_residual(N::to_d(r), part, pmax);
             }
         }
@@ -146,6 +153,8 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
                                           unsigned long long& pmax)
 {
     using T = typename N::T;
+    using HV = typename N::HV;
+    using HS = typename N::HS;
     const int lane = threadIdx.x;
     const int i = 31 * tile + lane;
     const int nx = a.nx, ny = a.ny;
@@ -162,36 +171,36 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
         long long idx = (long long)j0 * sy + ic;
 
         constexpr bool HASD = ModelTraits<MODEL>::hasd;
-        T Hc = ld<N>(a.Hin, idx);
-        float hc = N::lo_f(Hc);
+        HV Hc = N::ldh(a.Hin, idx);
+        float hc = N::hf(Hc);
         T Dc = HASD ? ld<N>(a.D, idx) : N::zero();
         float dcf = MODEL == LINSTEP ? N::lo_f(Dc) : 0.0f;
         float dbf = 0.0f;
         T wyb = N::zero(), uyb = N::zero();
         if (upd) {
             // face (j0 - 1/2), owned by the chunk below unless j0 == 1
-            const T Hb = ld<N>(a.Hin, idx - sy);
+            const HV Hb = N::ldh(a.Hin, idx - sy);
             const T Db = HASD ? ld<N>(a.D, idx - sy) : N::zero();
             dbf = MODEL == LINSTEP ? N::lo_f(Db) : 0.0f;
-            wyb = face_t<N, MODEL, CHECK>(a, Hb, Hc, N::lo_f(Hb) + hc, Db, Dc, ld<N>(a.win[1], idx - sy), uyb);
+            wyb = face_t<N, MODEL, CHECK>(a, Hb, Hc, N::hf(Hb) + hc, Db, Dc, ld<N>(a.win[1], idx - sy), uyb);
             if (j0 == 1) st<N>(a.wout[1], idx - sy, wyb);
         }
         for (int j = j0; j < j1; ++j, idx += sy) {
-            const T Hn = ld<N>(a.Hin, idx + sy);
+            const HV Hn = N::ldh(a.Hin, idx + sy);
             const T wx = ld<N>(a.win[0], idx);
             const T wy = ld<N>(a.win[1], idx);
-            const T Ho = ld<N>(a.Hold, idx);
+            const HS Ho = N::ldo(a.Hold, idx);
             const T Dn = HASD ? ld<N>(a.D, idx + sy) : N::zero();
-            T Hr = N::shfl_down(Hc, 1);
+            HV Hr = N::shfl_down_h(Hc, 1);
             float hr = __shfl_down_sync(FULL, hc, 1);
             T Dr = HASD ? N::shfl_down(Dc, 1) : N::zero();
             if (lane == 31) {
                 const bool ok = ic + 1 < nx;
-                Hr = ok ? ld<N>(a.Hin, idx + 1) : Hc;
-                hr = N::lo_f(Hr);
+                Hr = ok ? N::ldh(a.Hin, idx + 1) : Hc;
+                hr = N::hf(Hr);
                 if (HASD) Dr = ok ? ld<N>(a.D, idx + 1) : Dc;
             }
-            const float hn = N::lo_f(Hn);
+            const float hn = N::hf(Hn);
             T ux = N::zero(), uy = N::zero(), wxn = N::zero(), wyn = N::zero();
             if (xface) wxn = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + hr, Dc, Dr, wx, ux);
             if (upd) wyn = face_t<N, MODEL, CHECK>(a, Hc, Hn, hc + hn, Dc, Dn, wy, uy);
@@ -206,11 +215,11 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
                                                     : (MODEL == NONLIN_EXPM ? N::lo_f(Dc) : 0.0f);
                 const float e = cell_e<MODEL>(a, hc, dmax);
                 const T div = N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0)));
-                const T Hnew = h_update<N>(a, Hc, Ho, div, e);
-                st<N>(a.Hout, idx, Hnew);
+                const HS Hnew = h_update<N>(a, Hc, Ho, div, e);
+                N::sth(a.Hout, idx, Hnew);
                 if (CHECK) {
                     const T divu = N::mad(N::sub(uy, uyb), cst<N>(a, 1), N::mul(N::sub(ux, uxl), cst<N>(a, 0)));
-                    const T r = N::sub(divu, N::mul(N::sub(Hnew, Ho), cst<N>(a, 3)));
+                    const T r = N::sub(divu, N::mul(N::hdn(Hnew, Ho), cst<N>(a, 3)));
                     accumulate_residual(N::to_d(r), part, pmax);
                 }
             }
@@ -237,7 +246,9 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
                                           unsigned long long& pmax)
 {
     using T = typename N::T;
-    __shared__ T sH[2][R][32];
+    using HV = typename N::HV;
+    using HS = typename N::HS;
+    __shared__ HV sH[2][R][32];
     __shared__ T sW[2][R][32];
     __shared__ T sU[CHECK ? 2 : 1][CHECK ? R : 1][32];
     constexpr bool HASD = ModelTraits<MODEL>::hasd;
@@ -264,17 +275,17 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
         const long long sy = a.sy, sz = a.sz;
         long long idx = (long long)k0 * sz + (long long)jc * sy + ic;
 
-        T Hc = ld<N>(a.Hin, idx);
-        float hc = N::lo_f(Hc);
+        HV Hc = N::ldh(a.Hin, idx);
+        float hc = N::hf(Hc);
         T Dc = HASD ? ld<N>(a.D, idx) : N::zero();
         float dcf = MODEL == LINSTEP ? N::lo_f(Dc) : 0.0f;
         float dbf = 0.0f;
         T wzb = N::zero(), uzb = N::zero();
         if (upd) {
-            const T Hb = ld<N>(a.Hin, idx - sz);
+            const HV Hb = N::ldh(a.Hin, idx - sz);
             const T Db = HASD ? ld<N>(a.D, idx - sz) : N::zero();
             dbf = MODEL == LINSTEP ? N::lo_f(Db) : 0.0f;
-            wzb = face_t<N, MODEL, CHECK>(a, Hb, Hc, N::lo_f(Hb) + hc, Db, Dc, ld<N>(a.win[2], idx - sz), uzb);
+            wzb = face_t<N, MODEL, CHECK>(a, Hb, Hc, N::hf(Hb) + hc, Db, Dc, ld<N>(a.win[2], idx - sz), uzb);
             if (k0 == 1) st<N>(a.wout[2], idx - sz, wzb);
         }
         int p = 0;
@@ -283,14 +294,15 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
         if (HASD) sD[0][r][lane] = Dc;
         __syncthreads();
         for (int k = k0; k < k1; ++k, idx += sz) {
-            const T Hn = ld<N>(a.Hin, idx + sz);
+            const HV Hn = N::ldh(a.Hin, idx + sz);
             const T wx = ld<N>(a.win[0], idx);
             const T wy = ld<N>(a.win[1], idx);
             const T wz = ld<N>(a.win[2], idx);
-            const T Ho = ld<N>(a.Hold, idx);
+            const HS Ho = N::ldo(a.Hold, idx);
             const T Dn = HASD ? ld<N>(a.D, idx + sz) : N::zero();
             // neighbours in y (row above: shared memory, top row: global)
-            T Hu, Du = N::zero();
+            HV Hu;
+            T Du = N::zero();
             float hu = 0.0f, duf = 0.0f;
             if (!top) {
                 Hu = sH[p][r + 1][lane];
@@ -298,8 +310,8 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
                 if (MODEL == LINSTEP) duf = sF[p][r + 1][lane];
                 else hu = sF[p][r + 1][lane];
             } else {
-                Hu = up_ok ? ld<N>(a.Hin, idx + sy) : Hc;
-                hu = N::lo_f(Hu);
+                Hu = up_ok ? N::ldh(a.Hin, idx + sy) : Hc;
+                hu = N::hf(Hu);
                 if (HASD) {
                     Du = up_ok ? ld<N>(a.D, idx + sy) : Dc;
                     duf = N::lo_f(Du);
@@ -308,16 +320,16 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
             // the row below's D for maxloc (sF[p] is rewritten only after the barrier)
             const float ddf = (MODEL == LINSTEP && r >= 1) ? sF[p][r - 1][lane] : 0.0f;
             // neighbour in x
-            T Hr = N::shfl_down(Hc, 1);
+            HV Hr = N::shfl_down_h(Hc, 1);
             float hr = __shfl_down_sync(FULL, hc, 1);
             T Dr = HASD ? N::shfl_down(Dc, 1) : N::zero();
             if (lane == 31) {
                 const bool ok = ic + 1 < nx;
-                Hr = ok ? ld<N>(a.Hin, idx + 1) : Hc;
-                hr = N::lo_f(Hr);
+                Hr = ok ? N::ldh(a.Hin, idx + 1) : Hc;
+                hr = N::hf(Hr);
                 if (HASD) Dr = ok ? ld<N>(a.D, idx + 1) : Dc;
             }
-            const float hn = N::lo_f(Hn);
+            const float hn = N::hf(Hn);
             const float dnf = MODEL == LINSTEP ? N::lo_f(Dn) : 0.0f;
             T ux = N::zero(), uy = N::zero(), uz = N::zero(), wxn = N::zero(), wyn = N::zero(), wzn = N::zero();
             if (xface) wxn = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + hr, Dc, Dr, wx, ux);
@@ -344,13 +356,13 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
                 const float e = cell_e<MODEL>(a, hc, dmax);
                 const T div = N::mad(N::sub(wzn, wzb), cst<N>(a, 2),
                                      N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0))));
-                const T Hnew = h_update<N>(a, Hc, Ho, div, e);
-                st<N>(a.Hout, idx, Hnew);
+                const HS Hnew = h_update<N>(a, Hc, Ho, div, e);
+                N::sth(a.Hout, idx, Hnew);
                 if (CHECK) {
                     const T uyb = sU[p][r - 1][lane];
                     const T divu = N::mad(N::sub(uz, uzb), cst<N>(a, 2),
                                           N::mad(N::sub(uy, uyb), cst<N>(a, 1), N::mul(N::sub(ux, uxl), cst<N>(a, 0))));
-                    const T r2 = N::sub(divu, N::mul(N::sub(Hnew, Ho), cst<N>(a, 3)));
+                    const T r2 = N::sub(divu, N::mul(N::hdn(Hnew, Ho), cst<N>(a, 3)));
                     accumulate_residual(N::to_d(r2), part, pmax);
                 }
             }

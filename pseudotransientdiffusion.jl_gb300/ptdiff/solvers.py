@@ -21,7 +21,8 @@ import numpy as np
 from . import _abi
 from .scripts import LINSTEP, SCRIPTS, Script, cell_centres, grid_shape, initial_condition, step_field
 
-PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC, "df64": _abi.PREC_DF64}
+PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC, "df64": _abi.PREC_DF64,
+              "dfh": _abi.PREC_DFH}
 
 
 def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=None,

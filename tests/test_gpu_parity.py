@@ -1,7 +1,8 @@
 """Parity of the CUDA library (through the C ABI) with the CPU oracle and the
-reference's golden data, for both FP64-accuracy forms of the PT iteration:
-native FP64 and double-float (DF64, FP32 pipe).  Bar: PT iteration counts
-equal, relative L2 error of H <= 1e-10."""
+reference's golden data, for the three FP64-accuracy forms of the PT
+iteration: native FP64, double-float (DF64, FP32 pipe) and double-float
+arithmetic on an FP64 H (DFH).  Bar: PT iteration counts equal, relative L2
+error of H <= 1e-10."""
 import numpy as np
 import pytest
 
@@ -63,7 +64,7 @@ def compare(s, shape, **kw):
     return H, iters
 
 
-PRECS = ["fp64", "df64"]
+PRECS = ["fp64", "df64", "dfh"]
 
 
 @pytest.mark.parametrize("prec", PRECS)
@@ -81,7 +82,8 @@ def test_golden_cases(name, prec):
 # DF64 holds H with a 48-bit significand: one unit in the last place of H moves
 # the residual by ~2^-48 |H| (1/dt + sum_d 4 sigma_d K), which reaches tol on
 # fine 1D/2D grids (1D nx >= 2048, 2D >= 1024^2); the DF64 cases stay below.
-LIMITS = {"fp64": {1: 2048, 2: 256, 3: 126}, "df64": {1: 1024, 2: 256, 3: 126}}
+LIMITS = {"fp64": {1: 2048, 2: 256, 3: 126}, "df64": {1: 1024, 2: 256, 3: 126},
+          "dfh": {1: 2048, 2: 256, 3: 126}}
 
 
 def _count_cases():
@@ -220,3 +222,21 @@ def test_autotuned_launch_shape_gives_the_same_solution(name, shape, prec):
     Hr, iters_r, _, _ = O.solve(s, H0, D)
     assert st == 0 and list(iters) == list(iters_r)
     assert rel_l2(H, Hr) <= RTOL_FP64
+
+
+# DFH keeps H in FP64: it reaches tol on the fine grids where DF64's 48-bit H
+# cannot, with FP64's iteration counts (and the published ones within 1 %).
+@pytest.mark.parametrize("key,n", [("1D_nonlin", 4096), ("1D_lin", 16384), ("2D_nonlin", 1024),
+                                   ("2D_linstep", 1024), ("2D_nonlin", 2048), ("3D_nonlin", 254)])
+def test_dfh_matches_fp64_on_fine_grids(key, n):
+    s = S.SCRIPTS[COUNT_SCRIPTS[key]]
+    shape = (n,) * s.ndim
+    D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
+    nl = multirank_norm_len(n) if s.ndim == 3 else 0.0
+    H64, it64, _, st64 = gpu_solve(s, shape, D, norm_len=nl, precision="fp64")
+    Hh, ith, _, sth = gpu_solve(s, shape, D, norm_len=nl, precision="dfh")
+    assert st64 == 0 and sth == 0
+    assert list(ith) == list(it64)
+    assert rel_l2(Hh, H64) <= RTOL_FP64
+    published = {tuple(r[: s.ndim]): r[s.ndim] for r in COUNTS[key]}[shape]
+    assert abs(int(ith.sum()) - published) <= 0.01 * published
