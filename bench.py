@@ -200,6 +200,10 @@ def run_reference(args, world, rank, pg):
 
     if rank != 0:
         return 0
+    if args.workload not in ptdiff.scripts.CONFIGS:
+        print(json.dumps({"impl": "reference", "unavailable": f"the reference has no {args.workload} "
+                          "workload (batched and adjoint solvers are new here)"}), flush=True)
+        return 0
     s = ptdiff.scripts.CONFIGS[args.workload]
     shape = (s.default_n,) * s.ndim
     cb = None
@@ -265,6 +269,113 @@ def run_batch(args, world, rank, local, pg):
                                                           "tuned": {"warps": w, "chunk": c, "us_per_iter": us}},
                           "gpu_launches": int(l1 - l0), "inner_iterations": int(i1 - i0),
                           "max_err_last": float(max(err))}), flush=True)
+    return 0
+
+
+def run_adjoint(args, world, rank, local, pg):
+    """The adjoint workload: 3D D = exp(m) H^3 on 256^3, m a smooth Gaussian
+    random field (correlation length 1, std 0.3, seeded), 10 implicit steps of
+    dt = 0.1, L2 misfit of H^10 against a target from a perturbed m; one bench
+    step = one gradient evaluation (forward with one checkpoint per physical
+    step + adjoint), dL/dm and dL/dH0.  The gradient is checked against
+    central finite differences (Richardson-combined) in random directions.
+    Replicas only for N > 1."""
+    import torch
+
+    import ptdiff
+    from ptdiff import scripts as S
+
+    torch.cuda.set_device(local)
+    n = args.n or 256
+    shape = (n,) * 3
+    s = S.SCRIPTS["diff_3D_nonlin_multixpu"].with_(
+        name="adjoint_3d_256", model=S.NONLIN_EXPM, shift=1.0, dirichlet=1.0, ttot=1.0, dt=0.1,
+        tol=args.adj_tol, itmax=200000, ic="linrange")
+    H0 = S.initial_condition(s, *shape)
+    m = S.log_coefficient_field(shape, seed=0)
+    mt = m + S.log_coefficient_field(shape, seed=1)   # the perturbed coefficient of the target
+    dev = lambda a: torch.from_numpy(np.ravel(a, order="F").copy()).cuda()
+    out = {}
+    Ht = None
+    for prec in ("df64", "fp64"):
+        A = ptdiff.AdjointSolver(ptdiff.make_params(s, shape, precision=prec, nchk=10))
+        if Ht is None:
+            _, Ht = A.forward(H0, mt, H0, want_HN=True)
+        H0d, md, Htd = dev(H0), dev(m), dev(Ht)
+        gmd, ghd = torch.empty_like(H0d), torch.empty_like(H0d)
+        for _ in range(args.warmup if prec == "df64" else 1):
+            A.forward(H0d, md, Htd)
+            A.gradient(out_m=gmd, out_H0=ghd)
+        torch.cuda.synchronize()
+        barrier(pg)
+        l0, i0 = A.counters()
+        t_fwd = t_adj = 0.0
+        nsteps = args.steps if prec == "df64" else 1
+        fwd_iters = adj_iters = 0
+        for _ in range(nsteps):
+            t0 = time.perf_counter()
+            loss = A.forward(H0d, md, Htd)
+            t1 = time.perf_counter()
+            A.gradient(out_m=gmd, out_H0=ghd)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            t_fwd += t1 - t0
+            t_adj += t2 - t1
+            fwd_iters += int(A.forward_iters.sum())
+            adj_iters += int(A.adjoint_iters.sum())
+        l1, i1 = A.counters()
+        t_tot = reduce_max(pg, t_fwd + t_adj)
+        rec = {"grads_per_s": round(world * nsteps / t_tot, 4), "ms_per_gradient": round(t_tot / nsteps * 1e3, 2),
+               "forward_ms": round(t_fwd / nsteps * 1e3, 2), "adjoint_ms": round(t_adj / nsteps * 1e3, 2),
+               "adjoint_over_forward": round(t_adj / t_fwd, 3),
+               "forward_pt_iterations": fwd_iters // nsteps, "adjoint_pt_iterations": adj_iters // nsteps,
+               "gpu_launches": int(l1 - l0), "loss": loss}
+        if prec == "df64":
+            # e2e: host arrays in and out, the library copies them
+            gm_h, gh_h = None, None
+            t0 = time.perf_counter()
+            for _ in range(nsteps):
+                A.forward(H0, m, Ht)
+                gm_h, gh_h = A.gradient()
+            rec["e2e_grads_per_s"] = round(world * nsteps / reduce_max(pg, time.perf_counter() - t0), 4)
+            # central differences (eps, eps/2, Richardson) in random joint directions (m, H0)
+            rng = np.random.default_rng(7)
+            worst = 0.0
+            rels = []
+            for _ in range(args.fd_directions if rank == 0 else 0):
+                vm = rng.standard_normal(shape)
+                vh = rng.standard_normal(shape)
+                gv = float(np.sum(gm_h * vm) + np.sum(gh_h * vh))
+                f = lambda e: A.forward(H0 + e * vh, m + e * vm, Ht)
+                eps = args.fd_eps
+                d1 = (f(eps) - f(-eps)) / (2 * eps)
+                d2 = (f(eps / 2) - f(-eps / 2)) / eps
+                fd = (4 * d2 - d1) / 3
+                rel = abs(fd - gv) / max(abs(gv), 1e-300)
+                rels.append(rel)
+                worst = max(worst, rel)
+            rec["fd_check"] = {"directions": len(rels), "eps": args.fd_eps, "max_rel_err": worst,
+                               "median_rel_err": float(np.median(rels)) if rels else None}
+        out[prec] = rec
+        A.close()
+    if rank != 0:
+        return 0
+    d = out["df64"]
+    print(json.dumps({
+        "metric": "adjoint gradient evaluations per second", "value": d["grads_per_s"], "unit": "gradients/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["ms_per_gradient"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "df64 (f32x2)", "data": "synthetic",
+        "config": {"workload": "adjoint_3d_256", "shape": list(shape), "nt": 10, "dt": 0.1, "tol": s.tol,
+                   "model": "D = exp(m) H^3", "m": "Gaussian random field, corr 1, std 0.3, seed 0",
+                   "target": "H^10 of m + a second such field (seed 1)", "checkpoints": "one per step",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": d["e2e_grads_per_s"], "unit": "gradients/s",
+                "h2d_bytes_per_step": int(3 * H0.size * 8), "d2h_bytes_per_step": int(2 * H0.size * 8)},
+        "gpu_launches": d["gpu_launches"],
+        "adjoint_over_forward": d["adjoint_over_forward"],
+        "fd_check": d["fd_check"],
+        "df64": d, "fp64": out["fp64"]}), flush=True)
     return 0
 
 
@@ -450,6 +561,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-dc", action="store_true", help="skip the FP32+DC time-to-tol comparison")
     ap.add_argument("--no-df64", action="store_true", help="skip the double-float (DFH, DF64) runs")
+    ap.add_argument("--adj-tol", type=float, default=1e-10, help="adjoint workload: PT tolerance of the solves")
+    ap.add_argument("--fd-directions", type=int, default=20, help="adjoint workload: finite-difference checks")
+    ap.add_argument("--fd-eps", type=float, default=1e-3, help="adjoint workload: finite-difference step")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -459,6 +573,8 @@ def main():
             return run_reference(args, world, rank, pg)
         if args.workload == "batch_linstep_256":
             return run_batch(args, world, rank, local, pg)
+        if args.workload == "adjoint_3d_256":
+            return run_adjoint(args, world, rank, local, pg)
         return run_ours(args, world, rank, local, pg)
     finally:
         if pg is not None:

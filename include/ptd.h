@@ -75,10 +75,13 @@ enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL
  *           the attainable residual on fine 1D/2D grids (1D nx >= 2048,
  *           2D >= 1024^2 at tol 1e-8).
  *  DFH      DF64 arithmetic on an FP64 state: H and Hold are doubles (the
- *           differences of H values and the H update in FP64, 4 FP64
- *           operations per cell in 2D, 5 in 3D), fluxes and D double-floats.
- *           Reaches tol wherever FP64 does.  Single grids only (not the
- *           batch or the adjoint). */
+ *           differences of H values and the H update in FP64: 5 FP64
+ *           operations per cell in 2D, 6 in 3D), fluxes and D double-floats.
+ *           Same iteration counts as FP64 and H within ~1e-14 of it on the
+ *           2D/3D grids of the reference and of the benchmarks (up to 8192^2
+ *           and 512^3).  The 48-bit flux arithmetic sets a residual floor
+ *           ~32x FP64's, which stalls 1D lin/linstep grids of nx >= 8192.
+ *           Single grids only (not the batch or the adjoint). */
 enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH = 3 };
 
 /* Residual used for the stopping test.  MIXED is the reference's: the

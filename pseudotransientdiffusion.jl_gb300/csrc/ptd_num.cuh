@@ -164,18 +164,22 @@ struct DFH : DF64 {
     {
         return HV{__shfl_down_sync(0xffffffffu, v.d, d), shfl_down(v.f, d)};
     }
-    // differences of H values, whose absolute accuracy sets the attainable
-    // residual, are taken in FP64 (exact for close values) and then split
+    // Differences of H values are taken in FP64 -- exact for close values --
+    // and then split: an error of 2^-48 |H| in a face gradient is multiplied
+    // by K*sigma in the residual and stalls it above tol on fine grids (the
+    // DF64 form's limit).
     __device__ static __forceinline__ T hdiff(const HV& r, const HV& l) { return split_bits(r.d - l.d); }
     __device__ static __forceinline__ T hsum(const HV& l, const HV& r) { return add(l.f, r.f); }
     __device__ static __forceinline__ T hdo(const HV& h, HS o) { return split_bits(h.d - o); }
     __device__ static __forceinline__ T hdn(HS h, HS o) { return split_bits(h - o); }
-    // H - e*Rp: the increment needs only FP32 accuracy (it vanishes at the
-    // fixed point, so its rounding does not move the solution); the
-    // accumulation into H is FP64
+    // H - e*Rp in FP64 with Rp's full double-float accuracy: e*hi and e*lo
+    // are exact in FP64 (24 x 24 bits), so two FMAs give the increment to
+    // ~2^-48.  (With the increment rounded to FP32 the 2D 8192^2 grid takes
+    // a different PT iteration count than FP64.)
     __device__ static __forceinline__ HS hstep(const HV& h, T rp, float e)
     {
-        return h.d - f2d_bits(__fmul_rn(e, rp.x));
+        const double ed = f2d_bits(e);
+        return fma(-ed, f2d_bits(rp.y), fma(-ed, f2d_bits(rp.x), h.d));
     }
 };
 

@@ -87,9 +87,13 @@ class AdjointSolver:
         self.forward_iters = iters[: self.params.nt].copy()
         return (loss.value, HN) if want_HN else loss.value
 
-    def gradient(self, want_m=True, want_H0=True):
-        gm = np.zeros(self.shape, dtype=np.float64, order="F") if want_m else None
-        gh = np.zeros(self.shape, dtype=np.float64, order="F") if want_H0 else None
+    def gradient(self, want_m=True, want_H0=True, out_m=None, out_H0=None):
+        """(dL/dm, dL/dH0) of the last forward().  out_m / out_H0: caller-owned
+        outputs (numpy Fortran arrays or contiguous device tensors of nx*ny*nz
+        float64), else new numpy arrays."""
+        gm = out_m if out_m is not None else (np.zeros(self.shape, dtype=np.float64, order="F") if want_m else None)
+        gh = out_H0 if out_H0 is not None else (np.zeros(self.shape, dtype=np.float64, order="F") if want_H0
+                                                 else None)
         iters = np.zeros(max(self.params.nt, 1), dtype=np.int32)
         _abi.check(_lib().ptd_adj_gradient(self._h, _ptr(gm), _ptr(gh),
                                            iters.ctypes.data_as(C.POINTER(C.c_int32))), "ptd_adj_gradient")

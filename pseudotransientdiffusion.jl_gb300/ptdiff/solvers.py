@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -203,28 +204,82 @@ def _env_int(name, default):
     return int(v) if v else default
 
 
+def _env_flag(name):
+    return os.environ.get(name, "false").strip().lower() in ("1", "true", "yes")
+
+
+def output_stem(s: Script) -> str:
+    """Name the driver gives its output files: the 3D multi-rank solvers write
+    out_diff_3D_<model>.txt / diff_3D_<model>.mat
+    (scripts/diff_3D/diff_3D_nonlin_multixpu.jl:131,137), every other script
+    its own name."""
+    return s.name[: -len("_multixpu")] if s.name.endswith("_multixpu") else s.name
+
+
 def run_script(name: str, nx: int | None = None, ny: int | None = None, nz: int | None = None, *,
-               script: Script | None = None, precision="fp64", verbose=False, **overrides) -> Result:
+               script: Script | None = None, precision="fp64", verbose=False, save=None, save_viz=None,
+               output_dir="output", viz_dir="out_visu", **overrides) -> Result:
     """Run the named reference driver on the GPU.  Grid sizes default to the
-    script's NX/NY/NZ environment variables (then to its built-in default)."""
+    script's NX/NY/NZ environment variables (then to its built-in default);
+    ``save`` / ``save_viz`` default to DO_SAVE / DO_SAVE_VIZ, like the scripts
+    (scripts/diff_2D_nonlin.jl:8-10,95-104): an iteration-count row appended
+    to ``<output_dir>/out_<stem>.txt`` and a ``<viz_dir>/<stem>.mat`` snapshot.
+    The *_perf scripts time the physical steps after the first, as the
+    reference does (scripts/diff_2D_nonlin_perf.jl:91,105-110), and write
+    their timing row instead."""
+    from . import output as out
+
     s = script if script is not None else SCRIPTS[name]
     nx = nx if nx is not None else _env_int("NX", s.default_n)
     ny = ny if ny is not None else _env_int("NY", nx)
     nz = nz if nz is not None else _env_int("NZ", nx)
+    save = _env_flag("DO_SAVE") if save is None else save
+    save_viz = _env_flag("DO_SAVE_VIZ") if save_viz is None else save_viz
     shape = grid_shape(s, nx, ny, nz)
     H = initial_condition(s, *shape)
     D = step_field(s, *shape) if s.model == LINSTEP else None
     params = make_params(s, shape, precision=precision, **overrides)
+    perf = s.name.endswith("_perf")
+    extra = {}
     with Solver(params) as sol:
         if s.react:
             Heq = H
             H = np.zeros_like(Heq, order="F")
             iters, eh, st = sol.solve(H, D, Hold=Heq)
+        elif perf and params.nt > 1:
+            sol.set_state(H, D)
+            i0, e0 = sol.step(1)
+            sol.sync()
+            t0 = time.perf_counter()
+            i1, e1 = sol.step(params.nt - 1)
+            sol.sync()
+            t_toc = time.perf_counter() - t0
+            H = sol.get_state().reshape(shape, order="F")
+            iters, eh, st = np.concatenate([i0, i1]), np.concatenate([e0, e1]), 0
+            niter = int(np.sum(i1))
+            a_eff = (2 * (s.ndim + 1) + 2) * int(np.prod(shape)) * 8 / 1e9
+            t_it = t_toc / max(niter, 1)
+            extra = {"t_toc": t_toc, "A_eff": a_eff, "t_it": t_it, "T_eff": a_eff / t_it, "niter": niter}
         else:
             iters, eh, st = sol.solve(H, D)
     lengths = (s.lx, s.ly, s.lz)
     coords = tuple(cell_centres(lengths[d], shape[d]) for d in range(s.ndim))
-    res = Result(coords, H, iters, eh, st)
-    if verbose:
-        print(f"Total time = {s.ttot:.2f}, time steps = {len(iters)}, nx = {nx}, iterations tot = {res.ittot}")
+    res = Result(coords, H, iters, eh, st, extra)
+    if verbose and s.react:   # scripts/diff_1D_react.jl:70, diff_2D_react.jl:74
+        dims = ", ".join(f"{c} = {n}" for c, n in zip(("nx", "ny"), shape))
+        print(f"{dims}, iterations tot = {res.ittot} ")
+    elif verbose:
+        if extra:
+            teff3 = float("%.3g" % extra["T_eff"])   # round(T_eff, sigdigits=3)
+            print(f"PERF: Time = {extra['t_toc']:1.3f} sec, T_eff = {teff3:1.2f} GB/s (niter = {extra['niter']})")
+        print(f"Total time = {s.ttot:1.2f}, time steps = {len(iters)}, nx = {nx}, iterations tot = {res.ittot} ")
+    stem = output_stem(s)
+    if save and not s.react:   # the reaction scripts write no files
+        if extra:
+            row = out.perf_row(shape, res.ittot, extra["t_toc"], extra["A_eff"], extra["t_it"], extra["T_eff"])
+        else:
+            row = out.counts_row(shape, res.ittot, len(iters))
+        out.append_row(os.path.join(output_dir, f"out_{stem}.txt"), row)
+    if save_viz and not s.react:
+        out.write_mat(os.path.join(viz_dir, f"{stem}.mat"), H, lengths)
     return res

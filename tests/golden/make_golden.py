@@ -5,7 +5,7 @@ default path below, or pass it as the first argument):
 
     python tests/golden/make_golden.py [REFERENCE_ROOT]
 
-It writes two small JSON files next to this script:
+It writes three small JSON files next to this script:
 
 * ``reftests.json`` -- the 14 golden arrays of the reference's own test suite
   (``test/reftest-files/*.bson``, produced by ``test/test_1D.jl:21-46``,
@@ -16,6 +16,9 @@ It writes two small JSON files next to this script:
 * ``iteration_counts.json`` -- the published total PT iteration counts of the
   convergence studies, ``output/out_diff_{1D,2D,3D}_{lin,linstep,nonlin}.txt``
   (rows ``nx [ny [nz]] ittot nt``).
+* ``output_rows.json`` -- the first three rows of every ``output/out_*.txt``
+  file verbatim (count rows and the perf scripts' timing rows), for the
+  byte-exact round trip of the output writer.
 
 The BSON files are read with the small decoder below (BSON 1.0 documents as
 written by Julia's BSON.jl: an array is ``{tag:"array", type, size, data}``
@@ -127,7 +130,17 @@ def main(root):
         fh.write("{\n")
         fh.write(",\n".join(f"{json.dumps(k)}: {json.dumps(v)}" for k, v in counts.items()))
         fh.write("\n}\n")
-    print(f"wrote {len(golden)} golden arrays and {len(counts)} iteration-count tables")
+    # the first rows of every output file, verbatim (format round trips)
+    rows = {}
+    for name in sorted(os.listdir(out_dir)):
+        if name.startswith("out_") and name.endswith(".txt"):
+            with open(os.path.join(out_dir, name)) as fh:
+                rows[name] = [ln.rstrip("\n") for ln in fh if ln.strip()][:3]
+    with open(os.path.join(HERE, "output_rows.json"), "w") as fh:
+        json.dump(rows, fh, indent=1)
+        fh.write("\n")
+    print(f"wrote {len(golden)} golden arrays, {len(counts)} iteration-count tables, "
+          f"{len(rows)} output-row samples")
 
 
 if __name__ == "__main__":

@@ -81,6 +81,9 @@ def test_batch_create_rejects_invalid_params():
     p = B.batch_params(2, precision="fp64")
     n2 = (C.c_int32 * 2)(32, 2)
     assert B._lib().ptd_batch_create(C.byref(h), C.byref(p), n2, n2) == _abi.PTD_EINVAL
+    p = B.batch_params(2, precision="fp64")
+    p.precision = _abi.PREC_DFH   # single grids only
+    assert B._lib().ptd_batch_create(C.byref(h), C.byref(p), n, n) == _abi.PTD_EINVAL
 
 
 @pytest.mark.parametrize("ndim,model", [(1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2), (3, 0), (3, 1), (3, 2)])
@@ -165,3 +168,14 @@ def test_benchmark_initial_condition():
     assert np.isclose(H[15, 15], 1.0 + np.exp(-2 * (10 / 64) ** 2))
     assert s.nout == 100 and s.nt == 5
     assert S.CONFIGS["3d_nonlin_512"].nt == 3
+
+
+def test_adjoint_create_rejects_unsupported_precisions():
+    from ptdiff import adjoint as A
+    from ptdiff.solvers import make_params
+
+    for prec in ("dfh", "fp32_dc"):
+        p = make_params(S.SCRIPTS["diff_3D_nonlin_multixpu"], (16, 16, 16), precision=prec)
+        h = C.c_void_p()
+        assert A._lib().ptd_adj_create(C.byref(h), C.byref(p)) == _abi.PTD_EINVAL
+        assert "FP64 or DF64" in _abi.last_error()
