@@ -18,7 +18,7 @@
 // what convergence to tol = 1e-8 needs; the FP32 inner iterations move half
 // the bytes of the FP64 ones and run on the FP32 pipe.
 //
-// The inner iterations use the fused-kernel layout of ptd_fp64.cu (31-cell x
+// The inner iterations use the fused-kernel layout of ptd_pt.cu (31-cell x
 // tiles per warp, y march in 2D, z march with shared-memory y exchange in 3D)
 // and the same device-side check/judge/done protocol, so a CUDA graph of
 // nchk inner iterations is replayed without a host round trip per check.

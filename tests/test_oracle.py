@@ -2,7 +2,7 @@
 
 Pins the restatement in oracle/ptd_oracle.c before it is trusted as the
 checker of the CUDA library:
-* the 12 golden arrays of the reference test suite (test/reftest-files/*.bson),
+* the 14 golden arrays of the reference test suite (test/reftest-files/*.bson),
   compared far tighter than the reference's own isapprox (rtol 1.5e-8);
 * the published iteration counts of the convergence studies (output/*.txt).
 """
