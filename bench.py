@@ -34,6 +34,7 @@ scripts/diff_3D/diff_3D_nonlin_perf.jl:114), in GB/s (1e9 bytes).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -245,6 +246,7 @@ def run_batch(args, world, rank, local, pg):
                             nt=1)
     b = ptdiff.BatchSolver(p, sz, sz)
     w, c, us = b.tune()
+    depth = b.config()[2]
     for _ in range(args.warmup):
         b.solve([Hs[i].copy(order="F") for i in mine], [Ds[i] for i in mine])
     barrier(pg)
@@ -266,7 +268,8 @@ def run_batch(args, world, rank, local, pg):
                           "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner + f64 outer",
                           "data": "synthetic", "config": {"workload": "batch_linstep_256", "instances": n,
                                                           "sides": "log-uniform 128..1024, seed 0",
-                                                          "tuned": {"warps": w, "chunk": c, "us_per_iter": us}},
+                                                          "tuned": {"warps": w, "chunk": c, "inner_iterations_per_launch": depth,
+                                                                    "us_per_iter": us}},
                           "gpu_launches": int(l1 - l0), "inner_iterations": int(i1 - i0),
                           "max_err_last": float(max(err))}), flush=True)
     return 0
@@ -288,9 +291,13 @@ def run_adjoint(args, world, rank, local, pg):
     torch.cuda.set_device(local)
     n = args.n or 256
     shape = (n,) * 3
+    # itmax bounds every solve (the forward at tol 1e-10 needs ~450 PT
+    # iterations per step at 256^3, an adjoint solve ~450 or stops at its
+    # arithmetic floor, see ptd_adj_residuals)
     s = S.SCRIPTS["diff_3D_nonlin_multixpu"].with_(
         name="adjoint_3d_256", model=S.NONLIN_EXPM, shift=1.0, dirichlet=1.0, ttot=1.0, dt=0.1,
-        tol=args.adj_tol, itmax=200000, ic="linrange")
+        tol=args.adj_tol, itmax=20000, ic="linrange")
+    log = lambda *a: print(*a, file=sys.stderr, flush=True)
     H0 = S.initial_condition(s, *shape)
     m = S.log_coefficient_field(shape, seed=0)
     mt = m + S.log_coefficient_field(shape, seed=1)   # the perturbed coefficient of the target
@@ -324,12 +331,17 @@ def run_adjoint(args, world, rank, local, pg):
             fwd_iters += int(A.forward_iters.sum())
             adj_iters += int(A.adjoint_iters.sum())
         l1, i1 = A.counters()
+        res_err, res_target = A.residuals()
+        log(f"adjoint {prec}: forward {t_fwd / nsteps:.2f} s, adjoint {t_adj / nsteps:.2f} s per gradient, "
+            f"forward iterations {list(A.forward_iters)}, adjoint {list(A.adjoint_iters)}")
         t_tot = reduce_max(pg, t_fwd + t_adj)
         rec = {"grads_per_s": round(world * nsteps / t_tot, 4), "ms_per_gradient": round(t_tot / nsteps * 1e3, 2),
                "forward_ms": round(t_fwd / nsteps * 1e3, 2), "adjoint_ms": round(t_adj / nsteps * 1e3, 2),
                "adjoint_over_forward": round(t_adj / t_fwd, 3),
                "forward_pt_iterations": fwd_iters // nsteps, "adjoint_pt_iterations": adj_iters // nsteps,
-               "gpu_launches": int(l1 - l0), "loss": loss}
+               "gpu_launches": int(l1 - l0), "loss": loss,
+               "adjoint_final_rel_residual": [float(e / t * 1e-10) if t > 0 else 0.0
+                                              for e, t in zip(res_err, res_target)]}
         if prec == "df64":
             # e2e: host arrays in and out, the library copies them
             gm_h, gh_h = None, None
@@ -353,6 +365,7 @@ def run_adjoint(args, world, rank, local, pg):
                 fd = (4 * d2 - d1) / 3
                 rel = abs(fd - gv) / max(abs(gv), 1e-300)
                 rels.append(rel)
+                log(f"fd direction {len(rels)}: adjoint {gv:.9e} fd {fd:.9e} rel {rel:.2e}")
                 worst = max(worst, rel)
             rec["fd_check"] = {"directions": len(rels), "eps": args.fd_eps, "max_rel_err": worst,
                                "median_rel_err": float(np.median(rels)) if rels else None}
@@ -441,6 +454,17 @@ def run_ours(args, world, rank, local, pg):
     peak, peak_kind = read_peaks()
     traffic = profile_traffic(args.workload)
     sol.close()
+    # the native-FP64 kernel's own roofline: FP64 instructions per cell x
+    # cells / launch time against this GPU's FP64 FMA rate, measured now
+    rate = ctypes.c_double(0.0)
+    ptdiff._abi.check(ptdiff._abi.lib().ptd_measure_fp64_rate(ctypes.byref(rate)), "ptd_measure_fp64_rate")
+    fp64_per_cell = {2: 19, 3: 27}.get(s.ndim) if s.model == ptdiff.scripts.NONLIN else None
+    fp64_pipe = None
+    if fp64_per_cell and args.precision == "fp64":
+        ach = fp64_per_cell * float(np.prod(shape)) / t_launch / 1e9
+        fp64_pipe = {"bound": "fp64 pipe", "achieved": round(ach, 1), "peak": round(rate.value / 1e9, 1),
+                     "unit": "G FP64 instr/s", "frac": round(ach / (rate.value / 1e9), 4),
+                     "instr_per_cell": fp64_per_cell, "peak_kind": "measured live (DFMA chains)"}
 
     # ---- the same FP64-accuracy iteration with double-float arithmetic on the
     # FP32 pipe: DFH (FP64 H, double-float fluxes) everywhere; DF64 (every value
@@ -533,6 +557,7 @@ def run_ours(args, world, rank, local, pg):
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_kind": peak_kind, "kernel": f"pt{s.ndim}d_kernel (fused PT iteration)",
                      "launch_us": round(t_launch * 1e6, 2), "algorithmic_bytes_per_launch": A},
+        "fp64_pipe": fp64_pipe,
         "cpu_baseline": cb,
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": int(H0.size * 8),
                 "d2h_bytes_per_step": int(H0.size * 8)},

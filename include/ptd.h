@@ -97,6 +97,8 @@ enum { PTD_NORM_RMS = 0, PTD_NORM_MAX = 1 };
 #define PTD_FLAG_STRICT 0x1   /* return PTD_ENOTCONV when a step stops at itmax */
 #define PTD_FLAG_AUTOTUNE 0x2 /* ptd_create times every launch shape of the fused kernel (2D: warps per CTA
                                  x rows per y march; 3D: z-march length x warps per CTA) and keeps the fastest */
+#define PTD_FLAG_DC_NO_TBLOCK 0x4 /* FP32_DC in 2D: one inner iteration per launch (default: two per launch,
+                                     temporally blocked, when the check cadence is even) */
 
 typedef struct ptd_params {
     int32_t ndim;        /* 1, 2, 3 */
@@ -206,8 +208,13 @@ PTD_API int ptd_batch_create(ptd_batch** b, const ptd_batch_params* p, const int
 PTD_API int ptd_batch_solve(ptd_batch* b, double* const* H, const double* const* D, int32_t* iters,
                             double* err_last, int32_t* n_done);
 /* Autotuner: times every (warps per CTA, rows per y chunk) launch shape of the
- * batched kernel on the batch's own instances and keeps the fastest. */
+ * batched kernel on the batch's own instances -- for FP32_DC also one or two
+ * (temporally blocked) inner iterations per launch -- and keeps the fastest
+ * per iteration. */
 PTD_API int ptd_batch_tune(ptd_batch* b, int32_t* warps, int32_t* chunk, float* us_per_iteration);
+/* The launch shape in use: warps per CTA, rows per y chunk, inner iterations
+ * per launch (2 = temporally blocked FP32_DC kernel). */
+PTD_API int ptd_batch_config(ptd_batch* b, int32_t* warps, int32_t* chunk, int32_t* iters_per_launch);
 PTD_API int ptd_batch_counters(ptd_batch* b, int64_t* kernel_launches, int64_t* pt_iterations);
 PTD_API void ptd_batch_destroy(ptd_batch* b);
 
@@ -224,6 +231,13 @@ PTD_API int ptd_adj_create(ptd_adj** a, const ptd_params* p);
 PTD_API int ptd_adj_forward(ptd_adj* a, const double* H0, const double* m, const double* Ht, double* loss,
                             double* HN, int32_t* iters_per_step);
 PTD_API int ptd_adj_gradient(ptd_adj* a, double* grad_m, double* grad_H0, int32_t* adj_iters_per_step);
+/* Last ptd_adj_gradient: the final RMS residual of each step's adjoint solve
+ * and its stopping target (1e-10 x the RMS of its right-hand side); nt
+ * entries each, nullable.  A solve also stops when its residual has stalled
+ * (no 1 % gain over ~2 max(nx,ny,nz) iterations) at an arithmetic floor below
+ * 1e-7 x the RMS of its right-hand side.  With PTD_FLAG_STRICT,
+ * ptd_adj_gradient returns PTD_ENOTCONV when a solve stopped at itmax. */
+PTD_API int ptd_adj_residuals(ptd_adj* a, double* err, double* target);
 PTD_API int ptd_adj_counters(ptd_adj* a, int64_t* kernel_launches, int64_t* pt_iterations);
 PTD_API void ptd_adj_destroy(ptd_adj* a);
 
@@ -250,6 +264,13 @@ PTD_API void ptd_adj_destroy(ptd_adj* a);
 #define PTD_NOALLOC_MAX_CELLS 524288
 PTD_API int ptd_solve_2d_noalloc(const ptd_params* p, double* H, const double* D, void* stream,
                                  int32_t* iters_per_step);
+
+/* Diagnostic, no reference counterpart: the FP64 FMA throughput of the
+ * current GPU in operations per second (8 independent FMA chains per thread,
+ * 8 CTAs of 256 threads per SM, CUDA-event timed; ~20 ms).  It is the roofline
+ * of the native-FP64 PT kernels, which need 19 (2D) / 27 (3D) FP64
+ * instructions per cell and so are bound by this rate rather than by HBM. */
+PTD_API int ptd_measure_fp64_rate(double* ops_per_s);
 
 PTD_API const char* ptd_strerror(int status);
 PTD_API const char* ptd_last_error(void);   /* detail of the last failure on this thread */

@@ -52,9 +52,12 @@ struct AdjArgs {
     double* acc;
 };
 
+// done: 1 converged (err <= target), 2 itmax, 3 stalled at an arithmetic
+// floor below the acceptable level (err <= accept, no 1 % improvement over
+// `stall` checks)
 struct AdjState {
-    int done, nchecks, iter, pad;
-    double acc, err, target;
+    int done, nchecks, iter, best_at;
+    double acc, err, target, accept, best;
 };
 
 template <class N>
@@ -291,18 +294,22 @@ __global__ void __launch_bounds__(256) adj_grad_kernel(AdjArgs a, const double* 
     }
 }
 
-__global__ void adj_target_kernel(AdjState* st, double rtol, double norm_den, double floor_abs)
+__global__ void adj_target_kernel(AdjState* st, double rtol, double accept_rtol, double norm_den,
+                                  double floor_abs)
 {
     const double gn = sqrt(st->acc) / sqrt(norm_den);
     st->acc = 0.0;
     st->target = fmax(rtol * gn, floor_abs);
+    st->accept = fmax(accept_rtol * gn, floor_abs);
     st->done = gn == 0.0 ? 1 : 0;
     st->nchecks = 0;
     st->iter = 0;
     st->err = gn;
+    st->best = gn;
+    st->best_at = 0;
 }
 
-__global__ void adj_judge_kernel(AdjState* st, int nchk, int itmax, double norm_den)
+__global__ void adj_judge_kernel(AdjState* st, int nchk, int itmax, double norm_den, int stall)
 {
     if (st->done) return;
     const double err = sqrt(st->acc) / sqrt(norm_den);
@@ -310,7 +317,13 @@ __global__ void adj_judge_kernel(AdjState* st, int nchk, int itmax, double norm_
     st->err = err;
     st->nchecks += 1;
     st->iter += nchk;
+    if (err < 0.99 * st->best) {
+        st->best = err;
+        st->best_at = st->nchecks;
+    }
     if (!(err > st->target)) st->done = 1;
+    else if (err != err) st->done = 2;
+    else if (st->nchecks - st->best_at >= stall && err <= st->accept) st->done = 3;
     else if (st->iter + nchk > itmax) st->done = 2;
 }
 
@@ -387,9 +400,13 @@ struct ptd_adj {
     AdjArgs* d_args[2] = {nullptr, nullptr};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int nchk = 20;
-    double rtol = 1e-10;
+    double rtol = 1e-10;        // adjoint solve target, relative to its right-hand side
+    double accept_rtol = 1e-7;  // a solve stalled at an arithmetic floor below this is accepted
+    int stall = 10;             // checks without 1 % improvement that count as stalled
     bool have_fwd = false;
     long long launches = 0, iterations = 0;
+    std::vector<double> step_err, step_target;   // last adjoint solve: final residual and target per step
+    bool any_capped = false;
 };
 
 namespace {
@@ -467,7 +484,7 @@ int adj_capture(ptd_adj* A)
             par ^= 1;
         }
         if (err == cudaSuccess) {
-            adj_judge_kernel<<<1, 1, 0, A->s>>>(A->st, A->nchk, A->p.itmax, A->dv.norm_den);
+            adj_judge_kernel<<<1, 1, 0, A->s>>>(A->st, A->nchk, A->p.itmax, A->dv.norm_den, A->stall);
             err = cudaGetLastError();
         }
         cudaError_t e2 = cudaStreamEndCapture(A->s, &gr);
@@ -519,6 +536,10 @@ extern "C" int ptd_adj_create(ptd_adj** out, const ptd_params* p)
     A->expm = p->model == PTD_MODEL_NONLIN_EXPM;
     derive(A->p, A->dv);
     A->cfg = tuned_config(A->p);
+    {   // stagnation window: ~2 n_max iterations, the PT iteration's own time scale
+        const int nmax = std::max(p->nx, std::max(p->ny, p->nz));
+        A->stall = std::max(10, (2 * nmax + A->nchk - 1) / A->nchk);
+    }
     A->g.nx = p->nx;
     A->g.ny = p->ny;
     A->g.nz = p->nz;
@@ -630,6 +651,9 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
     if (!A) return set_error(PTD_EINVAL, "ptd_adj_gradient: NULL argument");
     if (!A->have_fwd) return set_error(PTD_ESTATE, "ptd_adj_gradient: run ptd_adj_forward first");
     const size_t b = (size_t)A->g.nfield * sizeof(double);
+    A->step_err.assign(A->p.nt, 0.0);
+    A->step_target.assign(A->p.nt, 0.0);
+    A->any_capped = false;
     ACK(cudaMemsetAsync(A->gm, 0, b, A->s));
     ACK(cudaMemsetAsync(A->gh, 0, b, A->s));
     // g = H^nt - Ht on inner cells
@@ -656,7 +680,7 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
             adj_sumsq_kernel<F64><<<152 * 8, 256, 0, A->s>>>(A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
                                                              A->g.sy, A->g.sz);
         ACK(cudaGetLastError());
-        adj_target_kernel<<<1, 1, 0, A->s>>>(A->st, A->rtol, A->dv.norm_den, 1e-300);
+        adj_target_kernel<<<1, 1, 0, A->s>>>(A->st, A->rtol, A->accept_rtol, A->dv.norm_den, 1e-300);
         ACK(cudaGetLastError());
         A->launches += 3;
         long long launched = 0, batch = 1;
@@ -676,6 +700,9 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         const int iters = A->h_st->iter;
         A->iterations += iters;
         if (adj_iters) adj_iters[n - 1] = iters;
+        A->step_err[n - 1] = A->h_st->err;
+        A->step_target[n - 1] = A->h_st->target;
+        if (A->h_st->done == 2) A->any_capped = true;   // 3 (stalled below accept_rtol) is accepted
         AdjArgs a;
         adj_fill(A, iters & 1, a);
 #define AGK(NT, EX) adj_grad_kernel<NT, EX><<<152 * 8, 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells)
@@ -704,6 +731,18 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         if (rc) return rc;
     }
     ACK(cudaStreamSynchronize(A->s));
+    if ((A->p.flags & PTD_FLAG_STRICT) && A->any_capped)
+        return set_error(PTD_ENOTCONV, "ptd_adj_gradient: an adjoint solve reached itmax");
+    return PTD_OK;
+}
+
+extern "C" int ptd_adj_residuals(ptd_adj* A, double* err, double* target)
+{
+    if (!A) return set_error(PTD_EINVAL, "adjoint is NULL");
+    for (int n = 0; n < A->p.nt; ++n) {
+        if (err) err[n] = A->step_err[n];
+        if (target) target[n] = A->step_target[n];
+    }
     return PTD_OK;
 }
 

@@ -115,6 +115,20 @@ __global__ void __launch_bounds__(256) dc2d_batch_kernel(const DcArgs* __restric
     if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
+// two inner iterations per launch (temporal blocking, ptd_dc_body.cuh)
+template <int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) dc2d_tb2_batch_kernel(const DcArgs* __restrict__ tab,
+                                                             const int4* __restrict__ work, int chunk)
+{
+    const int4 w = work[blockIdx.x];
+    const DcArgs a = tab[w.x];
+    if (dc_done(a.done)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    dc2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+}
+
 __global__ void inner_judge_batch_kernel(BDev* st, int ninst, int nchk, int itmax, int norm_max, int stall)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -309,11 +323,13 @@ __global__ void set_done_batch_kernel(BDev* st, int ninst, int v)
     if (i < ninst) st[i].done = v;
 }
 
-__global__ void parity_batch_kernel(const BDev* st, int* cur_parity, int ninst)
+// buffer of each instance's current correction: one swap per launch, `tb`
+// inner iterations per launch
+__global__ void parity_batch_kernel(const BDev* st, int* cur_parity, int ninst, int tb)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ninst) return;
-    if (st[i].phase == PH_INNER) cur_parity[i] = st[i].iter & 1;
+    if (st[i].phase == PH_INNER) cur_parity[i] = (st[i].iter / tb) & 1;
 }
 
 __global__ void tofloat_batch_kernel(const double* src, float* dst, long long n)
@@ -384,6 +400,7 @@ struct ptd_batch {
     int4* work = nullptr;
     int nwork = 0;
     int nchk = 10;
+    int tb = 1;        // FP32_DC: inner iterations per launch (2: temporal blocking)
     int stall = 10;
     cudaGraphExec_t g[2] = {nullptr, nullptr};
     int kernels_per_graph = 0;
@@ -431,8 +448,10 @@ cudaError_t launch_dc_batch(ptd_batch* b, int par, bool check)
     const dim3 blk(32, b->cfg.warps2d);
     const DcArgs* t = b->dtab[par];
 #define DCB(M)                                                                                                 \
-    (check ? dc2d_batch_kernel<M, true><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)                 \
-           : dc2d_batch_kernel<M, false><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d))
+    (b->tb == 2 ? (check ? dc2d_tb2_batch_kernel<M, true><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d) \
+                         : dc2d_tb2_batch_kernel<M, false><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)) \
+                : (check ? dc2d_batch_kernel<M, true><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)    \
+                         : dc2d_batch_kernel<M, false><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)))
     if (b->model == LIN) DCB(LIN);
     else if (b->model == LINSTEP) DCB(LINSTEP);
     else DCB(NONLIN);
@@ -445,7 +464,8 @@ void build_work(ptd_batch* b, std::vector<int4>& work)
     work.clear();
     const int W = b->cfg.warps2d, ch = b->cfg.chunk2d;
     for (int i = 0; i < b->ninst; ++i) {
-        const int tiles = (b->inst[i].nx - 2 + 30) / 31;
+        // x tiles of 31 updated columns, or 29 for the temporally blocked kernel
+        const int tiles = (b->dc && b->tb == 2) ? (b->inst[i].nx - 1 + 28) / 29 : (b->inst[i].nx - 2 + 30) / 31;
         const int bx = (tiles + W - 1) / W;
         const int by = (b->inst[i].ny - 2 + ch - 1) / ch;
         for (int y = 0; y < by; ++y)
@@ -475,8 +495,9 @@ int capture(ptd_batch* b)
         BCK(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
         cudaError_t err = cudaSuccess;
         int par = q, nk = 0;
-        for (int it = 0; it < b->nchk && err == cudaSuccess; ++it) {
-            const bool check = it == b->nchk - 1;
+        const int nl = b->dc ? b->nchk / b->tb : b->nchk;   // launches per check block
+        for (int it = 0; it < nl && err == cudaSuccess; ++it) {
+            const bool check = it == nl - 1;
             err = b->dc ? launch_dc_batch(b, par, check) : launch_pt_batch(b, par, check);
             par ^= 1;
             ++nk;
@@ -759,6 +780,7 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
     }
     b->nchk = b->dc ? std::max(1, std::min(p->nchk, 50)) : p->nchk;
     if (b->dc && p->itmax % b->nchk) b->nchk = p->nchk;
+    b->tb = (b->dc && b->nchk % 2 == 0 && !(p->flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
     cudaError_t e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         free_batch(b);
@@ -927,7 +949,7 @@ static int batch_dc_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
             while (launched < blocks_max) {
                 const long long k = std::min(batch, blocks_max - launched);
                 for (long long j = 0; j < k; ++j) {
-                    BCK(cudaGraphLaunch(b->g[(int)(((launched + j) * b->nchk) & 1)], b->s));
+                    BCK(cudaGraphLaunch(b->g[(int)(((launched + j) * (b->nchk / b->tb)) & 1)], b->s));
                     b->launches += b->kernels_per_graph;
                 }
                 launched += k;
@@ -940,7 +962,7 @@ static int batch_dc_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
             }
             for (int i = 0; i < n; ++i)
                 if (b->h_bst[i].phase == PH_INNER) b->iterations += b->h_bst[i].iter;
-            parity_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, b->cur_parity, n);
+            parity_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, b->cur_parity, n, b->tb);
             BCK(cudaGetLastError());
         }
         apply_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->dtab[0], b->bst, b->fwork, b->H_ptrs, b->cur_parity);
@@ -1024,15 +1046,19 @@ extern "C" int ptd_batch_solve(ptd_batch* b, double* const* H, const double* con
     return PTD_OK;
 }
 
-// Autotuner: time each (warps per block, rows per y chunk) candidate on the
-// current state with a few plain iterations, keep the fastest, re-capture.
+// Autotuner: time each (warps per block, rows per y chunk[, iterations per
+// launch]) candidate on the current state with a few plain launches, keep the
+// fastest per inner iteration, re-capture.  FP32_DC with an even check cadence
+// also tries the temporally blocked kernel (two iterations per launch).
 extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_out, float* us_out)
 {
     if (!b) return bfail(PTD_EINVAL, "batch is NULL");
     const int Ws[] = {2, 4, 8};
     const int Cs[] = {16, 32, 64, 128};
-    float best = 1e30f;
+    const bool try_tb = b->dc && b->nchk % 2 == 0 && !(b->bp.flags & PTD_FLAG_DC_NO_TBLOCK);
+    float best = 1e30f;   // ms per inner iteration
     LaunchCfg bestc = b->cfg;
+    int best_tb = b->tb;
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
@@ -1045,27 +1071,32 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
     } else {
         BCK(cudaMemsetAsync(b->st, 0, b->ninst * sizeof(DevState), b->s));
     }
-    for (int W : Ws)
-        for (int C : Cs) {
-            b->cfg.warps2d = W;
-            b->cfg.chunk2d = C;
-            int rc = upload_work(b);
-            if (rc) return rc;
-            for (int rep = 0; rep < 2; ++rep) {
-                BCK(cudaEventRecord(e0, b->s));
-                for (int it = 0; it < 6; ++it)
-                    BCK(b->dc ? launch_dc_batch(b, it & 1, false) : launch_pt_batch(b, it & 1, false));
-                BCK(cudaEventRecord(e1, b->s));
-                BCK(cudaEventSynchronize(e1));
+    for (int tbc = 1; tbc <= (try_tb ? 2 : 1); ++tbc)
+        for (int W : Ws)
+            for (int C : Cs) {
+                b->tb = b->dc ? tbc : 1;
+                b->cfg.warps2d = W;
+                b->cfg.chunk2d = C;
+                int rc = upload_work(b);
+                if (rc) return rc;
+                const int nl = 12 / tbc;   // 12 inner iterations either way
+                for (int rep = 0; rep < 2; ++rep) {
+                    BCK(cudaEventRecord(e0, b->s));
+                    for (int it = 0; it < nl; ++it)
+                        BCK(b->dc ? launch_dc_batch(b, it & 1, false) : launch_pt_batch(b, it & 1, false));
+                    BCK(cudaEventRecord(e1, b->s));
+                    BCK(cudaEventSynchronize(e1));
+                }
+                float ms = 0.0f;
+                BCK(cudaEventElapsedTime(&ms, e0, e1));
+                ms /= 12.0f;
+                b->launches += 2 * nl;
+                if (ms < best) {
+                    best = ms;
+                    bestc = b->cfg;
+                    best_tb = b->tb;
+                }
             }
-            float ms = 0.0f;
-            BCK(cudaEventElapsedTime(&ms, e0, e1));
-            b->launches += 12;
-            if (ms < best) {
-                best = ms;
-                bestc = b->cfg;
-            }
-        }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (b->dc) {
@@ -1073,11 +1104,21 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
         BCK(cudaGetLastError());
     }
     b->cfg = bestc;
+    b->tb = best_tb;
     int rc = upload_work(b);
     if (!rc) rc = capture(b);
     if (rc) return rc;
     if (warps_out) *warps_out = bestc.warps2d;
     if (chunk_out) *chunk_out = bestc.chunk2d;
-    if (us_out) *us_out = best * 1000.0f / 6.0f;
+    if (us_out) *us_out = best * 1000.0f;
+    return PTD_OK;
+}
+
+extern "C" int ptd_batch_config(ptd_batch* b, int32_t* warps, int32_t* chunk, int32_t* iters_per_launch)
+{
+    if (!b) return bfail(PTD_EINVAL, "batch is NULL");
+    if (warps) *warps = b->cfg.warps2d;
+    if (chunk) *chunk = b->cfg.chunk2d;
+    if (iters_per_launch) *iters_per_launch = b->dc ? b->tb : 1;
     return PTD_OK;
 }

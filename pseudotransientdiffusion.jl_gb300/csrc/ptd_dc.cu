@@ -52,6 +52,17 @@ __global__ void __launch_bounds__(256) dc2d_kernel(DcArgs a, int chunk)
     if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
+// two inner iterations per launch (temporal blocking), see dc2d_tb2_body
+template <int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) dc2d_tb2_kernel(DcArgs a, int chunk)
+{
+    if (dc_done(a.done)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    dc2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+}
+
 template <int MODEL, bool CHECK, int R>
 __global__ void __launch_bounds__(32 * R) dc3d_kernel(DcArgs a, int chunk)
 {
@@ -204,6 +215,7 @@ struct DcState {
     cudaGraphExec_t gblock[2] = {nullptr, nullptr};
     int kernels_per_block = 0;
     int nchk = 0;
+    int tb = 1;                // inner iterations per launch (2: temporal blocking, 2D)
     int cur = 0;
     double rtol = 1e-3;
     int max_outer = 30;
@@ -213,10 +225,15 @@ struct DcState {
 };
 
 template <int MODEL, bool CHECK>
-static cudaError_t dc_launch_model(const DcArgs& a, int ndim, const LaunchCfg& cfg, cudaStream_t s)
+static cudaError_t dc_launch_model(const DcArgs& a, int ndim, const LaunchCfg& cfg, cudaStream_t s, int tb)
 {
     if (ndim == 1) {
         dc1d_kernel<MODEL, CHECK><<<(a.nx + 255) / 256, 256, 0, s>>>(a);
+    } else if (ndim == 2 && tb == 2) {
+        const int W = cfg.warps2d;
+        const int tiles = (a.nx - 1 + 28) / 29;
+        dim3 grid((tiles + W - 1) / W, (a.ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);
+        dc2d_tb2_kernel<MODEL, CHECK><<<grid, dim3(32, W), 0, s>>>(a, cfg.chunk2d);
     } else if (ndim == 2) {
         const int W = cfg.warps2d;
         const int tiles = (a.nx - 2 + 30) / 31;
@@ -231,15 +248,15 @@ static cudaError_t dc_launch_model(const DcArgs& a, int ndim, const LaunchCfg& c
 }
 
 static cudaError_t dc_launch(const DcArgs& a, int ndim, int model, bool check, const LaunchCfg& cfg,
-                             cudaStream_t s)
+                             cudaStream_t s, int tb = 1)
 {
     switch (model * 2 + (check ? 1 : 0)) {
-    case 0: return dc_launch_model<LIN, false>(a, ndim, cfg, s);
-    case 1: return dc_launch_model<LIN, true>(a, ndim, cfg, s);
-    case 2: return dc_launch_model<LINSTEP, false>(a, ndim, cfg, s);
-    case 3: return dc_launch_model<LINSTEP, true>(a, ndim, cfg, s);
-    case 4: return dc_launch_model<NONLIN, false>(a, ndim, cfg, s);
-    case 5: return dc_launch_model<NONLIN, true>(a, ndim, cfg, s);
+    case 0: return dc_launch_model<LIN, false>(a, ndim, cfg, s, tb);
+    case 1: return dc_launch_model<LIN, true>(a, ndim, cfg, s, tb);
+    case 2: return dc_launch_model<LINSTEP, false>(a, ndim, cfg, s, tb);
+    case 3: return dc_launch_model<LINSTEP, true>(a, ndim, cfg, s, tb);
+    case 4: return dc_launch_model<NONLIN, false>(a, ndim, cfg, s, tb);
+    case 5: return dc_launch_model<NONLIN, true>(a, ndim, cfg, s, tb);
     }
     return cudaErrorInvalidValue;
 }
@@ -283,10 +300,11 @@ static int dc_capture(DcState* dc, int parity)
     DCK(cudaStreamBeginCapture(dc->s, cudaStreamCaptureModeThreadLocal));
     cudaError_t err = cudaSuccess;
     int par = parity, nk = 0;
-    for (int it = 0; it < dc->nchk && err == cudaSuccess; ++it) {
+    const int nl = dc->nchk / dc->tb;   // launches per check block
+    for (int it = 0; it < nl && err == cudaSuccess; ++it) {
         DcArgs a;
         dc_args(dc, par, &dc->dev->done, a);
-        err = dc_launch(a, dc->ndim, dc->model, it == dc->nchk - 1, dc->cfg, dc->s);
+        err = dc_launch(a, dc->ndim, dc->model, it == nl - 1, dc->cfg, dc->s, dc->tb);
         ++nk;
         par ^= 1;
     }
@@ -323,6 +341,8 @@ int dc_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     dc->nfield = g.nfield;
     dc->cfg = tuned_config(p);
     dc->nchk = std::max(1, std::min(p.nchk, 50));
+    // 2D: two inner iterations per launch when a check block has an even count
+    dc->tb = (p.ndim == 2 && dc->nchk % 2 == 0 && !(p.flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
     dc->rtol = p.dc_inner_rtol > 0.0 ? p.dc_inner_rtol : 1e-3;
     dc->max_outer = p.dc_max_outer > 0 ? p.dc_max_outer : 30;
     {
@@ -453,7 +473,7 @@ static int dc_inner(DcState* dc, long long budget, int* iters)
     while (launched < blocks_max) {
         const long long nb = std::min(batch, blocks_max - launched);
         for (long long b = 0; b < nb; ++b) {
-            const int par = (int)(((launched + b) * dc->nchk) & 1);
+            const int par = (int)(((launched + b) * (dc->nchk / dc->tb)) & 1);
             DCK(cudaGraphLaunch(dc->gblock[par], dc->s));
             dc->k.launches += dc->kernels_per_block;
         }
@@ -465,7 +485,7 @@ static int dc_inner(DcState* dc, long long budget, int* iters)
         if (done != DONE_RUNNING) break;
         batch = std::min<long long>(batch * 2, 32);
     }
-    dc->cur = iter & 1;
+    dc->cur = (iter / dc->tb) & 1;   // one buffer swap per launch
     dc->k.iterations += iter;
     *iters = iter;
     return PTD_OK;
@@ -540,13 +560,18 @@ int dc_step(DcState* dc, const ptd_ctx_base& g, int32_t* iters, double* err_hist
 
 int dc_iterate(DcState* dc, const ptd_ctx_base&, int32_t niter)
 {
-    for (int32_t it = 0; it < niter; ++it) {
+    // fixed inner iterations (perf protocol): two per launch where the
+    // temporally blocked kernel is in use, a single one for an odd remainder
+    int32_t it = 0;
+    while (it < niter) {
+        const int tb = (dc->tb == 2 && niter - it >= 2) ? 2 : 1;
         DcArgs a;
         dc_args(dc, dc->cur, dc->zero_flag, a);
-        DCK(dc_launch(a, dc->ndim, dc->model, false, dc->cfg, dc->s));
+        DCK(dc_launch(a, dc->ndim, dc->model, false, dc->cfg, dc->s, tb));
         dc->cur ^= 1;
         dc->k.launches += 1;
-        dc->k.iterations += 1;
+        dc->k.iterations += tb;
+        it += tb;
     }
     return PTD_OK;
 }

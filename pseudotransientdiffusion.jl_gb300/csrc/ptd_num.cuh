@@ -93,8 +93,27 @@ struct DF64 {
         const float e = __fmaf_rn(a.y, c, __fmaf_rn(a.x, c, -p));
         return fast_two_sum(p, e);
     }
-    __device__ static __forceinline__ T mad(T a, T b, T c) { return add(mul(a, b), c); }
+    // a*b + c: the exact-product pair (p, e) of a.x*b.x, plus the cross
+    // terms, summed into c with one normalisation (15 FP32 operations instead
+    // of 18 for add(mul(a, b), c); same error bound)
+    __device__ static __forceinline__ T mad(T a, T b, T c)
+    {
+        const float p = __fmul_rn(a.x, b.x);
+        float e = __fmaf_rn(a.x, b.x, -p);
+        e = __fmaf_rn(a.x, b.y, e);
+        e = __fmaf_rn(a.y, b.x, e);
+        const T s = two_sum(p, c.x);
+        return fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(e, c.y)));
+    }
     __device__ static __forceinline__ T nmad(T a, T b, T c) { return sub(c, mul(a, b)); }
+    // w - c*t with a float c, one normalisation (14 operations instead of 19)
+    __device__ static __forceinline__ T nmadf(T t, float c, T w)
+    {
+        const float p = __fmul_rn(t.x, c);
+        const float e = __fmaf_rn(t.y, c, __fmaf_rn(t.x, c, -p));
+        const T s = two_sum(w.x, -p);
+        return fast_two_sum(s.x, __fadd_rn(s.y, __fsub_rn(w.y, e)));
+    }
     __device__ static __forceinline__ float lo_f(T a) { return a.x; }
     __device__ static __forceinline__ double to_d(T a) { return (double)a.x + (double)a.y; }
     __device__ static __forceinline__ T zero() { return make_float2(0.0f, 0.0f); }
@@ -117,7 +136,7 @@ struct DF64 {
     __device__ static __forceinline__ T hsum(HV l, HV r) { return add(l, r); }
     __device__ static __forceinline__ T hdo(HV h, HS o) { return sub(h, o); }
     __device__ static __forceinline__ T hdn(HS h, HS o) { return sub(h, o); }
-    __device__ static __forceinline__ HS hstep(HV h, T rp, float e) { return sub(h, mulf(rp, e)); }
+    __device__ static __forceinline__ HS hstep(HV h, T rp, float e) { return nmadf(rp, e, h); }
 };
 
 // A double as a double-float, with integer operations only (the hardware
@@ -125,7 +144,9 @@ struct DF64 {
 // significant bits, lo = the remainder truncated to 24 bits, so
 // |x - (hi + lo)| < 2^-47 |x| and |lo| < ulp(hi).  For 2^-126 <= |x| < 2^-74
 // the remainder is dropped (absolute error < 2^-97), below 2^-126 the result
-// is 0; Inf stays Inf and NaN NaN (in hi).
+// is 0.  |x| >= 2^128, Inf and NaN give hi = Inf: every double-float operation
+// on it (two-sum, two-product) then yields NaN, so a NaN state still shows up
+// as a NaN residual.
 __device__ __forceinline__ float2 split_bits(double x)
 {
     const unsigned hi32 = (unsigned)__double2hiint(x);
@@ -135,13 +156,12 @@ __device__ __forceinline__ float2 split_bits(double x)
     const int ef = E - 896;   // biased float exponent of x
     unsigned h = sign | ((unsigned)ef << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
     h = ef <= 0 ? sign : h;
-    const bool nan = E == 0x7ff && ((hi32 & 0xfffffu) | lo32) != 0u;
-    h = ef >= 255 ? (sign | 0x7f800000u | (nan ? 0x400000u : 0u)) : h;
-    // remainder: the low 29 significand bits, worth m29 * 2^(E - 1075)
+    h = ef >= 255 ? (sign | 0x7f800000u) : h;
+    // remainder: the low 29 significand bits, worth m29 * 2^(E - 1075); a
+    // scale exponent <= 0 (x < 2^-74) gives the scale 0 and so lo = 0
     const int es = E - 948;   // biased float exponent of 2^(E - 1075)
     const float m29 = __uint2float_rz(lo32 & 0x1fffffffu);
-    float l = __fmul_rn(m29, __uint_as_float((unsigned)max(es, 1) << 23));
-    l = (es >= 1 && ef < 255) ? l : 0.0f;
+    const float l = __fmul_rn(m29, __uint_as_float((unsigned)max(es, 0) << 23));
     return make_float2(__uint_as_float(h), __uint_as_float(__float_as_uint(l) | sign));
 }
 

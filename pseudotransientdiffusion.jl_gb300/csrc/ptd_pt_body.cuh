@@ -12,7 +12,7 @@ namespace ptd {
 
 // w - c*t with a float damping coefficient c.
 __device__ __forceinline__ double nmadf(F64, float c, double t, double w) { return fma(-f2d_bits(c), t, w); }
-__device__ __forceinline__ float2 nmadf(DF64, float c, float2 t, float2 w) { return DF64::sub(w, DF64::mulf(t, c)); }
+__device__ __forceinline__ float2 nmadf(DF64, float c, float2 t, float2 w) { return DF64::nmadf(t, c, w); }
 
 template <class N>
 __device__ __forceinline__ typename N::T ld(const void* p, long long i)

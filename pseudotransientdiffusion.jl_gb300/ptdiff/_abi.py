@@ -22,6 +22,7 @@ RESID_MIXED, RESID_CONSISTENT = 0, 1
 NORM_RMS, NORM_MAX = 0, 1
 FLAG_STRICT = 0x1
 FLAG_AUTOTUNE = 0x2
+FLAG_DC_NO_TBLOCK = 0x4
 
 
 class PtdParams(C.Structure):
@@ -72,6 +73,7 @@ def lib():
         "ptd_solve": (C.c_int, [vp, vp, vp, ip, dp, C.c_int32, ip]),
         "ptd_set_state": (C.c_int, [vp, vp, vp]),
         "ptd_set_state2": (C.c_int, [vp, vp, vp, vp]),
+        "ptd_measure_fp64_rate": (C.c_int, [dp]),
         "ptd_step": (C.c_int, [vp, C.c_int32, ip, dp, C.c_int32, ip]),
         "ptd_iterate": (C.c_int, [vp, C.c_int32]),
         "ptd_get_state": (C.c_int, [vp, vp]),

@@ -30,6 +30,8 @@ def _lib():
         L.ptd_adj_forward.restype = C.c_int
         L.ptd_adj_gradient.argtypes = [vp, vp, vp, ip]
         L.ptd_adj_gradient.restype = C.c_int
+        L.ptd_adj_residuals.argtypes = [vp, dp, dp]
+        L.ptd_adj_residuals.restype = C.c_int
         L.ptd_adj_counters.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.ptd_adj_counters.restype = C.c_int
         L.ptd_adj_destroy.argtypes = [vp]
@@ -99,6 +101,14 @@ class AdjointSolver:
                                            iters.ctypes.data_as(C.POINTER(C.c_int32))), "ptd_adj_gradient")
         self.adjoint_iters = iters[: self.params.nt].copy()
         return gm, gh
+
+    def residuals(self):
+        """(final residual, target) of each step's adjoint solve in the last gradient()."""
+        e = np.zeros(max(self.params.nt, 1))
+        t = np.zeros(max(self.params.nt, 1))
+        _abi.check(_lib().ptd_adj_residuals(self._h, e.ctypes.data_as(C.POINTER(C.c_double)),
+                                            t.ctypes.data_as(C.POINTER(C.c_double))), "ptd_adj_residuals")
+        return e[: self.params.nt], t[: self.params.nt]
 
     def counters(self):
         l, it = C.c_int64(0), C.c_int64(0)

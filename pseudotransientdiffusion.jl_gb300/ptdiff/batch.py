@@ -50,6 +50,8 @@ def _lib():
         L.ptd_batch_solve.restype = C.c_int
         L.ptd_batch_tune.argtypes = [vp, ip, ip, C.POINTER(C.c_float)]
         L.ptd_batch_tune.restype = C.c_int
+        L.ptd_batch_config.argtypes = [vp, ip, ip, ip]
+        L.ptd_batch_config.restype = C.c_int
         L.ptd_batch_counters.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.ptd_batch_counters.restype = C.c_int
         L.ptd_batch_destroy.argtypes = [vp]
@@ -99,6 +101,12 @@ class BatchSolver:
         w, c, us = C.c_int32(0), C.c_int32(0), C.c_float(0)
         _abi.check(_lib().ptd_batch_tune(self._h, C.byref(w), C.byref(c), C.byref(us)), "ptd_batch_tune")
         return w.value, c.value, us.value
+
+    def config(self):
+        """(warps per CTA, rows per y chunk, inner iterations per launch)."""
+        w, c, t = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        _abi.check(_lib().ptd_batch_config(self._h, C.byref(w), C.byref(c), C.byref(t)), "ptd_batch_config")
+        return w.value, c.value, t.value
 
     def solve(self, Hs, Ds=None):
         """Solve in place on the list of Fortran-ordered arrays Hs.  Returns

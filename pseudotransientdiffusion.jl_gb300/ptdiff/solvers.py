@@ -28,7 +28,7 @@ PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC, "df64": _abi
 
 def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=None,
                 precision="fp64", resid="mixed", norm="rms", norm_len=0.0, strict=False,
-                autotune=False, dc_max_outer=0, dc_inner_rtol=0.0) -> _abi.PtdParams:
+                autotune=False, dc_max_outer=0, dc_inner_rtol=0.0, dc_tblock=True) -> _abi.PtdParams:
     """ptd_params for a script at a grid shape (x fastest)."""
     p = _abi.PtdParams()
     _abi.check(_abi.lib().ptd_params_init(C.byref(p), script.ndim, script.model), "ptd_params_init")
@@ -48,7 +48,8 @@ def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=No
     p.resid_mode = {"mixed": _abi.RESID_MIXED, "consistent": _abi.RESID_CONSISTENT}[resid]
     p.norm = {"rms": _abi.NORM_RMS, "max": _abi.NORM_MAX}[norm]
     p.norm_len = norm_len
-    p.flags = (_abi.FLAG_STRICT if strict else 0) | (_abi.FLAG_AUTOTUNE if autotune else 0)
+    p.flags = ((_abi.FLAG_STRICT if strict else 0) | (_abi.FLAG_AUTOTUNE if autotune else 0)
+               | (0 if dc_tblock else _abi.FLAG_DC_NO_TBLOCK))
     p.dc_max_outer = dc_max_outer
     p.dc_inner_rtol = dc_inner_rtol
     return p

@@ -59,6 +59,7 @@ def test_batch_autotuner(prec):
     with ptdiff.BatchSolver(p, sizes, sizes) as b:
         w, c, us = b.tune()
         assert w in (2, 4, 8) and c in (16, 32, 64, 128) and us > 0
+        assert b.config()[:2] == (w, c) and b.config()[2] in ((1, 2) if prec == "fp32_dc" else (1,))
         iters, err = b.solve(Hs, Ds)
     for k in range(len(sizes)):
         Hr, it_r, _, _ = oracle_instance(S.LINSTEP, Hs0[k], Ds[k], ttot=0.2)
@@ -67,3 +68,27 @@ def test_batch_autotuner(prec):
             assert rel_l2(Hs[k], Hr) <= 1e-10
         else:
             assert err[k] <= 1e-8
+
+
+@pytest.mark.parametrize("model", [S.LIN, S.LINSTEP, S.NONLIN])
+def test_batch_temporal_blocking_matches_one_iteration_per_launch(model):
+    """FP32_DC: two inner iterations per launch give the per-launch kernel's
+    iterations (same arithmetic per iteration) on uneven instances."""
+    from ptdiff import _abi
+
+    sizes, Hs, Ds = ptdiff.batch_instances(6, seed=5, nmin=3, nmax=140)
+    if model != S.LINSTEP:
+        Ds = None
+    out = []
+    for flags in (0, _abi.FLAG_DC_NO_TBLOCK):
+        H = [h.copy(order="F") for h in Hs]
+        p = ptdiff.batch_params(len(sizes), model=model, precision="fp32_dc", nt=2, flags=flags,
+                                resc=(1 / 1.2 if model == S.NONLIN else 1.0))
+        with ptdiff.BatchSolver(p, sizes, sizes) as b:
+            assert b.config()[2] == (1 if flags else 2)
+            iters, err = b.solve(H, Ds)
+        out.append((H, iters))
+    (H2, it2), (H1, it1) = out
+    assert np.array_equal(it1, it2)
+    for k in range(len(sizes)):
+        assert rel_l2(H2[k], H1[k]) <= 1e-12

@@ -72,3 +72,19 @@ def test_dc_nan_input():
     with ptdiff.Solver(p) as sol:
         _, _, st = sol.solve(H0, raise_on_nan=False)
     assert st == _abi.PTD_ENAN
+
+
+# 2D inner iterations run two per launch (temporal blocking); the arithmetic
+# of each iteration is the one-per-launch kernel's, so the two agree to the
+# order of the residual reduction.
+@pytest.mark.parametrize("name,shape", [
+    ("diff_2D_lin", (64, 64)), ("diff_2D_linstep", (66, 33)), ("diff_2D_nonlin", (97, 130)),
+    ("diff_2D_nonlin", (3, 3)), ("diff_2D_linstep", (200, 7)), ("diff_2D_lin", (31, 250)),
+    ("diff_2D_nonlin", (256, 256))])
+def test_temporal_blocking_matches_one_iteration_per_launch(name, shape):
+    s = S.SCRIPTS[name]
+    H2, _, it2, _, st2 = run_dc(s, shape)
+    H1, _, it1, _, st1 = run_dc(s, shape, dc_tblock=False)
+    assert st1 == 0 and st2 == 0
+    assert list(it1) == list(it2)
+    assert rel_l2(H2, H1) <= 1e-12
