@@ -81,8 +81,17 @@ enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL
  *           2D/3D grids of the reference and of the benchmarks (up to 8192^2
  *           and 512^3).  The 48-bit flux arithmetic sets a residual floor
  *           ~32x FP64's, which stalls 1D lin/linstep grids of nx >= 8192.
- *           Single grids only (not the batch or the adjoint). */
-enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH = 3 };
+ *           Single grids only (not the batch or the adjoint).
+ *  FP32_RB  FP32 PT iterations on the change since an FP64 base state
+ *           (H_b, fluxes w_b), rebased in FP64 every ~200 iterations: the
+ *           FP32 iteration carries only changes and defects that shrink as
+ *           the step converges, and keeps the PT iteration's momentum across
+ *           rebases (no restarted inner solves).  A step stops when the
+ *           reference's check residual (every nchk, formed in FP32 from the
+ *           FP64 base residual) and the FP64 residual of the rebased state
+ *           are both <= tol; H is the FP64 base.  2D and 3D, models LIN,
+ *           LINSTEP, NONLIN, mixed residual; single grids only. */
+enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH = 3, PTD_PREC_FP32_RB = 4 };
 
 /* Residual used for the stopping test.  MIXED is the reference's: the
  * undamped flux from the H the fluxes of that iteration were computed on, the

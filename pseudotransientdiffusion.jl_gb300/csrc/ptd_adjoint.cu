@@ -527,7 +527,7 @@ extern "C" int ptd_adj_create(ptd_adj** out, const ptd_params* p)
     if (p->ndim != 3) return set_error(PTD_EINVAL, "the adjoint solver is 3D");
     if (p->model != PTD_MODEL_NONLIN && p->model != PTD_MODEL_NONLIN_EXPM)
         return set_error(PTD_EINVAL, "the adjoint solver supports D = H^3 and D = exp(m) H^3");
-    if (p->precision == PTD_PREC_FP32_DC || p->precision == PTD_PREC_DFH)
+    if (p->precision == PTD_PREC_FP32_DC || p->precision == PTD_PREC_DFH || p->precision == PTD_PREC_FP32_RB)
         return set_error(PTD_EINVAL, "the adjoint runs in FP64 or DF64");
     ptd_adj* A = new (std::nothrow) ptd_adj();
     if (!A) return set_error(PTD_ENOMEM, "adjoint: host allocation failed");

@@ -142,8 +142,13 @@ int ptd::validate(const ptd_params* p)
     if (p->model < PTD_MODEL_NONLIN && (!(p->D > 0.0) || !std::isfinite(p->D)))
         return fail(PTD_EINVAL, "D must be > 0");
     if (p->precision != PTD_PREC_FP64 && p->precision != PTD_PREC_FP32_DC && p->precision != PTD_PREC_DF64 &&
-        p->precision != PTD_PREC_DFH)
+        p->precision != PTD_PREC_DFH && p->precision != PTD_PREC_FP32_RB)
         return fail(PTD_EINVAL, "unknown precision %d", p->precision);
+    if (p->precision == PTD_PREC_FP32_RB) {
+        if (p->ndim < 2) return fail(PTD_EINVAL, "FP32_RB: 2D and 3D grids only");
+        if (p->model > PTD_MODEL_NONLIN) return fail(PTD_EINVAL, "FP32_RB: models LIN, LINSTEP, NONLIN");
+        if (p->resid_mode != PTD_RESID_MIXED) return fail(PTD_EINVAL, "FP32_RB: mixed residual only");
+    }
     if (p->resid_mode != PTD_RESID_MIXED && p->resid_mode != PTD_RESID_CONSISTENT)
         return fail(PTD_EINVAL, "unknown resid_mode %d", p->resid_mode);
     if (p->norm != PTD_NORM_RMS && p->norm != PTD_NORM_MAX) return fail(PTD_EINVAL, "unknown norm %d", p->norm);
@@ -269,6 +274,7 @@ struct ptd_ctx : ptd_ctx_base {
     long long launches = 0, iterations = 0;
     int kernels_per_block = 0;
     DcState* dc = nullptr;        // FP32 defect-correction resources
+    RbState* rb = nullptr;        // FP32 rebased-form resources
     bool df64 = false;            // H and Hold hold double-floats (PTD_PREC_DF64)
     bool ddf = false;             // D and the fluxes hold double-floats (PTD_PREC_DF64, PTD_PREC_DFH)
     int num = NUM_F64;            // number type of the PT kernels
@@ -438,6 +444,7 @@ static void free_ctx(ptd_ctx* c)
         if (c->gplain[q]) cudaGraphExecDestroy(c->gplain[q]);
     }
     if (c->dc) dc_destroy(c->dc);
+    if (c->rb) rb_destroy(c->rb);
     cudaFree(c->H[0]);
     cudaFree(c->H[1]);
     cudaFree(c->Hold);
@@ -520,6 +527,12 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
             free_ctx(c);
             return rc;
         }
+    } else if (p->precision == PTD_PREC_FP32_RB) {
+        rc = rb_create(*c, c->p, c->dv, c->stream, &c->rb);
+        if (rc) {
+            free_ctx(c);
+            return rc;
+        }
     } else {
         if ((p->flags & PTD_FLAG_AUTOTUNE) && p->ndim > 1) rc = autotune(c);
         for (int q = 0; q < 2 && !rc; ++q) {
@@ -560,8 +573,8 @@ extern "C" int ptd_counters(ptd_ctx* c, int64_t* launches, int64_t* iters)
 {
     if (!c) return fail(PTD_EINVAL, "ctx is NULL");
     long long l = c->launches, it = c->iterations;
-    if (c->dc) {
-        const DcCounters k = dc_counters(c->dc);
+    if (c->dc || c->rb) {
+        const DcCounters k = c->dc ? dc_counters(c->dc) : rb_counters(c->rb);
         l += k.launches;
         it += k.iterations;
     }
@@ -630,6 +643,11 @@ extern "C" int ptd_set_state2(ptd_ctx* c, const double* H, const double* Hold, c
         rc = dc_set_state(c->dc, *c, c->H[0], c->Hold, c->D, c->stream);
         if (rc) return rc;
     }
+    if (c->rb) {
+        double* wb[3] = {c->W[0][0], c->W[1][0], c->W[2][0]};
+        rc = rb_set_state(c->rb, c->H[0], c->Hold, wb, c->D, c->stream);
+        if (rc) return rc;
+    }
     CK(cudaStreamSynchronize(c->stream));
     c->have_state = true;
     return PTD_OK;
@@ -679,6 +697,7 @@ extern "C" int ptd_iterate(ptd_ctx* c, int32_t niter)
     if (niter < 0) return fail(PTD_EINVAL, "niter must be >= 0");
     if (!c->have_state) return fail(PTD_ESTATE, "no state set");
     if (c->dc) return dc_iterate(c->dc, *c, niter);
+    if (c->rb) return rb_iterate(c->rb, niter);
     return run_plain(c, niter);
 }
 
@@ -746,8 +765,9 @@ extern "C" int ptd_step(ptd_ctx* c, int32_t nsteps, int32_t* iters_per_step, dou
     for (int s = 0; s < nsteps; ++s) {
         int32_t it = 0;
         int nan_flag = 0, capped = 0;
-        int rc = c->dc ? dc_step(c->dc, *c, &it, err_hist, err_cap, &ne, &nan_flag, &capped)
-                       : fp64_step(c, &it, err_hist, err_cap, &ne, &nan_flag, &capped);
+        int rc = c->dc   ? dc_step(c->dc, *c, &it, err_hist, err_cap, &ne, &nan_flag, &capped)
+                 : c->rb ? rb_step(c->rb, &it, err_hist, err_cap, &ne, &nan_flag, &capped)
+                         : fp64_step(c, &it, err_hist, err_cap, &ne, &nan_flag, &capped);
         if (rc) return rc;
         if (iters_per_step) iters_per_step[s] = it;
         any_capped |= capped;

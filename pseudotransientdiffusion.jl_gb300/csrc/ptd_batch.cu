@@ -740,7 +740,7 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
         return bfail(PTD_EINVAL, "batch: itmax must be a positive multiple of nchk");
     for (int k = 0; k < 8; ++k)
         if (p->reserved[k]) return bfail(PTD_EINVAL, "reserved fields must be zero");
-    if (p->precision == PTD_PREC_DFH) return bfail(PTD_EINVAL, "batch: precision FP64, DF64 or FP32_DC");
+    if (p->precision == PTD_PREC_DFH || p->precision == PTD_PREC_FP32_RB) return bfail(PTD_EINVAL, "batch: precision FP64, DF64 or FP32_DC");
     ptd_batch* b = new (std::nothrow) ptd_batch();
     if (!b) return bfail(PTD_ENOMEM, "batch: host allocation failed");
     b->bp = *p;

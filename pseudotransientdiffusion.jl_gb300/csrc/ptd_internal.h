@@ -60,4 +60,14 @@ struct DcCounters {
 };
 DcCounters dc_counters(const DcState* dc);
 
+// FP32 PT iterations on the change since an FP64 base, rebased (ptd_rb.cu).
+struct RbState;
+int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cudaStream_t s, RbState** out);
+void rb_destroy(RbState* rb);
+int rb_set_state(RbState* rb, double* H, double* Hold, double* const* wb, const double* D, cudaStream_t s);
+int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int32_t* n_err, int* nan_flag,
+            int* capped);
+int rb_iterate(RbState* rb, int32_t niter);
+DcCounters rb_counters(const RbState* rb);
+
 }  // namespace ptd

@@ -17,7 +17,7 @@ HEADER = os.path.join(ROOT, "include", "ptd.h")
 
 PTD_OK, PTD_EINVAL, PTD_ENAN, PTD_ENOTCONV, PTD_ECUDA, PTD_ENOMEM, PTD_ESTATE, PTD_ETIMEOUT = range(8)
 MODEL_LIN, MODEL_LINSTEP, MODEL_NONLIN = 0, 1, 2
-PREC_FP64, PREC_FP32_DC, PREC_DF64, PREC_DFH = 0, 1, 2, 3
+PREC_FP64, PREC_FP32_DC, PREC_DF64, PREC_DFH, PREC_FP32_RB = 0, 1, 2, 3, 4
 RESID_MIXED, RESID_CONSISTENT = 0, 1
 NORM_RMS, NORM_MAX = 0, 1
 FLAG_STRICT = 0x1

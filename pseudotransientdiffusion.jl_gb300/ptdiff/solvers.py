@@ -23,7 +23,7 @@ from . import _abi
 from .scripts import LINSTEP, SCRIPTS, Script, cell_centres, grid_shape, initial_condition, step_field
 
 PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC, "df64": _abi.PREC_DF64,
-              "dfh": _abi.PREC_DFH}
+              "dfh": _abi.PREC_DFH, "fp32_rb": _abi.PREC_FP32_RB}
 
 
 def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=None,

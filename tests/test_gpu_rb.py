@@ -1,0 +1,106 @@
+"""FP32 PT iterations on the change since an FP64 base, rebased in FP64
+(precision FP32_RB).  Every step must end with both the reference's check
+residual and the FP64 residual of the returned H at tol, so the bar against
+the FP64 oracle is the bound 2*dt*tol/rms(H) that any two solutions
+converged to tol obey; the PT iteration counts stay close to FP64's (the
+form keeps the iteration's fluxes across rebases)."""
+import numpy as np
+import pytest
+
+import ptdiff
+from oracle import oracle as O
+from ptdiff import _abi
+from ptdiff import scripts as S
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def run(s, shape, H0=None, **kw):
+    H = S.initial_condition(s, *shape) if H0 is None else np.array(H0, order="F", copy=True)
+    D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
+    p = ptdiff.make_params(s, shape, precision="fp32_rb", **kw)
+    with ptdiff.Solver(p) as sol:
+        iters, eh, st = sol.solve(H, D, raise_on_nan=False)
+    return H, D, iters, eh, st
+
+
+@pytest.mark.parametrize("name,shape", [
+    ("diff_2D_lin", (64, 64)), ("diff_2D_linstep", (66, 33)), ("diff_2D_nonlin", (64, 64)),
+    ("diff_2D_nonlin", (3, 3)), ("diff_2D_nonlin", (37, 95)),
+    ("diff_3D_lin_multixpu", (24, 24, 24)), ("diff_3D_linstep_multixpu", (3, 4, 5)),
+    ("diff_3D_nonlin_multixpu", (32, 30, 34)), ("diff_3D_linstep_multixpu", (40, 36, 50))])
+def test_rebased_fp32_matches_oracle(name, shape):
+    s = S.SCRIPTS[name]
+    H, D, iters, eh, st = run(s, shape)
+    H0 = S.initial_condition(s, *shape)
+    Hr, it_r, _, st_r = O.solve(s, H0, D)
+    assert st == 0 and st_r == 0
+    rms = float(np.sqrt(np.mean(np.square(Hr))))
+    assert rel_l2(H, Hr) <= 2 * s.dt * s.tol / rms
+    # close to the FP64 counts: a few extra check blocks at most per step
+    assert np.all(iters <= it_r + 6 * s.nout + 20), (list(iters), list(it_r))
+    assert len(eh) > 0 and eh[-1] <= s.tol
+
+
+@pytest.mark.parametrize("name,shape", [("diff_2D_nonlin_perf", (64, 64)), ("diff_3D_nonlin_perf", (32, 32, 32))])
+def test_rebased_fp32_fixed_iterations(name, shape):
+    """Perf scripts (nchk > itmax): exactly itmax PT iterations per step, no
+    checks; FP32 changes on an FP64 base track the FP64 iterates closely."""
+    s = S.SCRIPTS[name]
+    H, D, iters, eh, st = run(s, shape)
+    Hr, it_r, _, _ = O.solve(s, S.initial_condition(s, *shape), D)
+    assert list(iters) == list(it_r) == [s.itmax] * s.nt
+    assert len(eh) == 0
+    assert rel_l2(H, Hr) <= 1e-6
+
+
+@pytest.mark.parametrize("name,shape", [("2d_nonlin_4096", (512, 512)), ("3d_nonlin_512", (64, 64, 64))])
+def test_rebased_fp32_benchmark_problems(name, shape):
+    """The benchmark problems (H0 = 1 + exp(-r^2), Dirichlet H = 1) at reduced
+    size: against the GPU FP64 solve."""
+    s = ptdiff.scripts.CONFIGS[name]
+    H, _, iters, _, st = run(s, shape, nt=2)
+    H64 = S.initial_condition(s, *shape)
+    with ptdiff.Solver(ptdiff.make_params(s, shape, nt=2)) as sol:
+        it64, _, st64 = sol.solve(H64)
+    assert st == 0 and st64 == 0
+    rms = float(np.sqrt(np.mean(np.square(H64))))
+    assert rel_l2(H, H64) <= 2 * s.dt * s.tol / rms
+    assert np.all(np.abs(iters.astype(int) - it64.astype(int)) <= 3 * s.nout), (list(iters), list(it64))
+
+
+def test_rebased_fp32_nan_and_strict():
+    s = S.SCRIPTS["diff_2D_nonlin"]
+    H0 = S.initial_condition(s, 40, 40)
+    H0[20, 20] = np.nan
+    _, _, _, _, st = run(s, (40, 40), H0=H0)
+    assert st == _abi.PTD_ENAN
+    _, _, iters, _, st = run(S.SCRIPTS["diff_2D_lin"], (64, 64), itmax=30, strict=True)
+    assert st == _abi.PTD_ENOTCONV
+    assert list(iters) == [30] * 5
+
+
+def test_rebased_fp32_device_pointers_and_iterate():
+    torch = pytest.importorskip("torch")
+    s = S.SCRIPTS["diff_3D_nonlin_multixpu"]
+    shape = (33, 28, 30)
+    H0 = S.initial_condition(s, *shape)
+    Hd = torch.from_numpy(np.ravel(H0, order="F").copy()).cuda()
+    p = ptdiff.make_params(s, shape, precision="fp32_rb")
+    with ptdiff.Solver(p) as sol:
+        iters, _, st = sol.solve(Hd)
+        sol.set_state(H0)
+        sol.iterate(25)   # fixed iterations (perf protocol), folded into the FP64 state
+        Hi = sol.get_state()
+    Hr, _, _, _ = O.solve(s, H0)
+    assert st == 0
+    rms = float(np.sqrt(np.mean(np.square(Hr))))
+    assert rel_l2(Hd.cpu().numpy(), np.ravel(Hr, order="F")) <= 2 * s.dt * s.tol / rms
+    H25 = np.array(H0, order="F")
+    q = [np.zeros_like(H25) for _ in range(3)]
+    O.iterate(s, H25, H0.copy(order="F"), q, 25)
+    assert rel_l2(Hi, np.ravel(H25, order="F") if Hi.ndim == 1 else H25) <= 1e-5

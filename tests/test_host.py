@@ -179,3 +179,17 @@ def test_adjoint_create_rejects_unsupported_precisions():
         h = C.c_void_p()
         assert A._lib().ptd_adj_create(C.byref(h), C.byref(p)) == _abi.PTD_EINVAL
         assert "FP64 or DF64" in _abi.last_error()
+
+
+@pytest.mark.parametrize("kw,msg", [({"ndim": 1}, "2D and 3D"), ({"resid_mode": 1}, "mixed residual")])
+def test_rebased_fp32_rejections(kw, msg):
+    from ptdiff.solvers import make_params
+
+    s = S.SCRIPTS["diff_1D_lin" if kw.get("ndim") == 1 else "diff_2D_lin"]
+    shape = (32,) if s.ndim == 1 else (32, 32)
+    p = make_params(s, shape, precision="fp32_rb")
+    if "resid_mode" in kw:
+        p.resid_mode = kw["resid_mode"]
+    h = C.c_void_p()
+    assert _abi.lib().ptd_create(C.byref(h), C.byref(p)) == _abi.PTD_EINVAL
+    assert msg in _abi.last_error()
