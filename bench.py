@@ -500,20 +500,42 @@ def run_ours(args, world, rank, local, pg):
         if s.ndim == 3:
             alts["df64"] = alt_precision("df64")
 
-    # ---- time to tol: FP32 iterations + FP64 defect correction, same K steps from H0
+    # ---- time to tol of the two FP32 + FP64 forms, same K steps from H0:
+    # FP32_RB (FP32 PT iterations on the change since an FP64 base, rebased in
+    # FP64) and FP32_DC (FP32 inner solves in an FP64 inexact-Newton loop)
     ttt = None
     if args.precision == "fp64" and not args.no_dc:
-        pdc = ptdiff.make_params(s, shape, nt=1, precision="fp32_dc")
-        sdc = ptdiff.Solver(pdc)
-        t_dc, dc_iters, _, _ = timed_steps(sdc, args.steps)
-        H_dc = sdc.get_state()
-        sdc.close()
-        t_dc = reduce_max(pg, t_dc)
-        rel = float(np.linalg.norm(H_dc - H_fp64) / np.linalg.norm(H_fp64))
-        ttt = {"fp64_ms_per_step": round(t_max / args.steps * 1e3, 3),
-               "fp32_dc_ms_per_step": round(t_dc / args.steps * 1e3, 3),
-               "speedup": round(t_max / t_dc, 3), "rel_l2_fp32_dc_vs_fp64": rel,
-               "fp32_inner_iterations_per_step": dc_iters}
+        ttt = {"fp64_ms_per_step": round(t_max / args.steps * 1e3, 3)}
+        for form in ("fp32_rb", "fp32_dc"):
+            pf = ptdiff.make_params(s, shape, nt=1, precision=form)
+            sf = ptdiff.Solver(pf)
+            t_f, f_iters, _, _ = timed_steps(sf, args.steps)
+            H_f = sf.get_state()
+            kern_us = None
+            if form == "fp32_rb":   # the FP32 kernel alone, fixed iterations
+                ext_f = torch.cuda.ExternalStream(sf.stream)
+                sf.iterate(8)
+                sf.sync()
+                g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                g0.record(ext_f)
+                sf.iterate(nfix)
+                g1.record(ext_f)
+                g1.synchronize()
+                kern_us = round(g0.elapsed_time(g1) * 1e3 / nfix, 2)
+            sf.close()
+            t_f = reduce_max(pg, t_f)
+            rel = float(np.linalg.norm(H_f - H_fp64) / np.linalg.norm(H_fp64))
+            ttt[form] = {"ms_per_step": round(t_f / args.steps * 1e3, 3), "speedup": round(t_max / t_f, 3),
+                         "rel_l2_vs_fp64": rel,
+                         ("pt_iterations_per_step" if form == "fp32_rb" else "fp32_inner_iterations_per_step"):
+                             f_iters}
+            if kern_us is not None:
+                # bytes of one FP32 iteration: delta, omega_d, t_b_d, R_b, H read, delta and omega_d written
+                fb = (2 + 3 * s.ndim + 2) * 4 * float(np.prod(shape))
+                ttt[form].update({"kernel_us": kern_us, "kernel_gbs": round(fb / kern_us / 1e3, 1),
+                                  "kernel_frac": round(fb / kern_us / 1e3 / peak, 4),
+                                  "kernel_bytes_per_cell": (2 + 3 * s.ndim + 2) * 4})
+        ttt["speedup"] = ttt["fp32_rb"]["speedup"]
 
     # ---- e2e: ptd_solve on pinned host buffers, one physical step per call
     pe = ptdiff.make_params(s, shape, nt=1, precision=args.precision)
