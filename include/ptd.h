@@ -173,6 +173,11 @@ PTD_API int ptd_get_state(ptd_ctx* ctx, double* H);    /* H out */
 
 /* Launch shape in use: {warps per 2D CTA, rows per 2D y march, warps per 3D CTA, planes per 3D z march}. */
 PTD_API int ptd_launch_config(ptd_ctx* ctx, int32_t cfg[4]);
+/* Set it (e.g. a shape found by PTD_FLAG_AUTOTUNE on another context of the
+ * same size): warps per 2D CTA in {1,2,4,8}, rows per 2D march in [1,4096],
+ * warps per 3D CTA in {8,16} (the FP32 forms use 16), planes per 3D march in
+ * [1,4096].  The state is kept. */
+PTD_API int ptd_set_launch_config(ptd_ctx* ctx, const int32_t cfg[4]);
 
 /* The context's CUDA stream (cudaStream_t) and a device synchronize of it. */
 PTD_API void* ptd_stream(ptd_ctx* ctx);

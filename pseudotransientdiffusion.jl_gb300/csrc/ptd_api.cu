@@ -562,6 +562,39 @@ extern "C" int ptd_launch_config(ptd_ctx* c, int32_t cfg[4])
     return PTD_OK;
 }
 
+extern "C" int ptd_set_launch_config(ptd_ctx* c, const int32_t cfg[4])
+{
+    if (!c || !cfg) return fail(PTD_EINVAL, "ptd_set_launch_config: NULL argument");
+    if (cfg[0] != 1 && cfg[0] != 2 && cfg[0] != 4 && cfg[0] != 8)
+        return fail(PTD_EINVAL, "warps per 2D CTA must be 1, 2, 4 or 8 (got %d)", cfg[0]);
+    if (cfg[1] < 1 || cfg[1] > 4096) return fail(PTD_EINVAL, "rows per 2D march must be in [1, 4096]");
+    if (cfg[2] != 8 && cfg[2] != 16) return fail(PTD_EINVAL, "warps per 3D CTA must be 8 or 16 (got %d)", cfg[2]);
+    if (cfg[3] < 1 || cfg[3] > 4096) return fail(PTD_EINVAL, "planes per 3D march must be in [1, 4096]");
+    LaunchCfg k = c->cfg;
+    k.warps2d = cfg[0];
+    k.chunk2d = cfg[1];
+    k.rows3d = cfg[2];
+    k.chunk3d = cfg[3];
+    CK(cudaStreamSynchronize(c->stream));
+    c->cfg = k;
+    int rc = PTD_OK;
+    if (c->dc) {
+        rc = dc_set_config(c->dc, k);
+    } else if (c->rb) {
+        rc = rb_set_config(c->rb, k);
+    } else {
+        for (int q = 0; q < 2 && !rc; ++q) {
+            if (c->gblock[q]) cudaGraphExecDestroy(c->gblock[q]);
+            if (c->gplain[q]) cudaGraphExecDestroy(c->gplain[q]);
+            c->gblock[q] = nullptr;
+            c->gplain[q] = nullptr;
+            if (c->p.nchk <= c->p.itmax) rc = capture_block(c, q, &c->gblock[q]);
+            if (!rc) rc = capture_plain(c, q, &c->gplain[q]);
+        }
+    }
+    return rc;
+}
+
 extern "C" int ptd_sync(ptd_ctx* c)
 {
     if (!c) return fail(PTD_EINVAL, "ctx is NULL");

@@ -558,6 +558,18 @@ int dc_step(DcState* dc, const ptd_ctx_base& g, int32_t* iters, double* err_hist
     return PTD_OK;
 }
 
+int dc_set_config(DcState* dc, const LaunchCfg& cfg)
+{
+    dc->cfg = cfg;
+    for (int q = 0; q < 2; ++q) {
+        if (dc->gblock[q]) cudaGraphExecDestroy(dc->gblock[q]);
+        dc->gblock[q] = nullptr;
+        int rc = dc_capture(dc, q);
+        if (rc) return rc;
+    }
+    return PTD_OK;
+}
+
 int dc_iterate(DcState* dc, const ptd_ctx_base&, int32_t niter)
 {
     // fixed inner iterations (perf protocol): two per launch where the

@@ -52,6 +52,7 @@ int dc_set_state(DcState* dc, const ptd_ctx_base& g, double* H, double* Hold, co
 int dc_step(DcState* dc, const ptd_ctx_base& g, int32_t* iters, double* err_hist, int32_t err_cap,
             int32_t* n_err, int* nan_flag, int* capped);
 int dc_iterate(DcState* dc, const ptd_ctx_base& g, int32_t niter);
+int dc_set_config(DcState* dc, const LaunchCfg& cfg);
 const double* dc_current(const DcState* dc);
 
 struct DcCounters {
@@ -68,6 +69,7 @@ int rb_set_state(RbState* rb, double* H, double* Hold, double* const* wb, const 
 int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int32_t* n_err, int* nan_flag,
             int* capped);
 int rb_iterate(RbState* rb, int32_t niter);
+int rb_set_config(RbState* rb, const LaunchCfg& cfg);
 DcCounters rb_counters(const RbState* rb);
 
 }  // namespace ptd

@@ -875,6 +875,17 @@ int rb_iterate(RbState* rb, int32_t niter)
     return PTD_OK;
 }
 
+int rb_set_config(RbState* rb, const LaunchCfg& cfg)
+{
+    rb->cfg = cfg;
+    if (rb->gphase) {   // captured once the base fields are known (rb_set_state)
+        cudaGraphExecDestroy(rb->gphase);
+        rb->gphase = nullptr;
+        return rb_capture(rb);
+    }
+    return PTD_OK;
+}
+
 DcCounters rb_counters(const RbState* rb) { return rb ? rb->k : DcCounters{}; }
 
 }  // namespace ptd

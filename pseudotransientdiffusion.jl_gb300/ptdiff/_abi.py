@@ -81,6 +81,7 @@ def lib():
         "ptd_sync": (C.c_int, [vp]),
         "ptd_counters": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "ptd_launch_config": (C.c_int, [vp, C.POINTER(C.c_int32)]),
+        "ptd_set_launch_config": (C.c_int, [vp, C.POINTER(C.c_int32)]),
         "ptd_destroy": (None, [vp]),
         "ptd_strerror": (C.c_char_p, [C.c_int]),
         "ptd_last_error": (C.c_char_p, []),

@@ -179,6 +179,12 @@ class Solver:
         _abi.check(_abi.lib().ptd_launch_config(self._h, cfg), "ptd_launch_config")
         return {"warps2d": cfg[0], "chunk2d": cfg[1], "rows3d": cfg[2], "chunk3d": cfg[3]}
 
+    def set_launch_config(self, warps2d=None, chunk2d=None, rows3d=None, chunk3d=None):
+        cur = self.launch_config()
+        new = [warps2d or cur["warps2d"], chunk2d or cur["chunk2d"], rows3d or cur["rows3d"],
+               chunk3d or cur["chunk3d"]]
+        _abi.check(_abi.lib().ptd_set_launch_config(self._h, (C.c_int32 * 4)(*new)), "ptd_set_launch_config")
+
 
 @dataclass
 class Result:

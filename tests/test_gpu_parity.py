@@ -256,3 +256,31 @@ def test_run_script_writes_the_reference_outputs(tmp_path):
     row = (tmp_path / "output" / "out_diff_3D_nonlin_perf.txt").read_text().split()
     assert row[:5] == ["1", "32", "32", "32", str(perf.ittot)]
     assert float(row[6]) == 10 * 32 ** 3 * 8 / 1e9 and float(row[8]) > 0
+
+
+@pytest.mark.parametrize("prec", ["fp64", "dfh", "fp32_rb"])
+@pytest.mark.parametrize("name,shape,cfg", [
+    ("diff_2D_nonlin", (130, 97), {"warps2d": 1, "chunk2d": 1}), ("diff_2D_nonlin", (130, 97), {"warps2d": 8, "chunk2d": 200}),
+    ("diff_2D_linstep", (66, 33), {"warps2d": 2, "chunk2d": 7}),
+    ("diff_3D_nonlin_multixpu", (40, 36, 50), {"rows3d": 8, "chunk3d": 1}),
+    ("diff_3D_linstep_multixpu", (40, 36, 50), {"rows3d": 16, "chunk3d": 13})])
+def test_set_launch_config_keeps_the_solution(name, shape, cfg, prec):
+    s = S.SCRIPTS[name]
+    if prec == "fp32_rb" and cfg.get("rows3d") == 8:
+        cfg = dict(cfg, rows3d=16)
+    D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
+    H0 = S.initial_condition(s, *shape)
+    H = np.array(H0, order="F", copy=True)
+    with ptdiff.Solver(ptdiff.make_params(s, shape, precision=prec)) as sol:
+        sol.set_launch_config(**cfg)
+        got = sol.launch_config()
+        iters, _, st = sol.solve(H, D)
+    assert all(got[k] == v for k, v in cfg.items())
+    Hr, iters_r, _, _ = O.solve(s, H0, D)
+    assert st == 0
+    if prec == "fp32_rb":
+        rms = float(np.sqrt(np.mean(np.square(Hr))))
+        assert rel_l2(H, Hr) <= 2 * s.dt * s.tol / rms
+    else:
+        assert list(iters) == list(iters_r)
+        assert rel_l2(H, Hr) <= RTOL_FP64
