@@ -15,13 +15,15 @@ is what the tests exercise.
 """
 module PTDiffusion
 
-export PtdParams, diffusion_1D_, diffusion_2D_, diffusion_3D_, solve!
+export PtdParams, diffusion_1D_, diffusion_2D_, diffusion_3D_, diffusion_react_1D_, diffusion_react_2D_,
+       solve!, AdjointSolver, misfit
 
 const libptd = joinpath(@__DIR__, "..", "libptd.so")
 
 const PTD_OK = Cint(0)
 const MODEL = Dict(:lin => Int32(0), :linstep => Int32(1), :nonlin => Int32(2))
-const PRECISION = Dict(:fp64 => Int32(0), :fp32_dc => Int32(1))
+const PRECISION = Dict(:fp64 => Int32(0), :fp32_dc => Int32(1), :df64 => Int32(2), :dfh => Int32(3),
+                       :fp32_rb => Int32(4))
 
 # Mirror of `ptd_params` (include/ptd.h); field order and types must match.
 mutable struct PtdParams
@@ -78,6 +80,34 @@ function solve!(p::PtdParams, H::AbstractArray{Float64}; D=nothing, errcap::Inte
     return iters[1:p.nt], errs[1:min(nerr[], errcap)]
 end
 
+"""
+    solve_react!(p, H, Heq) -> iters
+
+The reaction scripts' single PT loop (scripts/diff_1D_react.jl:45-66,
+diff_2D_react.jl:55-72): H from zero towards Heq with theta_kin in place of
+dt, i.e. one implicit step of the linear solver with Hold = Heq
+(`ptd_set_state2`).
+"""
+function solve_react!(p::PtdParams, H::AbstractArray{Float64}, Heq::AbstractArray{Float64})
+    ctx = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:ptd_create, libptd), Cint, (Ref{Ptr{Cvoid}}, Ref{PtdParams}), ctx, p)
+    st == PTD_OK || error(ptd_error("ptd_create", st))
+    iters = zeros(Int32, 1)
+    try
+        st = ccall((:ptd_set_state2, libptd), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                   ctx[], pointer(H), pointer(Heq), C_NULL)
+        st == PTD_OK || error(ptd_error("ptd_set_state2", st))
+        st = ccall((:ptd_step, libptd), Cint, (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Int32, Ptr{Int32}),
+                   ctx[], Int32(1), iters, C_NULL, Int32(0), C_NULL)
+        st == PTD_OK || error(st == 2 ? "NaN" : ptd_error("ptd_step", st))
+        st = ccall((:ptd_get_state, libptd), Cint, (Ptr{Cvoid}, Ptr{Float64}), ctx[], pointer(H))
+        st == PTD_OK || error(ptd_error("ptd_get_state", st))
+    finally
+        ccall((:ptd_destroy, libptd), Cvoid, (Ptr{Cvoid},), ctx[])
+    end
+    return iters[1]
+end
+
 # Julia's LinRange cell centres, as in the scripts (e.g. scripts/diff_2D_nonlin.jl:63).
 cell_centres(l, n) = LinRange(l / n / 2, l - l / n / 2, n)
 
@@ -127,6 +157,90 @@ function diffusion_3D_(; model::Symbol=:nonlin, nx::Integer=parse(Int, get(ENV, 
     end
     iters, errs = solve!(p, H; D=D)
     return cell_centres(lx, nx), cell_centres(ly, ny), cell_centres(lz, nz), H, iters, errs
+end
+
+# Reaction-diffusion drivers (scripts/diff_1D_react.jl:31-47, diff_2D_react.jl:33-58):
+# D = 1, theta_kin = 0.1 (the dt of the equivalent implicit step), H0 = Heq a
+# Gaussian, H starting at zero.
+function diffusion_react_1D_(; nx::Integer=parse(Int, get(ENV, "NX", "512")), precision::Symbol=:fp64)
+    p = PtdParams(1, :lin); p.nx = nx; p.lx = 20.0; p.dt = 0.1; p.nt = 1; p.cfl = 0.99
+    p.precision = PRECISION[precision]
+    xc = cell_centres(p.lx, nx)
+    Heq = Array(exp.(-(xc .- p.lx / 2) .^ 2))
+    H = zeros(nx)
+    iters = solve_react!(p, H, Heq)
+    return xc, H, iters
+end
+
+function diffusion_react_2D_(; nx::Integer=parse(Int, get(ENV, "NX", "512")),
+                             ny::Integer=parse(Int, get(ENV, "NY", "512")), precision::Symbol=:fp64)
+    p = PtdParams(2, :lin); p.nx = nx; p.ny = ny; p.dt = 0.1; p.nt = 1
+    p.precision = PRECISION[precision]
+    xc, yc = cell_centres(p.lx, nx), cell_centres(p.ly, ny)
+    Heq = Array(exp.(-(xc .- p.lx / 2) .^ 2 .- ((yc .- p.ly / 2)') .^ 2))
+    H = zeros(nx, ny)
+    iters = solve_react!(p, H, Heq)
+    return xc, yc, H, iters
+end
+
+# ---------------------------------------------------------------------------
+# Adjoint (no reference counterpart): gradient of L = 1/2 sum_inner (H^nt - Ht)^2
+# with respect to the log-coefficient m (D = exp(m) H^3) and H0, through
+# ptd_adj_* (one FP64 checkpoint per physical step).
+
+mutable struct AdjointSolver
+    h::Ptr{Cvoid}
+    p::PtdParams
+end
+
+function AdjointSolver(p::PtdParams)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:ptd_adj_create, libptd), Cint, (Ref{Ptr{Cvoid}}, Ref{PtdParams}), h, p)
+    st == PTD_OK || error(ptd_error("ptd_adj_create", st))
+    a = AdjointSolver(h[], p)
+    finalizer(x -> ccall((:ptd_adj_destroy, libptd), Cvoid, (Ptr{Cvoid},), x.h), a)
+    return a
+end
+
+function forward!(a::AdjointSolver, H0, m, Ht)
+    loss = Ref{Float64}(0.0)
+    iters = zeros(Int32, max(a.p.nt, 1))
+    st = ccall((:ptd_adj_forward, libptd), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64}, Ptr{Int32}),
+               a.h, pointer(H0), pointer(m), pointer(Ht), loss, C_NULL, iters)
+    st == PTD_OK || error(ptd_error("ptd_adj_forward", st))
+    return loss[]
+end
+
+function gradient!(a::AdjointSolver)
+    gm, gh = similar(zeros(a.p.nx, a.p.ny, a.p.nz)), similar(zeros(a.p.nx, a.p.ny, a.p.nz))
+    iters = zeros(Int32, max(a.p.nt, 1))
+    st = ccall((:ptd_adj_gradient, libptd), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}),
+               a.h, pointer(gm), pointer(gh), iters)
+    st == PTD_OK || error(ptd_error("ptd_adj_gradient", st))
+    return gm, gh
+end
+
+"""
+    misfit(a, m, H0, Ht) -> L
+
+L2 misfit of the final state; differentiable through the ChainRulesCore
+`rrule` below (the Julia counterpart of ptdiff.misfit_function()).
+"""
+misfit(a::AdjointSolver, m, H0, Ht) = forward!(a, H0, m, Ht)
+
+# ChainRulesCore is a weak dependency: the rule is defined when it is loaded.
+if isdefined(Main, :ChainRulesCore)
+    import ChainRulesCore
+    function ChainRulesCore.rrule(::typeof(misfit), a::AdjointSolver, m, H0, Ht)
+        L = forward!(a, H0, m, Ht)
+        function misfit_pullback(dL)
+            gm, gh = gradient!(a)
+            return ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), dL .* gm, dL .* gh,
+                   ChainRulesCore.NoTangent()
+        end
+        return L, misfit_pullback
+    end
 end
 
 end # module
