@@ -89,8 +89,8 @@ enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL
  *           rebases (no restarted inner solves).  A step stops when the
  *           reference's check residual (every nchk, formed in FP32 from the
  *           FP64 base residual) and the FP64 residual of the rebased state
- *           are both <= tol; H is the FP64 base.  2D and 3D, models LIN,
- *           LINSTEP, NONLIN, mixed residual; single grids only. */
+ *           are both <= tol; H is the FP64 base.  Models LIN, LINSTEP,
+ *           NONLIN, mixed residual; single grids only. */
 enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH = 3, PTD_PREC_FP32_RB = 4 };
 
 /* Residual used for the stopping test.  MIXED is the reference's: the

@@ -111,6 +111,37 @@ __device__ __forceinline__ float rb_cell_e(const RbArgs& a, float h, float dmax)
 __device__ __forceinline__ bool rb_skip(const int* skip) { return __ldcg(skip) != 0; }
 
 // ---------------------------------------------------------------------------
+// 1D: one thread per cell; the left face is recomputed (1D grids are small).
+template <int MODEL, bool CHECK>
+__device__ __forceinline__ void rb1d_body(const RbArgs& a, int bx, double& part, unsigned long long& pmax)
+{
+    constexpr bool LS = MODEL == LINSTEP;
+    const int i = bx * blockDim.x + threadIdx.x;
+    const int nx = a.nx;
+    if (i >= nx) return;
+    const float dc = a.din[i], hc = a.Hf[i];
+    const float Dc = LS ? a.Df[i] : 0.0f;
+    float wr = 0.0f, ur = 0.0f, Dr = 0.0f;
+    if (i <= nx - 2) {
+        Dr = LS ? a.Df[i + 1] : 0.0f;
+        wr = rb_face<MODEL, CHECK>(a, dc, a.din[i + 1], hc, a.Hf[i + 1], Dc, Dr, a.win[0][i], a.tb[0][i], ur);
+        a.wout[0][i] = wr;
+    }
+    if (i >= 1 && i <= nx - 2) {
+        const float Dl = LS ? a.Df[i - 1] : 0.0f;
+        float ul = 0.0f;
+        const float wl = rb_face<MODEL, CHECK>(a, a.din[i - 1], dc, a.Hf[i - 1], hc, Dl, Dc, a.win[0][i - 1],
+                                               a.tb[0][i - 1], ul);
+        const float e = rb_cell_e<MODEL>(a, hc + dc, fmaxf(fmaxf(Dl, Dr), Dc));
+        const float dnew = fmaf(-e, fmaf(dc, a.rdt, a.Rb[i] + (wr - wl) * a.sig[0]), dc);
+        a.dout[i] = dnew;
+        if (CHECK)
+            accumulate_residual(a.Cb[i] + (double)((ur - ul) * a.sig[0]) - (double)dnew * (double)a.rdt, part,
+                                pmax);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // 2D: the tiling of ptd_pt_body.cuh (31 updated columns per warp, y march).
 template <int MODEL, bool CHECK>
 __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
@@ -290,6 +321,16 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
             p ^= 1;
         }
     }
+}
+
+template <int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) rb1d_kernel(RbArgs a)
+{
+    if (rb_skip(a.skip)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    rb1d_body<MODEL, CHECK>(a, blockIdx.x, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
 template <int MODEL, bool CHECK>
@@ -565,7 +606,9 @@ void rb_args(const RbState* rb, int parity, const int* skip, RbArgs& a)
 template <int MODEL, bool CHECK>
 cudaError_t rb_launch_model(const RbArgs& a, int ndim, const LaunchCfg& cfg, cudaStream_t s)
 {
-    if (ndim == 2) {
+    if (ndim == 1) {
+        rb1d_kernel<MODEL, CHECK><<<(a.nx + 255) / 256, 256, 0, s>>>(a);
+    } else if (ndim == 2) {
         const int W = cfg.warps2d;
         const int tiles = (a.nx - 2 + 30) / 31;
         dim3 grid((tiles + W - 1) / W, (a.ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);

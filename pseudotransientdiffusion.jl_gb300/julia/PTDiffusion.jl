@@ -213,7 +213,7 @@ function forward!(a::AdjointSolver, H0, m, Ht)
 end
 
 function gradient!(a::AdjointSolver)
-    gm, gh = similar(zeros(a.p.nx, a.p.ny, a.p.nz)), similar(zeros(a.p.nx, a.p.ny, a.p.nz))
+    gm, gh = zeros(a.p.nx, a.p.ny, a.p.nz), zeros(a.p.nx, a.p.ny, a.p.nz)
     iters = zeros(Int32, max(a.p.nt, 1))
     st = ccall((:ptd_adj_gradient, libptd), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}),
                a.h, pointer(gm), pointer(gh), iters)

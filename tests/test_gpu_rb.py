@@ -9,6 +9,7 @@ import pytest
 
 import ptdiff
 from oracle import oracle as O
+from golden_cases import start_fields
 from ptdiff import _abi
 from ptdiff import scripts as S
 
@@ -20,24 +21,28 @@ def rel_l2(a, b):
 
 
 def run(s, shape, H0=None, **kw):
-    H = S.initial_condition(s, *shape) if H0 is None else np.array(H0, order="F", copy=True)
+    H, Hold = start_fields(s, shape)
+    if H0 is not None:
+        H = np.array(H0, order="F", copy=True)
     D = S.step_field(s, *shape) if s.model == S.LINSTEP else None
     p = ptdiff.make_params(s, shape, precision="fp32_rb", **kw)
     with ptdiff.Solver(p) as sol:
-        iters, eh, st = sol.solve(H, D, raise_on_nan=False)
+        iters, eh, st = sol.solve(H, D, raise_on_nan=False, Hold=Hold)
     return H, D, iters, eh, st
 
 
 @pytest.mark.parametrize("name,shape", [
+    ("diff_1D_lin", (128,)), ("diff_1D_linstep", (200,)), ("diff_1D_nonlin", (97,)), ("diff_1D_react", (64,)),
     ("diff_2D_lin", (64, 64)), ("diff_2D_linstep", (66, 33)), ("diff_2D_nonlin", (64, 64)),
+    ("diff_2D_react", (64, 64)),
     ("diff_2D_nonlin", (3, 3)), ("diff_2D_nonlin", (37, 95)),
     ("diff_3D_lin_multixpu", (24, 24, 24)), ("diff_3D_linstep_multixpu", (3, 4, 5)),
     ("diff_3D_nonlin_multixpu", (32, 30, 34)), ("diff_3D_linstep_multixpu", (40, 36, 50))])
 def test_rebased_fp32_matches_oracle(name, shape):
     s = S.SCRIPTS[name]
     H, D, iters, eh, st = run(s, shape)
-    H0 = S.initial_condition(s, *shape)
-    Hr, it_r, _, st_r = O.solve(s, H0, D)
+    H0, Hold0 = start_fields(s, shape)
+    Hr, it_r, _, st_r = O.solve(s, H0, D, Hold0=Hold0)
     assert st == 0 and st_r == 0
     rms = float(np.sqrt(np.mean(np.square(Hr))))
     assert rel_l2(H, Hr) <= 2 * s.dt * s.tol / rms

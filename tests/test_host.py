@@ -181,15 +181,13 @@ def test_adjoint_create_rejects_unsupported_precisions():
         assert "FP64 or DF64" in _abi.last_error()
 
 
-@pytest.mark.parametrize("kw,msg", [({"ndim": 1}, "2D and 3D"), ({"resid_mode": 1}, "mixed residual")])
+@pytest.mark.parametrize("kw,msg", [({"model": 3}, "models LIN"), ({"resid_mode": 1}, "mixed residual")])
 def test_rebased_fp32_rejections(kw, msg):
     from ptdiff.solvers import make_params
 
-    s = S.SCRIPTS["diff_1D_lin" if kw.get("ndim") == 1 else "diff_2D_lin"]
-    shape = (32,) if s.ndim == 1 else (32, 32)
-    p = make_params(s, shape, precision="fp32_rb")
-    if "resid_mode" in kw:
-        p.resid_mode = kw["resid_mode"]
+    p = make_params(S.SCRIPTS["diff_2D_lin"], (32, 32), precision="fp32_rb")
+    for k, v in kw.items():
+        setattr(p, k, v)
     h = C.c_void_p()
     assert _abi.lib().ptd_create(C.byref(h), C.byref(p)) == _abi.PTD_EINVAL
     assert msg in _abi.last_error()
