@@ -284,3 +284,13 @@ def test_set_launch_config_keeps_the_solution(name, shape, cfg, prec):
     else:
         assert list(iters) == list(iters_r)
         assert rel_l2(H, Hr) <= RTOL_FP64
+
+
+@pytest.mark.parametrize("name,shape", [("diff_2D_nonlin", (96, 96)), ("diff_3D_nonlin_multixpu", (34, 34, 34))])
+def test_resc_search_never_worse_than_the_script(name, shape):
+    from ptdiff import dispersion as DP
+
+    s = S.SCRIPTS[name]
+    best, counts = DP.tune_resc(s, shape)
+    assert best in counts and s.resc in counts
+    assert counts[best] <= counts[s.resc]
