@@ -210,14 +210,18 @@ def run_reference(args, world, rank, pg):
     cb = None
     vals = []
     budget = max(4.0, 60.0 / max(args.steps, 1))
+    times = []
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         cb = cpu_baseline(s, shape, budget_s=budget)
+        times.append(time.perf_counter() - t0)
         vals.append(cb["value"])
     value = statistics.median(vals) if vals else 0.0
     cb["value"] = value
     line = {
         "impl": "reference", "metric": "T_eff", "value": value, "unit": "GB/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(statistics.median(times) * 1e3, 3) if times else None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload, "shape": list(shape), "protocol": "fixed PT iterations"},
         "cpu_baseline": cb,

@@ -109,3 +109,20 @@ def test_rebased_fp32_device_pointers_and_iterate():
     q = [np.zeros_like(H25) for _ in range(3)]
     O.iterate(s, H25, H0.copy(order="F"), q, 25)
     assert rel_l2(Hi, np.ravel(H25, order="F") if Hi.ndim == 1 else H25) <= 1e-5
+
+
+@pytest.mark.parametrize("name,shape,kw,okw", [
+    ("diff_2D_nonlin", (50, 61), {"norm": "max"}, {"norm": 1}),
+    ("diff_2D_linstep", (66, 33), {"nchk": 7}, {"nout": 7}),
+    ("diff_3D_nonlin_multixpu", (30, 31, 29), {"nchk": 3}, {"nout": 3}),
+    ("diff_2D_lin", (64, 64), {"nchk": 10, "itmax": 95}, {"nout": 10, "itmax": 95}),
+    ("diff_2D_nonlin", (64, 64), {"nchk": 1}, {"nout": 1})])
+def test_rebased_fp32_driver_options(name, shape, kw, okw):
+    s = S.SCRIPTS[name]
+    H, D, iters, eh, st = run(s, shape, **kw)
+    Hr, it_r, _, st_r = O.solve(s, S.initial_condition(s, *shape), D, **okw)
+    assert st == 0 and st_r == 0
+    rms = float(np.sqrt(np.mean(np.square(Hr))))
+    assert rel_l2(H, Hr) <= 2 * s.dt * s.tol / rms
+    nchk = kw.get("nchk", s.nout)
+    assert np.all(iters <= it_r + 6 * nchk + 20) and np.all(iters % nchk == 0), (list(iters), list(it_r))
