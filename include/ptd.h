@@ -61,8 +61,8 @@ typedef enum ptd_status {
 enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL_NONLIN_EXPM = 3 };
 /* PTD_MODEL_NONLIN_EXPM (no reference counterpart; the model of the adjoint
  * solver): D = exp(m) H^3 with a per-cell log-coefficient field m passed in
- * place of D; face value ((exp(m_L)+exp(m_R))/2) ((H_L+H_R)/2)^3.  FP64 and
- * DF64 only. */
+ * place of D; face value ((exp(m_L)+exp(m_R))/2) ((H_L+H_R)/2)^3.  FP64,
+ * DF64, DFH and FP32_RB. */
 
 /* Arithmetic of the PT iterations.
  *  FP64     every PT iteration in native FP64 (the reference's form).
@@ -89,8 +89,8 @@ enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL
  *           rebases (no restarted inner solves).  A step stops when the
  *           reference's check residual (every nchk, formed in FP32 from the
  *           FP64 base residual) and the FP64 residual of the rebased state
- *           are both <= tol; H is the FP64 base.  Models LIN, LINSTEP,
- *           NONLIN, mixed residual; single grids only. */
+ *           are both <= tol; H is the FP64 base.  Every model, mixed
+ *           residual; single grids only. */
 enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH = 3, PTD_PREC_FP32_RB = 4 };
 
 /* Residual used for the stopping test.  MIXED is the reference's: the

@@ -145,7 +145,6 @@ int ptd::validate(const ptd_params* p)
         p->precision != PTD_PREC_DFH && p->precision != PTD_PREC_FP32_RB)
         return fail(PTD_EINVAL, "unknown precision %d", p->precision);
     if (p->precision == PTD_PREC_FP32_RB) {
-        if (p->model > PTD_MODEL_NONLIN) return fail(PTD_EINVAL, "FP32_RB: models LIN, LINSTEP, NONLIN");
         if (p->resid_mode != PTD_RESID_MIXED) return fail(PTD_EINVAL, "FP32_RB: mixed residual only");
     }
     if (p->resid_mode != PTD_RESID_MIXED && p->resid_mode != PTD_RESID_CONSISTENT)

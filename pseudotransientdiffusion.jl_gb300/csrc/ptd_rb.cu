@@ -57,7 +57,7 @@ struct RbArgs {
     const float* Rb;      // base update residual
     const double* Cb;     // base check residual (FP64: read on check iterations only)
     const float* Hf;      // H_b as FP32 (iteration parameters, u_d)
-    const float* Df;      // LINSTEP: D as FP32
+    const float* Df;      // LINSTEP: D, NONLIN_EXPM: exp(m), as FP32
     const int* skip;
     double* acc;
     int norm_max;
@@ -90,11 +90,17 @@ __device__ __forceinline__ float rb_face(const RbArgs& a, float dL, float dR, fl
     } else if (MODEL == LINSTEP) {
         ud = (DL + DR) * gd;
         c = a.c_lin;
-    } else {
+    } else {   // NONLIN, NONLIN_EXPM (D holds exp(m): K = (E_L + E_R) s^3, kappa 1/16)
         const float sb = hL + hR, sd = dL + dR, gb = hR - hL;
         const float st = sb + sd;
         ud = fmaf(sd * fmaf(3.0f * sb, st, sd * sd), gb, st * st * st * gd);
-        c = nonlin_face_c(a.f, st);
+        if (MODEL == NONLIN_EXPM) {
+            const float e2 = DL + DR;
+            ud *= e2;
+            c = nonlin_face_c(a.f, st, 0.5f * e2);
+        } else {
+            c = nonlin_face_c(a.f, st);
+        }
     }
     if (U) u = ud;
     return fmaf(-c, w + (tb + ud), w);
@@ -105,6 +111,7 @@ __device__ __forceinline__ float rb_cell_e(const RbArgs& a, float h, float dmax)
 {
     if (MODEL == LIN) return a.e_lin;
     if (MODEL == LINSTEP) return linstep_cell_e(a.f, dmax);
+    if (MODEL == NONLIN_EXPM) return nonlin_cell_e(a.f, h, dmax);   // dmax carries exp(m) of the cell
     return nonlin_cell_e(a.f, h);
 }
 
@@ -116,23 +123,24 @@ template <int MODEL, bool CHECK>
 __device__ __forceinline__ void rb1d_body(const RbArgs& a, int bx, double& part, unsigned long long& pmax)
 {
     constexpr bool LS = MODEL == LINSTEP;
+    constexpr bool HASD = LS || MODEL == NONLIN_EXPM;   // a per-cell field in Df
     const int i = bx * blockDim.x + threadIdx.x;
     const int nx = a.nx;
     if (i >= nx) return;
     const float dc = a.din[i], hc = a.Hf[i];
-    const float Dc = LS ? a.Df[i] : 0.0f;
+    const float Dc = HASD ? a.Df[i] : 0.0f;
     float wr = 0.0f, ur = 0.0f, Dr = 0.0f;
     if (i <= nx - 2) {
-        Dr = LS ? a.Df[i + 1] : 0.0f;
+        Dr = HASD ? a.Df[i + 1] : 0.0f;
         wr = rb_face<MODEL, CHECK>(a, dc, a.din[i + 1], hc, a.Hf[i + 1], Dc, Dr, a.win[0][i], a.tb[0][i], ur);
         a.wout[0][i] = wr;
     }
     if (i >= 1 && i <= nx - 2) {
-        const float Dl = LS ? a.Df[i - 1] : 0.0f;
+        const float Dl = HASD ? a.Df[i - 1] : 0.0f;
         float ul = 0.0f;
         const float wl = rb_face<MODEL, CHECK>(a, a.din[i - 1], dc, a.Hf[i - 1], hc, Dl, Dc, a.win[0][i - 1],
                                                a.tb[0][i - 1], ul);
-        const float e = rb_cell_e<MODEL>(a, hc + dc, fmaxf(fmaxf(Dl, Dr), Dc));
+        const float e = rb_cell_e<MODEL>(a, hc + dc, LS ? fmaxf(fmaxf(Dl, Dr), Dc) : Dc);
         const float dnew = fmaf(-e, fmaf(dc, a.rdt, a.Rb[i] + (wr - wl) * a.sig[0]), dc);
         a.dout[i] = dnew;
         if (CHECK)
@@ -148,6 +156,7 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
                                           unsigned long long& pmax)
 {
     constexpr bool LS = MODEL == LINSTEP;
+    constexpr bool HASD = LS || MODEL == NONLIN_EXPM;   // a per-cell field in Df
     const int lane = threadIdx.x;
     const int i = 31 * tile + lane;
     const int nx = a.nx, ny = a.ny;
@@ -161,10 +170,10 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
         const long long sy = a.sy;
         long long idx = (long long)j0 * sy + ic;
         float dc = a.din[idx], hc = a.Hf[idx];
-        float Dc = LS ? a.Df[idx] : 0.0f, Db = 0.0f;
+        float Dc = HASD ? a.Df[idx] : 0.0f, Db = 0.0f;
         float wyb = 0.0f, uyb = 0.0f;
         if (upd) {
-            Db = LS ? a.Df[idx - sy] : 0.0f;
+            Db = HASD ? a.Df[idx - sy] : 0.0f;
             wyb = rb_face<MODEL, CHECK>(a, a.din[idx - sy], dc, a.Hf[idx - sy], hc, Db, Dc, a.win[1][idx - sy],
                                         a.tb[1][idx - sy], uyb);
             if (j0 == 1) a.wout[1][idx - sy] = wyb;
@@ -173,26 +182,26 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
             const float dn = a.din[idx + sy], hn = a.Hf[idx + sy];
             const float wx = a.win[0][idx], wy = a.win[1][idx];
             const float tbx = a.tb[0][idx], tby = a.tb[1][idx], rb = a.Rb[idx];
-            const float Dn = LS ? a.Df[idx + sy] : 0.0f;
+            const float Dn = HASD ? a.Df[idx + sy] : 0.0f;
             float dr = __shfl_down_sync(FULL, dc, 1);
             float hr = __shfl_down_sync(FULL, hc, 1);
-            float Dr = LS ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
+            float Dr = HASD ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
             if (lane == 31) {
                 const bool ok = ic + 1 < nx;
                 dr = ok ? a.din[idx + 1] : dc;
                 hr = ok ? a.Hf[idx + 1] : hc;
-                if (LS) Dr = ok ? a.Df[idx + 1] : Dc;
+                if (HASD) Dr = ok ? a.Df[idx + 1] : Dc;
             }
             float ux = 0.0f, uy = 0.0f, wxn = 0.0f, wyn = 0.0f;
             if (xface) wxn = rb_face<MODEL, CHECK>(a, dc, dr, hc, hr, Dc, Dr, wx, tbx, ux);
             if (upd) wyn = rb_face<MODEL, CHECK>(a, dc, dn, hc, hn, Dc, Dn, wy, tby, uy);
             const float wxl = __shfl_up_sync(FULL, wxn, 1);
             const float uxl = CHECK ? __shfl_up_sync(FULL, ux, 1) : 0.0f;
-            const float Dl = LS ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
+            const float Dl = HASD ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
             if (own_x) a.wout[0][idx] = wxn;
             if (upd) {
                 a.wout[1][idx] = wyn;
-                const float e = rb_cell_e<MODEL>(a, hc + dc, fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Db)), Dn));
+                const float e = rb_cell_e<MODEL>(a, hc + dc, LS ? fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Db)), Dn) : Dc);
                 const float div = fmaf(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]);
                 const float dnew = fmaf(-e, fmaf(dc, a.rdt, rb + div), dc);
                 a.dout[idx] = dnew;
@@ -205,7 +214,7 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
             hc = hn;
             wyb = wyn;
             uyb = uy;
-            if (LS) {
+            if (HASD) {
                 Db = Dc;
                 Dc = Dn;
             }
@@ -220,11 +229,12 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
                                           unsigned long long& pmax)
 {
     constexpr bool LS = MODEL == LINSTEP;
+    constexpr bool HASD = LS || MODEL == NONLIN_EXPM;   // a per-cell field in Df
     __shared__ float sd[2][R][32];
     __shared__ float sh[2][R][32];
     __shared__ float sw[2][R][32];
     __shared__ float su[CHECK ? 2 : 1][CHECK ? R : 1][32];
-    __shared__ float sD[LS ? 2 : 1][LS ? R : 1][32];
+    __shared__ float sD[HASD ? 2 : 1][HASD ? R : 1][32];
     const int lane = threadIdx.x, r = threadIdx.y;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int i = 31 * bx + lane;
@@ -243,10 +253,10 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
         const long long sy = a.sy, sz = a.sz;
         long long idx = (long long)k0 * sz + (long long)jc * sy + ic;
         float dc = a.din[idx], hc = a.Hf[idx];
-        float Dc = LS ? a.Df[idx] : 0.0f, Db = 0.0f;
+        float Dc = HASD ? a.Df[idx] : 0.0f, Db = 0.0f;
         float wzb = 0.0f, uzb = 0.0f;
         if (upd) {
-            Db = LS ? a.Df[idx - sz] : 0.0f;
+            Db = HASD ? a.Df[idx - sz] : 0.0f;
             wzb = rb_face<MODEL, CHECK>(a, a.din[idx - sz], dc, a.Hf[idx - sz], hc, Db, Dc, a.win[2][idx - sz],
                                         a.tb[2][idx - sz], uzb);
             if (k0 == 1) a.wout[2][idx - sz] = wzb;
@@ -254,32 +264,32 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
         int p = 0;
         sd[0][r][lane] = dc;
         sh[0][r][lane] = hc;
-        if (LS) sD[0][r][lane] = Dc;
+        if (HASD) sD[0][r][lane] = Dc;
         __syncthreads();
         for (int k = k0; k < k1; ++k, idx += sz) {
             const float dn = a.din[idx + sz], hn = a.Hf[idx + sz];
             const float wx = a.win[0][idx], wy = a.win[1][idx], wz = a.win[2][idx];
             const float tbx = a.tb[0][idx], tby = a.tb[1][idx], tbz = a.tb[2][idx], rb = a.Rb[idx];
-            const float Dn = LS ? a.Df[idx + sz] : 0.0f;
+            const float Dn = HASD ? a.Df[idx + sz] : 0.0f;
             float du, hu, Du = 0.0f;
             if (!top) {
                 du = sd[p][r + 1][lane];
                 hu = sh[p][r + 1][lane];
-                if (LS) Du = sD[p][r + 1][lane];
+                if (HASD) Du = sD[p][r + 1][lane];
             } else {
                 du = up_ok ? a.din[idx + sy] : dc;
                 hu = up_ok ? a.Hf[idx + sy] : hc;
-                if (LS) Du = up_ok ? a.Df[idx + sy] : Dc;
+                if (HASD) Du = up_ok ? a.Df[idx + sy] : Dc;
             }
             const float Dd = (LS && r >= 1) ? sD[p][r - 1][lane] : 0.0f;
             float dr = __shfl_down_sync(FULL, dc, 1);
             float hr = __shfl_down_sync(FULL, hc, 1);
-            float Dr = LS ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
+            float Dr = HASD ? __shfl_down_sync(FULL, Dc, 1) : 0.0f;
             if (lane == 31) {
                 const bool ok = ic + 1 < nx;
                 dr = ok ? a.din[idx + 1] : dc;
                 hr = ok ? a.Hf[idx + 1] : hc;
-                if (LS) Dr = ok ? a.Df[idx + 1] : Dc;
+                if (HASD) Dr = ok ? a.Df[idx + 1] : Dc;
             }
             float ux = 0.0f, uy = 0.0f, uz = 0.0f, wxn = 0.0f, wyn = 0.0f, wzn = 0.0f;
             if (xface) wxn = rb_face<MODEL, CHECK>(a, dc, dr, hc, hr, Dc, Dr, wx, tbx, ux);
@@ -290,17 +300,17 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
             if (upd) a.wout[2][idx] = wzn;
             const float wxl = __shfl_up_sync(FULL, wxn, 1);
             const float uxl = CHECK ? __shfl_up_sync(FULL, ux, 1) : 0.0f;
-            const float Dl = LS ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
+            const float Dl = HASD ? __shfl_up_sync(FULL, Dc, 1) : 0.0f;
             sw[p][r][lane] = wyn;
             if (CHECK) su[p][r][lane] = uy;
             sd[p ^ 1][r][lane] = dn;
             sh[p ^ 1][r][lane] = hn;
-            if (LS) sD[p ^ 1][r][lane] = Dn;
+            if (HASD) sD[p ^ 1][r][lane] = Dn;
             __syncthreads();
             if (upd) {
                 const float wyb = sw[p][r - 1][lane];
                 const float e = rb_cell_e<MODEL>(
-                    a, hc + dc, fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Du)), fmaxf(fmaxf(Dd, Db), Dn)));
+                    a, hc + dc, LS ? fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Du)), fmaxf(fmaxf(Dd, Db), Dn)) : Dc);
                 const float div = fmaf(wzn - wzb, a.sig[2], fmaf(wyn - wyb, a.sig[1], (wxn - wxl) * a.sig[0]));
                 const float dnew = fmaf(-e, fmaf(dc, a.rdt, rb + div), dc);
                 a.dout[idx] = dnew;
@@ -314,7 +324,7 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
             hc = hn;
             wzb = wzn;
             uzb = uz;
-            if (LS) {
+            if (HASD) {
                 Db = Dc;
                 Dc = Dn;
             }
@@ -416,6 +426,7 @@ __device__ __forceinline__ double rb_u64(const RbBaseArgs& b, long long cL, long
     if (b.model == LIN) return g;
     if (b.model == LINSTEP) return (b.D[cL] + b.D[cR]) * g;
     const double s = b.H[cL] + b.H[cR];
+    if (b.model == NONLIN_EXPM) return (b.D[cL] + b.D[cR]) * (s * s * s) * g;
     return s * s * s * g;
 }
 
@@ -630,6 +641,8 @@ cudaError_t rb_launch(const RbArgs& a, int ndim, int model, bool check, const La
     case 3: return rb_launch_model<LINSTEP, true>(a, ndim, cfg, s);
     case 4: return rb_launch_model<NONLIN, false>(a, ndim, cfg, s);
     case 5: return rb_launch_model<NONLIN, true>(a, ndim, cfg, s);
+    case 6: return rb_launch_model<NONLIN_EXPM, false>(a, ndim, cfg, s);
+    case 7: return rb_launch_model<NONLIN_EXPM, true>(a, ndim, cfg, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -763,7 +776,7 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     if (!rc) rc = alloc((void**)&rb->Rb, fb);
     if (!rc) rc = alloc((void**)&rb->Cb, (size_t)g.nfield * sizeof(double));
     if (!rc) rc = alloc((void**)&rb->Hf, fb);
-    if (!rc && p.model == PTD_MODEL_LINSTEP) rc = alloc((void**)&rb->Df, fb);
+    if (!rc && (p.model == PTD_MODEL_LINSTEP || p.model == PTD_MODEL_NONLIN_EXPM)) rc = alloc((void**)&rb->Df, fb);
     if (!rc) rc = alloc((void**)&rb->dev, sizeof(RbDev));
     if (!rc) rc = alloc((void**)&rb->zero_flag, sizeof(int));
     if (!rc) rc = alloc((void**)&rb->errhist, (size_t)rb->errcap * sizeof(double));

@@ -126,3 +126,22 @@ def test_rebased_fp32_driver_options(name, shape, kw, okw):
     assert rel_l2(H, Hr) <= 2 * s.dt * s.tol / rms
     nchk = kw.get("nchk", s.nout)
     assert np.all(iters <= it_r + 6 * nchk + 20) and np.all(iters % nchk == 0), (list(iters), list(it_r))
+
+
+@pytest.mark.parametrize("shape", [(40, 44), (24, 26, 22)])
+def test_rebased_fp32_expm_model_matches_fp64(shape):
+    """D = exp(m) H^3 (the adjoint's model) with a seeded log-coefficient field."""
+    base = S.SCRIPTS["diff_2D_nonlin" if len(shape) == 2 else "diff_3D_nonlin_multixpu"]
+    s = base.with_(name="expm", model=S.NONLIN_EXPM, shift=1.0, dirichlet=1.0, ic="linrange", ttot=0.4)
+    m = np.asfortranarray(S.log_coefficient_field(shape, lengths=(10.0,) * len(shape), seed=3))
+    out = {}
+    for prec in ("fp64", "fp32_rb"):
+        H = S.initial_condition(s, *shape)
+        with ptdiff.Solver(ptdiff.make_params(s, shape, precision=prec)) as sol:
+            iters, _, st = sol.solve(H, m)
+        assert st == 0
+        out[prec] = (H, iters)
+    (H64, it64), (H32, it32) = out["fp64"], out["fp32_rb"]
+    rms = float(np.sqrt(np.mean(np.square(H64))))
+    assert rel_l2(H32, H64) <= 2 * s.dt * s.tol / rms
+    assert np.all(np.abs(it32.astype(int) - it64.astype(int)) <= 3 * s.nout)

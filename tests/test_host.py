@@ -181,7 +181,7 @@ def test_adjoint_create_rejects_unsupported_precisions():
         assert "FP64 or DF64" in _abi.last_error()
 
 
-@pytest.mark.parametrize("kw,msg", [({"model": 3}, "models LIN"), ({"resid_mode": 1}, "mixed residual")])
+@pytest.mark.parametrize("kw,msg", [({"resid_mode": 1}, "mixed residual")])
 def test_rebased_fp32_rejections(kw, msg):
     from ptdiff.solvers import make_params
 
