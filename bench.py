@@ -308,20 +308,21 @@ def run_adjoint(args, world, rank, local, pg):
     dev = lambda a: torch.from_numpy(np.ravel(a, order="F").copy()).cuda()
     out = {}
     Ht = None
-    for prec in ("df64", "fp64"):
+    head = "fp32_rb"   # the headline form: FP32 iterations on the change since an FP64 base
+    for prec in (head, "df64", "fp64"):
         A = ptdiff.AdjointSolver(ptdiff.make_params(s, shape, precision=prec, nchk=10))
         if Ht is None:
             _, Ht = A.forward(H0, mt, H0, want_HN=True)
         H0d, md, Htd = dev(H0), dev(m), dev(Ht)
         gmd, ghd = torch.empty_like(H0d), torch.empty_like(H0d)
-        for _ in range(args.warmup if prec == "df64" else 1):
+        for _ in range(args.warmup if prec == head else 1):
             A.forward(H0d, md, Htd)
             A.gradient(out_m=gmd, out_H0=ghd)
         torch.cuda.synchronize()
         barrier(pg)
         l0, i0 = A.counters()
         t_fwd = t_adj = 0.0
-        nsteps = args.steps if prec == "df64" else 1
+        nsteps = args.steps if prec == head else 1
         fwd_iters = adj_iters = 0
         for _ in range(nsteps):
             t0 = time.perf_counter()
@@ -346,7 +347,7 @@ def run_adjoint(args, world, rank, local, pg):
                "gpu_launches": int(l1 - l0), "loss": loss,
                "adjoint_final_rel_residual": [float(e / t * 1e-10) if t > 0 else 0.0
                                               for e, t in zip(res_err, res_target)]}
-        if prec == "df64":
+        if prec == head:
             # e2e: host arrays in and out, the library copies them
             gm_h, gh_h = None, None
             t0 = time.perf_counter()
@@ -377,12 +378,12 @@ def run_adjoint(args, world, rank, local, pg):
         A.close()
     if rank != 0:
         return 0
-    d = out["df64"]
+    d = out[head]
     print(json.dumps({
         "metric": "adjoint gradient evaluations per second", "value": d["grads_per_s"], "unit": "gradients/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["ms_per_gradient"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "df64 (f32x2)", "data": "synthetic",
+        "dtype": "f32 changes on an f64 base (rebased)", "data": "synthetic",
         "config": {"workload": "adjoint_3d_256", "shape": list(shape), "nt": 10, "dt": 0.1, "tol": s.tol,
                    "model": "D = exp(m) H^3", "m": "Gaussian random field, corr 1, std 0.3, seed 0",
                    "target": "H^10 of m + a second such field (seed 1)", "checkpoints": "one per step",
@@ -392,7 +393,7 @@ def run_adjoint(args, world, rank, local, pg):
         "gpu_launches": d["gpu_launches"],
         "adjoint_over_forward": d["adjoint_over_forward"],
         "fd_check": d["fd_check"],
-        "df64": d, "fp64": out["fp64"]}), flush=True)
+        "fp32_rb": d, "df64": out["df64"], "fp64": out["fp64"]}), flush=True)
     return 0
 
 

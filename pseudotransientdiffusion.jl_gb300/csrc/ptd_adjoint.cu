@@ -47,10 +47,32 @@ struct AdjArgs {
     void* wout[3];
     const void* H;      // H^n (frozen, number type of the kernel)
     const void* E;      // exp(m) (number type of the kernel); NULL for D = H^3
-    const void* g;      // right-hand side
+    const void* g;      // right-hand side (rebased form: minus the base update residual)
     const int* done;
     double* acc;
+    // rebased FP32 form (precision FP32_RB): the adjoint PT iteration on the
+    // change since an FP64 base (lam_b, w_b), see ptd_rb.cu for the scheme
+    float rdtf;
+    float sigf[3];
+    const void* tb[3];  // base flux defect w_b + K v_b per face (FP32)
+    const double* Cb;   // base check residual (FP64)
 };
+
+// FP32 number type of the rebased adjoint iteration (ptd_num.cuh interface).
+struct F32 {
+    using T = float;
+    static constexpr bool native = true;
+    __device__ static __forceinline__ T add(T a, T b) { return a + b; }
+    __device__ static __forceinline__ T sub(T a, T b) { return a - b; }
+    __device__ static __forceinline__ T mul(T a, T b) { return a * b; }
+    __device__ static __forceinline__ T mad(T a, T b, T c) { return fmaf(a, b, c); }
+    __device__ static __forceinline__ float lo_f(T a) { return a; }
+    __device__ static __forceinline__ double to_d(T a) { return (double)a; }
+    __device__ static __forceinline__ T zero() { return 0.0f; }
+    __device__ static __forceinline__ T shfl_down(T v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
+    __device__ static __forceinline__ T shfl_up(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+};
+__device__ __forceinline__ float nmadf(F32, float c, float t, float w) { return fmaf(-c, t, w); }
 
 // done: 1 converged (err <= target), 2 itmax, 3 stalled at an arithmetic
 // floor below the acceptable level (err <= accept, no 1 % improvement over
@@ -72,14 +94,20 @@ __device__ __forceinline__ float2 acst<DF64>(const AdjArgs& a, int which)
 {
     return which < 3 ? a.sig_df[which] : a.rdt_df;
 }
+template <>
+__device__ __forceinline__ float acst<F32>(const AdjArgs& a, int which)
+{
+    return which < 3 ? a.sigf[which] : a.rdtf;
+}
 
 // One adjoint face: damped symmetric flux, and the Newton-transpose value n.
-// kv = K v (undamped, for the check).
-template <class N, bool EXPM, bool U>
+// kv = K v (undamped, for the check).  DELTA: the rebased form, whose flux
+// relaxes towards -(t_b + K v) (t_b: the base flux defect).
+template <class N, bool EXPM, bool U, bool DELTA = false>
 __device__ __forceinline__ typename N::T adj_face(const AdjArgs& a, typename N::T HL, typename N::T HR, float hsum,
                                                   typename N::T EL, typename N::T ER, typename N::T lL,
                                                   typename N::T lR, typename N::T w, typename N::T& n,
-                                                  typename N::T& kv)
+                                                  typename N::T& kv, typename N::T tb = typename N::T())
 {
     using T = typename N::T;
     const T v = N::sub(lR, lL);
@@ -102,10 +130,11 @@ __device__ __forceinline__ typename N::T adj_face(const AdjArgs& a, typename N::
     const T kvv = N::mul(K, v);
     if (U) kv = kvv;
     const float c = nonlin_face_c(a.f, hsum, efac);
+    if (DELTA) return nmadf(N(), c, N::add(N::add(w, tb), kvv), w);
     return nmadf(N(), c, N::add(w, kvv), w);
 }
 
-template <class N, bool EXPM, bool CHECK, int R>
+template <class N, bool EXPM, bool CHECK, int R, bool DELTA = false>
 __global__ void __launch_bounds__(32 * R) adj3d_kernel(const AdjArgs* __restrict__ ap, int chunk)
 {
     using T = typename N::T;
@@ -144,8 +173,9 @@ __global__ void __launch_bounds__(32 * R) adj3d_kernel(const AdjArgs* __restrict
         if (upd) {
             const T lb = ld<N>(a.lin, idx - sz), Hb = ld<N>(a.H, idx - sz);
             const T Eb = EXPM ? ld<N>(a.E, idx - sz) : N::zero();
-            wzb = adj_face<N, EXPM, CHECK>(a, Hb, Hc, N::lo_f(Hb) + hc, Eb, Ec, lb, lc, ld<N>(a.win[2], idx - sz),
-                                           nzb, kzb);
+            wzb = adj_face<N, EXPM, CHECK, DELTA>(a, Hb, Hc, N::lo_f(Hb) + hc, Eb, Ec, lb, lc,
+                                                  ld<N>(a.win[2], idx - sz), nzb, kzb,
+                                                  DELTA ? ld<N>(a.tb[2], idx - sz) : N::zero());
             if (k0 == 1) st<N>(a.wout[2], idx - sz, wzb);
         }
         int p = 0;
@@ -158,6 +188,9 @@ __global__ void __launch_bounds__(32 * R) adj3d_kernel(const AdjArgs* __restrict
             const T En = EXPM ? ld<N>(a.E, idx + sz) : N::zero();
             const T wx = ld<N>(a.win[0], idx), wy = ld<N>(a.win[1], idx), wz = ld<N>(a.win[2], idx);
             const T gg = ld<N>(a.g, idx);
+            const T tbx = DELTA ? ld<N>(a.tb[0], idx) : N::zero();
+            const T tby = DELTA ? ld<N>(a.tb[1], idx) : N::zero();
+            const T tbz = DELTA ? ld<N>(a.tb[2], idx) : N::zero();
             T lu, Hu, Eu = N::zero();
             if (!top) {
                 lu = sL[p][r + 1][lane];
@@ -179,9 +212,12 @@ __global__ void __launch_bounds__(32 * R) adj3d_kernel(const AdjArgs* __restrict
             T nx_ = N::zero(), ny_ = N::zero(), nz_ = N::zero();
             T kx = N::zero(), ky = N::zero(), kz = N::zero();
             T wxn = N::zero(), wyn = N::zero(), wzn = N::zero();
-            if (xface) wxn = adj_face<N, EXPM, CHECK>(a, Hc, Hr, hc + N::lo_f(Hr), Ec, Er, lc, lr, wx, nx_, kx);
-            if (yface) wyn = adj_face<N, EXPM, CHECK>(a, Hc, Hu, hc + N::lo_f(Hu), Ec, Eu, lc, lu, wy, ny_, ky);
-            if (upd) wzn = adj_face<N, EXPM, CHECK>(a, Hc, Hn, hc + N::lo_f(Hn), Ec, En, lc, ln, wz, nz_, kz);
+            if (xface)
+                wxn = adj_face<N, EXPM, CHECK, DELTA>(a, Hc, Hr, hc + N::lo_f(Hr), Ec, Er, lc, lr, wx, nx_, kx, tbx);
+            if (yface)
+                wyn = adj_face<N, EXPM, CHECK, DELTA>(a, Hc, Hu, hc + N::lo_f(Hu), Ec, Eu, lc, lu, wy, ny_, ky, tby);
+            if (upd)
+                wzn = adj_face<N, EXPM, CHECK, DELTA>(a, Hc, Hn, hc + N::lo_f(Hn), Ec, En, lc, ln, wz, nz_, kz, tbz);
             if (own_x) st<N>(a.wout[0], idx, wxn);
             if (own_y) st<N>(a.wout[1], idx, wyn);
             if (upd) st<N>(a.wout[2], idx, wzn);
@@ -210,8 +246,12 @@ __global__ void __launch_bounds__(32 * R) adj3d_kernel(const AdjArgs* __restrict
                     T q = N::mul(N::sub(N::sub(kx, kxl), N::add(nx_, nxl)), acst<N>(a, 0));
                     q = N::mad(N::sub(N::sub(ky, kyb), N::add(ny_, nyb)), acst<N>(a, 1), q);
                     q = N::mad(N::sub(N::sub(kz, kzb), N::add(nz_, nzb)), acst<N>(a, 2), q);
-                    const T res = N::add(N::sub(gg, N::mul(lnew, acst<N>(a, 3))), q);
-                    accumulate_residual(N::to_d(res), part, pmax);
+                    if (DELTA) {   // C_b + (the same terms of the changes)
+                        accumulate_residual(a.Cb[idx] + N::to_d(q) - N::to_d(lnew) * a.rdt, part, pmax);
+                    } else {
+                        const T res = N::add(N::sub(gg, N::mul(lnew, acst<N>(a, 3))), q);
+                        accumulate_residual(N::to_d(res), part, pmax);
+                    }
                 }
             }
             lc = ln;
@@ -344,6 +384,195 @@ __global__ void __launch_bounds__(256) adj_sumsq_kernel(const void* v, double* a
     block_reduce_residual(acc, 0, part, pm);
 }
 
+// ---------------------------------------------------------------------------
+// Rebased FP32 adjoint (precision FP32_RB).  The adjoint system of a step is
+// linear in lam, so the PT iteration runs in FP32 on the change since an FP64
+// base (lam_b, w_b) exactly like the forward's rebased form (ptd_rb.cu): the
+// FP32 flux relaxes towards -(t_b + K v) with the base flux defect
+// t_b = w_b + K v_b, and the update uses the base residual
+// R_b = lam_b/dt + div_b - g (passed as g = -R_b).  The base is rebased in
+// FP64 when a phase has cut its residual 1e4-fold, when the FP32 check (from
+// the FP64 base check residual C_b and the changes) reaches the target, or
+// when it stalls below the acceptable level; the FP64 residual of the rebased
+// base confirms the stop.
+struct AdjRbState {
+    int skip, done, iter, phase_iter, nchecks, capped, stalled, best_at;
+    double acc, acc64, err, err64, target, accept, best;
+};
+
+__global__ void adj_tofloat_kernel(const double* src, float* dst, long long n)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x)
+        dst[t] = __double2float_rn(src[t]);
+}
+
+struct AdjFold {
+    long long n;
+    double* lamb;
+    double* wb[3];
+    float* d[2];
+    float* w[3][2];
+};
+
+// lam_b += delta, w_b += omega; clear the parity-0 buffers the next phase reads
+__global__ void adj_rb_fold_kernel(AdjFold f, const AdjRbState* st)
+{
+    if (st->done) return;
+    const int par = st->phase_iter & 1;
+    const float* dp = par ? f.d[1] : f.d[0];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < f.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        f.lamb[t] += (double)dp[t];
+        f.d[0][t] = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float* wp = par ? f.w[d][1] : f.w[d][0];
+            f.wb[d][t] += (double)wp[t];
+            f.w[d][0][t] = 0.0f;
+        }
+    }
+}
+
+struct AdjBase {
+    int nx, ny, nz;
+    long long sy, sz;
+    double rdt;
+    double sig[3];
+    const double* H;     // H^n (FP64)
+    const double* E;     // exp(m) (FP64); NULL for D = H^3
+    const double* lamb;
+    const double* wb[3];
+    const double* g;     // right-hand side (FP64)
+    float* tb[3];
+    float* rbf;          // -R_b
+    double* Cb;
+    double* acc64;
+};
+
+// FP64 base quantities (one thread per cell): t_b for the +d faces, and for
+// inner cells -R_b, C_b = g - lam_b/dt + sum sigma [(Kv_+ - Kv_-) - (n_+ + n_-)]
+// and |C_b|^2.
+template <bool EXPM>
+__global__ void __launch_bounds__(256) adj_rb_base_kernel(AdjBase b, const AdjRbState* st)
+{
+    if (st->done) return;
+    const long long total = (long long)b.nx * b.ny * b.nz;
+    const long long stp[3] = {1, b.sy, b.sz};
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int co[3] = {(int)(t % b.nx), (int)((t / b.nx) % b.ny), (int)(t / ((long long)b.nx * b.ny))};
+        const int nn[3] = {b.nx, b.ny, b.nz};
+        const long long c = co[2] * b.sz + co[1] * b.sy + co[0];
+        bool in[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) in[d] = co[d] >= 1 && co[d] <= nn[d] - 2;
+        const bool inner = in[0] && in[1] && in[2];
+        auto face = [&](long long cL, long long cR, double& kv, double& n) {
+            const double HL = b.H[cL], HR = b.H[cR];
+            const double sm = HL + HR;
+            const double e2 = EXPM ? b.E[cL] + b.E[cR] : 2.0;
+            const double v = b.lamb[cR] - b.lamb[cL];
+            kv = e2 * sm * sm * sm * v;
+            n = 3.0 * e2 * sm * sm * (HR - HL) * v;
+        };
+        double div = 0.0, q = 0.0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const bool others = (d == 0 || in[0]) && (d == 1 || in[1]) && (d == 2 || in[2]);
+            double kvp = 0.0, np = 0.0;
+            if (others && co[d] <= nn[d] - 2) {
+                face(c, c + stp[d], kvp, np);
+                b.tb[d][c] = (float)(b.wb[d][c] + kvp);
+            }
+            if (inner) {
+                double kvm, nm;
+                face(c - stp[d], c, kvm, nm);
+                div = fma(b.wb[d][c] - b.wb[d][c - stp[d]] + (np + nm), b.sig[d], div);
+                q = fma((kvp - kvm) - (np + nm), b.sig[d], q);
+            }
+        }
+        if (inner) {
+            const double lr = b.lamb[c] * b.rdt;
+            b.rbf[c] = (float)(b.g[c] - lr - div);
+            const double cb = b.g[c] - lr + q;
+            b.Cb[c] = cb;
+            accumulate_residual(cb, part, pmax);
+        }
+    }
+    block_reduce_residual(b.acc64, 0, part, pmax);
+}
+
+__global__ void adj_rb_init_kernel(AdjRbState* st, double rtol, double accept_rtol, double norm_den)
+{
+    const double gn = sqrt(st->acc) / sqrt(norm_den);
+    st->acc = 0.0;
+    st->acc64 = 0.0;
+    st->target = fmax(rtol * gn, 1e-300);
+    st->accept = fmax(accept_rtol * gn, 1e-300);
+    st->done = gn == 0.0 ? 1 : 0;
+    st->skip = st->done;
+    st->iter = st->phase_iter = st->nchecks = st->capped = st->stalled = st->best_at = 0;
+    st->err = st->err64 = st->best = gn;
+}
+
+__global__ void adj_rb_check_judge_kernel(AdjRbState* st, int nchk, int itmax, double norm_den, int stall)
+{
+    if (st->skip || st->done) return;
+    const double err = sqrt(st->acc) / sqrt(norm_den);
+    st->acc = 0.0;
+    st->err = err;
+    st->nchecks += 1;
+    st->iter += nchk;
+    st->phase_iter += nchk;
+    if (err < 0.99 * st->best) {
+        st->best = err;
+        st->best_at = st->nchecks;
+    }
+    if (err != err) {
+        st->done = 2;
+        st->skip = 1;
+        return;
+    }
+    if (!(err > st->target)) {
+        st->skip = 1;
+    } else if (st->nchecks - st->best_at >= stall && err <= st->accept) {
+        st->skip = 1;
+        st->stalled = 1;
+    } else if (err <= 1e-4 * st->err64) {
+        st->skip = 1;
+    }
+    if (st->iter + nchk > itmax) {
+        st->skip = 1;
+        st->capped = 1;
+    }
+}
+
+__global__ void adj_rb_base_judge_kernel(AdjRbState* st, double norm_den)
+{
+    if (st->done) return;
+    const double err64 = sqrt(st->acc64) / sqrt(norm_den);
+    st->acc64 = 0.0;
+    st->err64 = err64;
+    st->phase_iter = 0;
+    if (err64 != err64) {
+        st->done = 2;
+        st->skip = 1;
+    } else if (st->iter > 0 && !(st->err > st->target) && !(err64 > st->target)) {
+        st->done = 1;
+    } else if (st->stalled && !(err64 > st->accept)) {
+        st->done = 3;
+    } else if (st->capped) {
+        st->done = 2;
+    } else {
+        st->skip = 0;
+        st->stalled = 0;
+        st->best_at = st->nchecks;
+    }
+}
+
 __global__ void __launch_bounds__(256) adj_misfit_kernel(const double* HN, const double* Ht, void* g, double* acc,
                                                          int nx, int ny, int nz, long long sy, long long sz, int df64)
 {
@@ -407,6 +636,21 @@ struct ptd_adj {
     long long launches = 0, iterations = 0;
     std::vector<double> step_err, step_target;   // last adjoint solve: final residual and target per step
     bool any_capped = false;
+    // rebased FP32 form (precision FP32_RB): lam[], w[] hold the FP32
+    // changes, Hk and E FP32 copies; the FP64 base and its defects below
+    bool rb = false;
+    double* lamb = nullptr;
+    double* wb[3] = {nullptr, nullptr, nullptr};
+    double* Hk64 = nullptr;                      // H^n of the current step (FP64)
+    void* tbf[3] = {nullptr, nullptr, nullptr};
+    void* rbf = nullptr;
+    double* Cb = nullptr;
+    AdjRbState* rbst = nullptr;
+    AdjRbState* h_rbst = nullptr;
+    AdjArgs* d_rbargs[2] = {nullptr, nullptr};
+    cudaGraphExec_t gphase = nullptr;
+    int blocks_per_phase = 1;
+    int kernels_per_phase = 0;
 };
 
 namespace {
@@ -416,6 +660,23 @@ namespace {
         cudaError_t _e = (call);                                  \
         if (_e != cudaSuccess) return cuda_fail(_e, #call);       \
     } while (0)
+
+cudaError_t adj_launch_rb(ptd_adj* A, int par, bool check)
+{
+    const dim3 blk(32, 16);
+    const int tx = (A->g.nx - 2 + 30) / 31, ty = (A->g.ny - 2 + 14) / 15;
+    const int ch = A->cfg.chunk3d;
+    const dim3 grid(tx, ty, (A->g.nz - 2 + ch - 1) / ch);
+    const AdjArgs* ap = A->d_rbargs[par];
+    if (A->expm) {
+        if (check) adj3d_kernel<F32, true, true, 16, true><<<grid, blk, 0, A->s>>>(ap, ch);
+        else adj3d_kernel<F32, true, false, 16, true><<<grid, blk, 0, A->s>>>(ap, ch);
+    } else {
+        if (check) adj3d_kernel<F32, false, true, 16, true><<<grid, blk, 0, A->s>>>(ap, ch);
+        else adj3d_kernel<F32, false, false, 16, true><<<grid, blk, 0, A->s>>>(ap, ch);
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t adj_launch(ptd_adj* A, int par, bool check)
 {
@@ -467,6 +728,108 @@ void adj_fill(ptd_adj* A, int par, AdjArgs& a)
     a.acc = &A->st->acc;
 }
 
+void adj_fill_rb(ptd_adj* A, int par, AdjArgs& a)
+{
+    adj_fill(A, par, a);
+    a.rdtf = (float)A->dv.rdt;
+    for (int d = 0; d < 3; ++d) {
+        a.sigf[d] = (float)a.sig[d];
+        a.tb[d] = A->tbf[d];
+    }
+    a.g = A->rbf;
+    a.Cb = A->Cb;
+    a.done = &A->rbst->skip;
+    a.acc = &A->rbst->acc;
+}
+
+AdjBase adj_base_args(ptd_adj* A)
+{
+    AdjBase b;
+    std::memset(&b, 0, sizeof(b));
+    b.nx = A->g.nx;
+    b.ny = A->g.ny;
+    b.nz = A->g.nz;
+    b.sy = A->g.sy;
+    b.sz = A->g.sz;
+    b.rdt = A->dv.rdt;
+    for (int d = 0; d < 3; ++d) {
+        b.sig[d] = 0.0625 / (A->dv.h[d] * A->dv.h[d]);
+        b.wb[d] = A->wb[d];
+        b.tb[d] = static_cast<float*>(A->tbf[d]);
+    }
+    b.H = A->Hk64;
+    b.E = A->expm ? A->Ed : nullptr;
+    b.lamb = A->lamb;
+    b.g = static_cast<const double*>(A->gbuf);
+    b.rbf = static_cast<float*>(A->rbf);
+    b.Cb = A->Cb;
+    b.acc64 = &A->rbst->acc64;
+    return b;
+}
+
+cudaError_t adj_rebase(ptd_adj* A)
+{
+    AdjFold f;
+    std::memset(&f, 0, sizeof(f));
+    f.n = A->g.nfield;
+    f.lamb = A->lamb;
+    for (int q = 0; q < 2; ++q) f.d[q] = static_cast<float*>(A->lam[q]);
+    for (int d = 0; d < 3; ++d) {
+        f.wb[d] = A->wb[d];
+        for (int q = 0; q < 2; ++q) f.w[d][q] = static_cast<float*>(A->w[d][q]);
+    }
+    adj_rb_fold_kernel<<<152 * 8, 256, 0, A->s>>>(f, A->rbst);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (A->expm) adj_rb_base_kernel<true><<<152 * 8, 256, 0, A->s>>>(adj_base_args(A), A->rbst);
+    else adj_rb_base_kernel<false><<<152 * 8, 256, 0, A->s>>>(adj_base_args(A), A->rbst);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    adj_rb_base_judge_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->dv.norm_den);
+    return cudaGetLastError();
+}
+
+// One phase of the rebased adjoint: check blocks of FP32 iterations, each
+// followed by the FP32 judge, then the FP64 rebase and judge.  Every phase
+// starts from buffer parity 0.
+int adj_capture_rb(ptd_adj* A)
+{
+    for (int q = 0; q < 2; ++q) {
+        AdjArgs a;
+        adj_fill_rb(A, q, a);
+        ACK(cudaMemcpy(A->d_rbargs[q], &a, sizeof(a), cudaMemcpyHostToDevice));
+    }
+    cudaGraph_t gr = nullptr;
+    ACK(cudaStreamBeginCapture(A->s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t err = cudaSuccess;
+    int par = 0, nk = 0;
+    for (int b = 0; b < A->blocks_per_phase && err == cudaSuccess; ++b) {
+        for (int it = 0; it < A->nchk && err == cudaSuccess; ++it) {
+            err = adj_launch_rb(A, par, it == A->nchk - 1);
+            par ^= 1;
+            ++nk;
+        }
+        if (err == cudaSuccess) {
+            adj_rb_check_judge_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->nchk, A->p.itmax, A->dv.norm_den, A->stall);
+            err = cudaGetLastError();
+            ++nk;
+        }
+    }
+    if (err == cudaSuccess) err = adj_rebase(A);
+    nk += 3;
+    cudaError_t e2 = cudaStreamEndCapture(A->s, &gr);
+    if (err != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        return cuda_fail(err, "adjoint capture (rebased)");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    cudaError_t e3 = cudaGraphInstantiate(&A->gphase, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+    A->kernels_per_phase = nk;
+    return PTD_OK;
+}
+
 int adj_capture(ptd_adj* A)
 {
     for (int q = 0; q < 2; ++q) {
@@ -506,13 +869,19 @@ void adj_free(ptd_adj* A)
     if (A->s) cudaStreamSynchronize(A->s);
     for (int q = 0; q < 2; ++q)
         if (A->graph[q]) cudaGraphExecDestroy(A->graph[q]);
+    if (A->gphase) cudaGraphExecDestroy(A->gphase);
     if (A->fwd) ptd_destroy(A->fwd);
     void* ptrs[] = {A->ck, A->Ht, A->Ed, A->E, A->Hk, A->lam[0], A->lam[1], A->gbuf, A->gm, A->gh, A->stage,
-                    A->st, A->d_args[0], A->d_args[1]};
+                    A->st, A->d_args[0], A->d_args[1], A->lamb, A->Hk64, A->rbf, A->Cb, A->rbst, A->d_rbargs[0],
+                    A->d_rbargs[1]};
     for (void* q : ptrs) cudaFree(q);
-    for (int d = 0; d < 3; ++d)
+    for (int d = 0; d < 3; ++d) {
         for (int q = 0; q < 2; ++q) cudaFree(A->w[d][q]);
+        cudaFree(A->wb[d]);
+        cudaFree(A->tbf[d]);
+    }
     if (A->h_st) cudaFreeHost(A->h_st);
+    if (A->h_rbst) cudaFreeHost(A->h_rbst);
     delete A;
 }
 
@@ -527,13 +896,15 @@ extern "C" int ptd_adj_create(ptd_adj** out, const ptd_params* p)
     if (p->ndim != 3) return set_error(PTD_EINVAL, "the adjoint solver is 3D");
     if (p->model != PTD_MODEL_NONLIN && p->model != PTD_MODEL_NONLIN_EXPM)
         return set_error(PTD_EINVAL, "the adjoint solver supports D = H^3 and D = exp(m) H^3");
-    if (p->precision == PTD_PREC_FP32_DC || p->precision == PTD_PREC_DFH || p->precision == PTD_PREC_FP32_RB)
-        return set_error(PTD_EINVAL, "the adjoint runs in FP64 or DF64");
+    if (p->precision == PTD_PREC_FP32_DC || p->precision == PTD_PREC_DFH)
+        return set_error(PTD_EINVAL, "the adjoint runs in FP64, DF64 or FP32_RB");
     ptd_adj* A = new (std::nothrow) ptd_adj();
     if (!A) return set_error(PTD_ENOMEM, "adjoint: host allocation failed");
     A->p = *p;
     A->df64 = p->precision == PTD_PREC_DF64;
+    A->rb = p->precision == PTD_PREC_FP32_RB;
     A->expm = p->model == PTD_MODEL_NONLIN_EXPM;
+    A->blocks_per_phase = std::max(1, (200 + A->nchk - 1) / A->nchk);
     derive(A->p, A->dv);
     A->cfg = tuned_config(A->p);
     {   // stagnation window: ~2 n_max iterations, the PT iteration's own time scale
@@ -578,6 +949,21 @@ extern "C" int ptd_adj_create(ptd_adj** out, const ptd_params* p)
     for (int q = 0; q < 2 && !rc; ++q) rc = al((void**)&A->d_args[q], sizeof(AdjArgs));
     if (!rc && cudaMallocHost((void**)&A->h_st, sizeof(AdjState)) != cudaSuccess)
         rc = set_error(PTD_ENOMEM, "adjoint: cudaMallocHost failed");
+    if (A->rb) {
+        if (!rc) rc = al((void**)&A->lamb, b);
+        if (!rc) rc = al((void**)&A->Hk64, b);
+        for (int d = 0; d < 3 && !rc; ++d) {
+            rc = al((void**)&A->wb[d], b);
+            if (!rc) rc = al(&A->tbf[d], b);
+        }
+        if (!rc) rc = al(&A->rbf, b);
+        if (!rc) rc = al((void**)&A->Cb, b);
+        if (!rc) rc = al((void**)&A->rbst, sizeof(AdjRbState));
+        for (int q = 0; q < 2 && !rc; ++q) rc = al((void**)&A->d_rbargs[q], sizeof(AdjArgs));
+        if (!rc && cudaMallocHost((void**)&A->h_rbst, sizeof(AdjRbState)) != cudaSuccess)
+            rc = set_error(PTD_ENOMEM, "adjoint: cudaMallocHost failed");
+        if (!rc) rc = adj_capture_rb(A);
+    }
     if (!rc) rc = adj_capture(A);
     if (rc) {
         adj_free(A);
@@ -619,7 +1005,12 @@ extern "C" int ptd_adj_forward(ptd_adj* A, const double* H0, const double* m, co
         if (rc) return rc;
         expd_kernel<<<152 * 8, 256, 0, A->s>>>(A->stage, A->Ed, A->g.nfield);
         ACK(cudaGetLastError());
-        ACK(launch_expm(A->stage, A->E, A->g.nfield, A->df64, A->s));
+        if (A->rb) {   // exp(m) as FP32 for the rebased adjoint iteration
+            adj_tofloat_kernel<<<152 * 8, 256, 0, A->s>>>(A->Ed, static_cast<float*>(A->E), A->g.nfield);
+            ACK(cudaGetLastError());
+        } else {
+            ACK(launch_expm(A->stage, A->E, A->g.nfield, A->df64, A->s));
+        }
     }
     ACK(cudaMemsetAsync(A->ck, 0, b, A->s));
     rc = copy_field_in(A->g, A->ck, H0, A->s);
@@ -664,7 +1055,56 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
     ACK(cudaGetLastError());
     ACK(cudaMemsetAsync(&A->st->acc, 0, sizeof(double), A->s));
     const long long cells = (long long)A->g.nx * A->g.ny * A->g.nz;
-    for (int n = A->p.nt; n >= 1; --n) {
+    for (int n = A->p.nt; n >= 1 && A->rb; --n) {
+        // rebased FP32 adjoint solve of step n
+        const double* Hn = A->ck + (size_t)n * A->g.nfield;
+        ACK(cudaMemcpyAsync(A->Hk64, Hn, b, cudaMemcpyDeviceToDevice, A->s));
+        adj_tofloat_kernel<<<152 * 8, 256, 0, A->s>>>(Hn, static_cast<float*>(A->Hk), A->g.nfield);
+        ACK(cudaGetLastError());
+        ACK(cudaMemsetAsync(A->lamb, 0, b, A->s));
+        for (int d = 0; d < 3; ++d) ACK(cudaMemsetAsync(A->wb[d], 0, b, A->s));
+        for (int q = 0; q < 2; ++q) {
+            ACK(cudaMemsetAsync(A->lam[q], 0, b, A->s));
+            for (int d = 0; d < 3; ++d) ACK(cudaMemsetAsync(A->w[d][q], 0, b, A->s));
+        }
+        ACK(cudaMemsetAsync(&A->rbst->acc, 0, sizeof(double), A->s));
+        adj_sumsq_kernel<F64><<<152 * 8, 256, 0, A->s>>>(A->gbuf, &A->rbst->acc, A->g.nx, A->g.ny, A->g.nz, A->g.sy,
+                                                         A->g.sz);
+        ACK(cudaGetLastError());
+        adj_rb_init_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->rtol, A->accept_rtol, A->dv.norm_den);
+        ACK(cudaGetLastError());
+        ACK(adj_rebase(A));   // base quantities of lam_b = 0 (the fold adds zeros)
+        A->launches += 7;
+        const long long per_phase = (long long)A->blocks_per_phase * A->nchk;
+        const long long phases_max = A->p.itmax / std::max<long long>(per_phase, 1) + A->p.itmax / A->nchk + 2;
+        long long launched = 0, batch = 1;
+        while (launched < phases_max) {
+            const long long k = std::min(batch, phases_max - launched);
+            for (long long j = 0; j < k; ++j) {
+                ACK(cudaGraphLaunch(A->gphase, A->s));
+                A->launches += A->kernels_per_phase;
+            }
+            launched += k;
+            ACK(cudaMemcpyAsync(A->h_rbst, A->rbst, sizeof(AdjRbState), cudaMemcpyDeviceToHost, A->s));
+            ACK(cudaStreamSynchronize(A->s));
+            if (A->h_rbst->done) break;
+            batch = std::min<long long>(batch * 2, 16);
+        }
+        const AdjRbState& rs = *A->h_rbst;
+        A->iterations += rs.iter;
+        if (adj_iters) adj_iters[n - 1] = rs.iter;
+        A->step_err[n - 1] = rs.err64;
+        A->step_target[n - 1] = rs.target;
+        if (rs.done == 2 || rs.done == 0) A->any_capped = true;
+        AdjArgs a;
+        adj_fill(A, 0, a);
+        a.lin = A->lamb;   // the FP64 base holds the solution
+        if (A->expm) adj_grad_kernel<F64, true><<<152 * 8, 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells);
+        else adj_grad_kernel<F64, false><<<152 * 8, 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells);
+        ACK(cudaGetLastError());
+        A->launches += 1;
+    }
+    for (int n = A->p.nt; n >= 1 && !A->rb; --n) {
         const double* Hn = A->ck + (size_t)n * A->g.nfield;
         if (A->df64) ACK(launch_to_df64(Hn, A->Hk, A->g.nfield, A->s));
         else ACK(cudaMemcpyAsync(A->Hk, Hn, b, cudaMemcpyDeviceToDevice, A->s));

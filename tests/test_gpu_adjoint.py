@@ -28,7 +28,7 @@ def make(s, shape, prec):
     return ptdiff.AdjointSolver(p)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "df64"])
+@pytest.mark.parametrize("prec", ["fp64", "df64", "fp32_rb"])
 @pytest.mark.parametrize("model", [S.NONLIN_EXPM, S.NONLIN])
 def test_adjoint_matches_reference_adjoint(prec, model):
     shape = (14, 13, 12)
@@ -47,7 +47,7 @@ def test_adjoint_matches_reference_adjoint(prec, model):
     assert np.linalg.norm(gh - gh_r) <= 1e-6 * np.linalg.norm(gh_r)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "df64"])
+@pytest.mark.parametrize("prec", ["fp64", "df64", "fp32_rb"])
 def test_adjoint_matches_finite_differences(prec):
     shape = (14, 13, 12)
     s, H0, m, Ht = problem(shape)
