@@ -463,7 +463,11 @@ def run_ours(args, world, rank, local, pg):
     # cells / launch time against this GPU's FP64 FMA rate, measured now
     rate = ctypes.c_double(0.0)
     ptdiff._abi.check(ptdiff._abi.lib().ptd_measure_fp64_rate(ctypes.byref(rate)), "ptd_measure_fp64_rate")
-    fp64_per_cell = {2: 19, 3: 27}.get(s.ndim) if s.model == ptdiff.scripts.NONLIN else None
+    # FP64 instructions per cell of the nonlinear kernel: per face s, s^3 (2),
+    # g, the flux FMA and the damping FMA (6 each), H - Hold, the flux
+    # differences and their sum (square cells: no sigma multiply), the
+    # residual FMA and the update FMA
+    fp64_per_cell = {2: 18, 3: 26}.get(s.ndim) if s.model == ptdiff.scripts.NONLIN else None
     fp64_pipe = None
     if fp64_per_cell and args.precision == "fp64":
         ach = fp64_per_cell * float(np.prod(shape)) / t_launch / 1e9

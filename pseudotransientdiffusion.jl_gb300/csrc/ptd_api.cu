@@ -230,6 +230,11 @@ void ptd::fill_args(const ptd_params& p, const Derived& dv, PTArgs& a)
     a.fe_lin = (float)dv.e_lin;
     a.f = fparams(dv);
     a.norm_max = p.norm == PTD_NORM_MAX;
+    a.sq = 1;
+    for (int d = 1; d < p.ndim; ++d) a.sq = a.sq && dv.sig[d] == dv.sig[0];
+    a.rdt_sig = dv.rdt / dv.sig[0];
+    a.rdt_sig_df = split_df(a.rdt_sig);
+    a.fsig = (float)dv.sig[0];
 }
 
 // ---------------------------------------------------------------------------

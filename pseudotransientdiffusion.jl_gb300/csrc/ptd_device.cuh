@@ -63,6 +63,13 @@ struct PTArgs {
     const int* done;    // nonzero: the step has stopped, skip the iteration
     double* acc;        // residual accumulator: sum R^2 (RMS) or max |R| bits (MAX)
     int norm_max;
+    // equal sigma_d in every dimension (square cells): the update is formed
+    // as (H - Hold) rdt/sigma + sum_d (w_R - w_L) with e*sigma, one
+    // multiplication fewer per cell
+    int sq;
+    double rdt_sig;     // rdt / sigma
+    float2 rdt_sig_df;
+    float fsig;         // sigma (FP32, scales e)
 };
 
 // ---------------------------------------------------------------------------

@@ -64,20 +64,21 @@ __device__ __forceinline__ typename N::T face_t(const PTArgs& a, const typename 
 
 template <class N>
 __device__ __forceinline__ typename N::T cst(const PTArgs& a, int which);
+// which: 0..2 sigma_d, 3 rdt, 4 rdt/sigma (square cells)
 template <>
 __device__ __forceinline__ double cst<F64>(const PTArgs& a, int which)
 {
-    return which < 3 ? a.sig[which] : a.rdt;
+    return which < 3 ? a.sig[which] : (which == 3 ? a.rdt : a.rdt_sig);
 }
 template <>
 __device__ __forceinline__ float2 cst<DF64>(const PTArgs& a, int which)
 {
-    return which < 3 ? a.sig_df[which] : a.rdt_df;
+    return which < 3 ? a.sig_df[which] : (which == 3 ? a.rdt_df : a.rdt_sig_df);
 }
 template <>
 __device__ __forceinline__ float2 cst<DFH>(const PTArgs& a, int which)
 {
-    return which < 3 ? a.sig_df[which] : a.rdt_df;
+    return which < 3 ? a.sig_df[which] : (which == 3 ? a.rdt_df : a.rdt_sig_df);
 }
 
 template <int MODEL>
@@ -101,6 +102,16 @@ __device__ __forceinline__ typename N::HS h_update(const PTArgs& a, const typena
 {
     const typename N::T Rp = N::mad(N::hdo(Hc, Ho), cst<N>(a, 3), div);
     return N::hstep(Hc, Rp, e);
+}
+
+// The same for square cells from the undivided flux differences:
+// H_new = H - (e sigma)*((H - Hold) rdt/sigma + sum_d (w_R - w_L)).
+template <class N>
+__device__ __forceinline__ typename N::HS h_update_sq(const PTArgs& a, const typename N::HV& Hc, typename N::HS Ho,
+                                                      typename N::T dsum, float e)
+{
+    const typename N::T Rp = N::mad(N::hdo(Hc, Ho), cst<N>(a, 4), dsum);
+    return N::hstep(Hc, Rp, e * a.fsig);
 }
 
 // ---------------------------------------------------------------------------
@@ -131,10 +142,9 @@ __device__ __forceinline__ void pt1d_body(const PTArgs& a, int bx, double& part,
             T ul = N::zero();
             const T wl = face_t<N, MODEL, CHECK>(a, Hl, Hc, N::hf(Hl) + hc, Dl, Dc, ld<N>(a.win[0], i - 1), ul);
             const HS Ho = N::ldo(a.Hold, i);
-            const T div = N::mul(N::sub(wr, wl), cst<N>(a, 0));
             const float e = cell_e<MODEL>(a, hc, MODEL == NONLIN_EXPM ? N::lo_f(Dc)
                                                  : fmaxf(fmaxf(N::lo_f(Dl), N::lo_f(Dr)), N::lo_f(Dc)));
-            const HS Hn = h_update<N>(a, Hc, Ho, div, e);
+            const HS Hn = h_update_sq<N>(a, Hc, Ho, N::sub(wr, wl), e);   // one dimension: sigma is the only one
             N::sth(a.Hout, i, Hn);
             if (CHECK) {
                 const T r = N::sub(N::mul(N::sub(ur, ul), cst<N>(a, 0)), N::mul(N::hdn(Hn, Ho), cst<N>(a, 3)));
@@ -214,8 +224,13 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
                 const float dmax = MODEL == LINSTEP ? fmaxf(fmaxf(fmaxf(dcf, dlf), fmaxf(N::lo_f(Dr), dbf)), dnf)
                                                     : (MODEL == NONLIN_EXPM ? N::lo_f(Dc) : 0.0f);
                 const float e = cell_e<MODEL>(a, hc, dmax);
-                const T div = N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0)));
-                const HS Hnew = h_update<N>(a, Hc, Ho, div, e);
+                HS Hnew;
+                if (a.sq) {
+                    Hnew = h_update_sq<N>(a, Hc, Ho, N::add(N::sub(wyn, wyb), N::sub(wxn, wxl)), e);
+                } else {
+                    const T div = N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0)));
+                    Hnew = h_update<N>(a, Hc, Ho, div, e);
+                }
                 N::sth(a.Hout, idx, Hnew);
                 if (CHECK) {
                     const T divu = N::mad(N::sub(uy, uyb), cst<N>(a, 1), N::mul(N::sub(ux, uxl), cst<N>(a, 0)));
@@ -354,9 +369,15 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
                                                             fmaxf(fmaxf(ddf, dbf), dnf))
                                                     : (MODEL == NONLIN_EXPM ? N::lo_f(Dc) : 0.0f);
                 const float e = cell_e<MODEL>(a, hc, dmax);
-                const T div = N::mad(N::sub(wzn, wzb), cst<N>(a, 2),
-                                     N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0))));
-                const HS Hnew = h_update<N>(a, Hc, Ho, div, e);
+                HS Hnew;
+                if (a.sq) {
+                    const T dsum = N::add(N::add(N::sub(wzn, wzb), N::sub(wyn, wyb)), N::sub(wxn, wxl));
+                    Hnew = h_update_sq<N>(a, Hc, Ho, dsum, e);
+                } else {
+                    const T div = N::mad(N::sub(wzn, wzb), cst<N>(a, 2),
+                                         N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0))));
+                    Hnew = h_update<N>(a, Hc, Ho, div, e);
+                }
                 N::sth(a.Hout, idx, Hnew);
                 if (CHECK) {
                     const T uyb = sU[p][r - 1][lane];
