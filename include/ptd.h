@@ -106,8 +106,8 @@ enum { PTD_NORM_RMS = 0, PTD_NORM_MAX = 1 };
 #define PTD_FLAG_STRICT 0x1   /* return PTD_ENOTCONV when a step stops at itmax */
 #define PTD_FLAG_AUTOTUNE 0x2 /* ptd_create times every launch shape of the fused kernel (2D: warps per CTA
                                  x rows per y march; 3D: z-march length x warps per CTA) and keeps the fastest */
-#define PTD_FLAG_DC_NO_TBLOCK 0x4 /* FP32_DC in 2D: one inner iteration per launch (default: two per launch,
-                                     temporally blocked, when the check cadence is even) */
+#define PTD_FLAG_DC_NO_TBLOCK 0x4 /* FP32_DC and FP32_RB in 2D: one FP32 iteration per launch (default: two
+                                     per launch, temporally blocked, when the check cadence is even) */
 
 typedef struct ptd_params {
     int32_t ndim;        /* 1, 2, 3 */

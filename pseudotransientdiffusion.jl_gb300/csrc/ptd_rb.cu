@@ -223,6 +223,151 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
 }
 
 // ---------------------------------------------------------------------------
+// 2D, two iterations per launch (temporal blocking).  The first iteration
+// (level 1) runs one row ahead of the second (level 2) in the y march; the
+// level-1 deltas and fluxes of the current and previous rows stay in
+// registers, so a launch reads and writes each field once for two
+// iterations.  A warp covers 32 columns, lane L <-> column 28 t + L - 1:
+// level-1 x faces on lanes 0..30, level-1 updates on lanes 1..30, level-2
+// x faces on lanes 1..29 and level-2 updates on lanes 2..29 (28 columns per
+// warp), so every right neighbour comes from a shuffle.  Each iteration's
+// arithmetic is rb2d_body's, operation for operation.
+template <int MODEL>
+__device__ __forceinline__ float rb_star(float Dc, float Db, float Dn)
+{
+    if (MODEL != LINSTEP) return Dc;   // NONLIN_EXPM: exp(m) of the cell; unused otherwise
+    const float Dr = __shfl_down_sync(FULL, Dc, 1);
+    const float Dl = __shfl_up_sync(FULL, Dc, 1);
+    return fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Db)), Dn);
+}
+
+template <int MODEL, bool CHECK>
+__device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
+                                              unsigned long long& pmax)
+{
+    constexpr bool HASD = MODEL == LINSTEP || MODEL == NONLIN_EXPM;
+    const int lane = threadIdx.x;
+    const int nx = a.nx, ny = a.ny;
+    const int j0 = 1 + cy * chunk;
+    const int j1 = min(j0 + chunk, ny - 1);
+    if (28 * tile >= nx - 2 || j0 >= j1) return;   // uniform over the warp
+    const int i = 28 * tile + lane - 1;
+    const int ic = min(max(i, 0), nx - 1);          // clamped column of this lane's loads
+    const bool colin = i >= 1 && i <= nx - 2;
+    const bool upd1 = colin && lane >= 1 && lane <= 30;
+    const bool xf2 = i >= 0 && i <= nx - 2 && lane >= 1 && lane <= 29;
+    const bool upd2 = colin && lane >= 2 && lane <= 29;
+    const bool own_x = xf2 && (lane <= 28 || i == nx - 2);   // face i+1/2 of lane 29: the next tile's lane 1
+    const long long sy = a.sy;
+    const float s0 = a.sig[0], s1 = a.sig[1], rdt = a.rdt;
+    float u;
+
+    // level-1 x face of a row at offset o (flux omega of the input state)
+    auto x1 = [&](long long o, float d, float h, float D, float& tbx) {
+        const float dr = __shfl_down_sync(FULL, d, 1);
+        const float hr = __shfl_down_sync(FULL, h, 1);
+        const float Dr = HASD ? __shfl_down_sync(FULL, D, 1) : 0.0f;
+        tbx = a.tb[0][o];
+        return rb_face<MODEL, false>(a, d, dr, h, hr, D, Dr, a.win[0][o], tbx, u);
+    };
+    auto cell = [&](float d, float e, float r, float wx, float wxl, float wy, float wyb) {
+        return fmaf(-e, fmaf(d, rdt, r + fmaf(wy - wyb, s1, (wx - wxl) * s0)), d);
+    };
+
+    // ---- prologue: level 1 of rows j0-1 (A) and j0 (B), level-2 face j0-1/2
+    const long long oA = (long long)(j0 - 1) * sy + ic, oB = oA + sy, oC = oB + sy;
+    const float dA = a.din[oA], hA = a.Hf[oA];
+    const float DA = HASD ? a.Df[oA] : 0.0f;
+    const float dB = a.din[oB], hB = a.Hf[oB];
+    const float DB = HASD ? a.Df[oB] : 0.0f;
+    float d1 = a.din[oC], h1 = a.Hf[oC];    // row j0+1 <= ny-1
+    float D1 = HASD ? a.Df[oC] : 0.0f;
+    const float tbyA = a.tb[1][oA];
+    const float wyAB = rb_face<MODEL, false>(a, dA, dB, hA, hB, DA, DB, a.win[1][oA], tbyA, u);  // omega'_y(j0-1/2)
+    float pA = dA;                          // delta'(j0-1)
+    if (j0 >= 2) {                          // row j0-1 is interior: level 1 there
+        const long long oZ = oA - sy;
+        const float dZ = a.din[oZ], hZ = a.Hf[oZ];
+        const float DZ = HASD ? a.Df[oZ] : 0.0f;
+        const float wyZA = rb_face<MODEL, false>(a, dZ, dA, hZ, hA, DZ, DA, a.win[1][oZ], a.tb[1][oZ], u);
+        float tbxA;
+        const float wxA = x1(oA, dA, hA, DA, tbxA);
+        const float wxAl = __shfl_up_sync(FULL, wxA, 1);
+        const float eA = rb_cell_e<MODEL>(a, hA + dA, rb_star<MODEL>(DA, DZ, DB));
+        if (upd1) pA = cell(dA, eA, a.Rb[oA], wxA, wxAl, wyAB, wyZA);
+    }
+    float tbx0;
+    float wx1p = x1(oB, dB, hB, DB, tbx0);                 // omega'_x(j0)
+    float tby0 = a.tb[1][oB];
+    float wy1p = rb_face<MODEL, false>(a, dB, d1, hB, h1, DB, D1, a.win[1][oB], tby0, u);  // omega'_y(j0+1/2)
+    float r0 = a.Rb[oB];
+    float p0 = dB;                                         // delta'(j0)
+    {
+        const float wxl = __shfl_up_sync(FULL, wx1p, 1);
+        const float eB = rb_cell_e<MODEL>(a, hB + dB, rb_star<MODEL>(DB, DA, D1));
+        if (upd1) p0 = cell(dB, eB, r0, wx1p, wxl, wy1p, wyAB);
+    }
+    float uy2b = 0.0f;
+    float wy2b = rb_face<MODEL, CHECK>(a, pA, p0, hA, hB, DA, DB, wyAB, tbyA, uy2b);   // omega''_y(j0-1/2)
+    if (j0 == 1 && upd2) a.wout[1][oA] = wy2b;
+    float h0 = hB, D0 = DB, Dm1 = DA;
+
+    // ---- march: level 1 of row s+1, level 2 of row s
+    long long o = oC;   // offset of row s+1
+    for (int s = j0; s < j1; ++s, o += sy) {
+        float p1 = d1, wx1 = 0.0f, wy1 = 0.0f, r1 = 0.0f, h2 = h1, D2 = D1, tbx1 = 0.0f, tby1 = 0.0f;
+        if (s + 1 <= ny - 2) {   // row s+1 interior (uniform): level 1 there
+            const float d2 = a.din[o + sy];
+            h2 = a.Hf[o + sy];
+            if (HASD) D2 = a.Df[o + sy];
+            r1 = a.Rb[o];
+            tby1 = a.tb[1][o];
+            wx1 = x1(o, d1, h1, D1, tbx1);
+            wy1 = rb_face<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], tby1, u);
+            const float wx1l = __shfl_up_sync(FULL, wx1, 1);
+            const float e1 = rb_cell_e<MODEL>(a, h1 + d1, rb_star<MODEL>(D1, D0, D2));
+            if (upd1) p1 = cell(d1, e1, r1, wx1, wx1l, wy1, wy1p);
+            d1 = d2;
+        }
+        // level 2 of row s
+        const float p0r = __shfl_down_sync(FULL, p0, 1);
+        const float h0r = __shfl_down_sync(FULL, h0, 1);
+        const float D0r = HASD ? __shfl_down_sync(FULL, D0, 1) : 0.0f;
+        float ux2 = 0.0f, uy2 = 0.0f;
+        const float wx2 = rb_face<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, tbx0, ux2);
+        const float wy2 = rb_face<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, tby0, uy2);
+        const float wx2l = __shfl_up_sync(FULL, wx2, 1);
+        const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
+        const float e0 = rb_cell_e<MODEL>(a, h0 + p0, rb_star<MODEL>(D0, Dm1, D1));
+        const long long os = o - sy;
+        if (own_x) a.wout[0][os] = wx2;
+        if (upd2) {
+            const float q = cell(p0, e0, r0, wx2, wx2l, wy2, wy2b);
+            a.dout[os] = q;
+            a.wout[1][os] = wy2;
+            if (CHECK) {
+                const float divu = fmaf(uy2 - uy2b, s1, (ux2 - ux2l) * s0);
+                accumulate_residual(a.Cb[os] + (double)divu - (double)q * (double)rdt, part, pmax);
+            }
+        }
+        // shift the windows
+        p0 = p1;
+        wx1p = wx1;
+        wy1p = wy1;
+        tbx0 = tbx1;
+        tby0 = tby1;
+        r0 = r1;
+        wy2b = wy2;
+        uy2b = uy2;
+        h0 = h1;
+        h1 = h2;
+        Dm1 = D0;
+        D0 = D1;
+        D1 = D2;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // 3D: R warps as the y rows of an x-y tile, z march (ptd_pt_body.cuh).
 template <int MODEL, bool CHECK, int R>
 __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int bz, int chunk, double& part,
@@ -354,6 +499,16 @@ __global__ void __launch_bounds__(256) rb2d_kernel(RbArgs a, int chunk)
 }
 
 template <int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) rb2d_tb2_kernel(RbArgs a, int chunk)
+{
+    if (rb_skip(a.skip)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    rb2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+}
+
+template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(512) rb3d_kernel(RbArgs a, int chunk)
 {
     if (rb_skip(a.skip)) return;
@@ -367,7 +522,7 @@ __global__ void __launch_bounds__(512) rb3d_kernel(RbArgs a, int chunk)
 // Rebase, FP64.  Fold the changes into the base: H_b += delta, w_b += omega
 // (positions that are never updated hold zeros), and clear the buffers the
 // next phase starts from (parity 0).  parity < 0: the buffers of the phase's
-// own parity (RbDev::phase_iter).
+// own parity (RbDev::phase_iter, tb iterations per launch).
 struct RbFoldArgs {
     long long n;
     double* H;
@@ -377,11 +532,11 @@ struct RbFoldArgs {
     int ndim;
 };
 
-__global__ void rb_fold_kernel(RbFoldArgs f, const RbDev* st, int parity)
+__global__ void rb_fold_kernel(RbFoldArgs f, const RbDev* st, int parity, int tb)
 {
     if (parity < 0) {
         if (st->step_done) return;
-        parity = st->phase_iter & 1;
+        parity = (st->phase_iter / tb) & 1;   // one buffer swap per launch of tb iterations
     }
     const float* dp = parity ? f.d[1] : f.d[0];
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < f.n;
@@ -571,6 +726,7 @@ struct RbState {
     double* errhist = nullptr;
     int errcap = 0;
     int blocks_per_phase = 1;
+    int tblk = 1;                                 // iterations per launch (2: temporal blocking, 2D)
     cudaGraphExec_t gphase = nullptr;
     int kernels_per_phase = 0;
     DcCounters k;
@@ -615,10 +771,18 @@ void rb_args(const RbState* rb, int parity, const int* skip, RbArgs& a)
 }
 
 template <int MODEL, bool CHECK>
-cudaError_t rb_launch_model(const RbArgs& a, int ndim, const LaunchCfg& cfg, cudaStream_t s)
+cudaError_t rb_launch_model(const RbArgs& a, int ndim, const LaunchCfg& cfg, cudaStream_t s, int tb)
 {
     if (ndim == 1) {
         rb1d_kernel<MODEL, CHECK><<<(a.nx + 255) / 256, 256, 0, s>>>(a);
+    } else if (ndim == 2 && tb == 2) {
+        // twice the configured rows per y march: the march starts with two
+        // extra level-1 rows (4096^2 nonlinear, 2 warps: 87.2 us per
+        // iteration at 16 rows, 85.9 at 32, 86.0 at 64)
+        const int W = cfg.warps2d, chunk = 2 * cfg.chunk2d;
+        const int tiles = (a.nx - 2 + 27) / 28;
+        dim3 grid((tiles + W - 1) / W, (a.ny - 2 + chunk - 1) / chunk);
+        rb2d_tb2_kernel<MODEL, CHECK><<<grid, dim3(32, W), 0, s>>>(a, chunk);
     } else if (ndim == 2) {
         const int W = cfg.warps2d;
         const int tiles = (a.nx - 2 + 30) / 31;
@@ -632,19 +796,39 @@ cudaError_t rb_launch_model(const RbArgs& a, int ndim, const LaunchCfg& cfg, cud
     return cudaGetLastError();
 }
 
-cudaError_t rb_launch(const RbArgs& a, int ndim, int model, bool check, const LaunchCfg& cfg, cudaStream_t s)
+// One launch of tb PT iterations (tb = 2: 2D only).
+cudaError_t rb_launch(const RbArgs& a, int ndim, int model, bool check, const LaunchCfg& cfg, cudaStream_t s,
+                      int tb = 1)
 {
     switch (model * 2 + (check ? 1 : 0)) {
-    case 0: return rb_launch_model<LIN, false>(a, ndim, cfg, s);
-    case 1: return rb_launch_model<LIN, true>(a, ndim, cfg, s);
-    case 2: return rb_launch_model<LINSTEP, false>(a, ndim, cfg, s);
-    case 3: return rb_launch_model<LINSTEP, true>(a, ndim, cfg, s);
-    case 4: return rb_launch_model<NONLIN, false>(a, ndim, cfg, s);
-    case 5: return rb_launch_model<NONLIN, true>(a, ndim, cfg, s);
-    case 6: return rb_launch_model<NONLIN_EXPM, false>(a, ndim, cfg, s);
-    case 7: return rb_launch_model<NONLIN_EXPM, true>(a, ndim, cfg, s);
+    case 0: return rb_launch_model<LIN, false>(a, ndim, cfg, s, tb);
+    case 1: return rb_launch_model<LIN, true>(a, ndim, cfg, s, tb);
+    case 2: return rb_launch_model<LINSTEP, false>(a, ndim, cfg, s, tb);
+    case 3: return rb_launch_model<LINSTEP, true>(a, ndim, cfg, s, tb);
+    case 4: return rb_launch_model<NONLIN, false>(a, ndim, cfg, s, tb);
+    case 5: return rb_launch_model<NONLIN, true>(a, ndim, cfg, s, tb);
+    case 6: return rb_launch_model<NONLIN_EXPM, false>(a, ndim, cfg, s, tb);
+    case 7: return rb_launch_model<NONLIN_EXPM, true>(a, ndim, cfg, s, tb);
     }
     return cudaErrorInvalidValue;
+}
+
+// niter PT iterations without checks from buffer parity 0 (pairs per launch
+// when temporal blocking is on); returns the parity of the result.
+cudaError_t rb_run_plain(const RbState* rb, int32_t niter, const int* skip, int& par, long long& launches)
+{
+    par = 0;
+    for (int32_t it = 0; it < niter;) {
+        const int tb = (rb->tblk == 2 && niter - it >= 2) ? 2 : 1;
+        RbArgs a;
+        rb_args(rb, par, skip, a);
+        cudaError_t e = rb_launch(a, rb->p.ndim, rb->p.model, false, rb->cfg, rb->s, tb);
+        if (e != cudaSuccess) return e;
+        par ^= 1;
+        ++launches;
+        it += tb;
+    }
+    return cudaSuccess;
 }
 
 RbFoldArgs fold_args(const RbState* rb)
@@ -702,11 +886,12 @@ int rb_capture(RbState* rb)
     cudaError_t err = cudaSuccess;
     int par = 0, nk = 0;
     const int nchk = rb->p.nchk;
+    const int nl = nchk / rb->tblk;   // launches per check block (tb divides nchk)
     for (int b = 0; b < rb->blocks_per_phase && err == cudaSuccess; ++b) {
-        for (int it = 0; it < nchk && err == cudaSuccess; ++it) {
+        for (int it = 0; it < nl && err == cudaSuccess; ++it) {
             RbArgs a;
             rb_args(rb, par, &rb->dev->skip, a);
-            err = rb_launch(a, rb->p.ndim, rb->p.model, it == nchk - 1, rb->cfg, rb->s);
+            err = rb_launch(a, rb->p.ndim, rb->p.model, it == nl - 1, rb->cfg, rb->s, rb->tblk);
             par ^= 1;
             ++nk;
         }
@@ -718,7 +903,7 @@ int rb_capture(RbState* rb)
         }
     }
     if (err == cudaSuccess) {
-        rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, -1);
+        rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, -1, rb->tblk);
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) {
@@ -757,6 +942,7 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     rb->cfg = tuned_config(p);
     // a phase: the check blocks of ~200 PT iterations between two FP64 rebases
     rb->blocks_per_phase = std::max(1, (200 + p.nchk - 1) / p.nchk);
+    rb->tblk = (p.ndim == 2 && p.nchk % 2 == 0 && !(p.flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
     rb->errcap = (p.nchk <= p.itmax ? p.itmax / p.nchk : 0) + 2;
     const size_t fb = (size_t)g.nfield * sizeof(float);
     auto alloc = [&](void** ptr, size_t n) -> int {
@@ -788,8 +974,12 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
         cudaError_t e = cudaMemsetAsync(rb->dev, 0, sizeof(RbDev), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(rb->zero_flag, 0, sizeof(int), s);
         for (int q = 0; q < 2 && e == cudaSuccess; ++q) e = cudaMemsetAsync(rb->d[q], 0, fb, s);
-        for (int d = 0; d < p.ndim && e == cudaSuccess; ++d)
+        for (int d = 0; d < p.ndim && e == cudaSuccess; ++d) {
             for (int q = 0; q < 2 && e == cudaSuccess; ++q) e = cudaMemsetAsync(rb->w[d][q], 0, fb, s);
+            // faces past the last one of each direction are read (never used) by the halo lanes
+            if (e == cudaSuccess) e = cudaMemsetAsync(rb->tb[d], 0, fb, s);
+        }
+        if (e == cudaSuccess) e = cudaMemsetAsync(rb->Rb, 0, fb, s);
         if (e != cudaSuccess) rc = cuda_fail(e, "rb: cudaMemsetAsync");
     }
     if (rc) {
@@ -885,15 +1075,11 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
         // checks, from the folded base, then fold them in
         const int32_t tail = rb->p.itmax - iter;
         int par = 0;
-        for (int32_t it = 0; it < tail; ++it) {
-            RbArgs a;
-            rb_args(rb, par, rb->zero_flag, a);
-            RCK(rb_launch(a, rb->p.ndim, rb->p.model, false, rb->cfg, rb->s));
-            par ^= 1;
-        }
-        rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, par);
+        long long nl = 0;
+        RCK(rb_run_plain(rb, tail, rb->zero_flag, par, nl));
+        rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
         RCK(cudaGetLastError());
-        rb->k.launches += tail + 1;
+        rb->k.launches += nl + 1;
         iter = rb->p.itmax;
     }
     *iters = iter;
@@ -918,15 +1104,11 @@ int rb_iterate(RbState* rb, int32_t niter)
     rb_base_kernel<<<152 * 8, 256, 0, rb->s>>>(base_args(rb), nullptr);
     RCK(cudaGetLastError());
     int par = 0;
-    for (int32_t it = 0; it < niter; ++it) {
-        RbArgs a;
-        rb_args(rb, par, rb->zero_flag, a);
-        RCK(rb_launch(a, rb->p.ndim, rb->p.model, false, rb->cfg, rb->s));
-        par ^= 1;
-    }
-    rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, par);
+    long long nl = 0;
+    RCK(rb_run_plain(rb, niter, rb->zero_flag, par, nl));
+    rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
     RCK(cudaGetLastError());
-    rb->k.launches += niter + 2;
+    rb->k.launches += nl + 2;
     rb->k.iterations += niter;
     return PTD_OK;
 }

@@ -29,7 +29,8 @@ PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC, "df64": _abi
 def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=None,
                 precision="fp64", resid="mixed", norm="rms", norm_len=0.0, strict=False,
                 autotune=False, dc_max_outer=0, dc_inner_rtol=0.0, dc_tblock=True) -> _abi.PtdParams:
-    """ptd_params for a script at a grid shape (x fastest)."""
+    """ptd_params for a script at a grid shape (x fastest).  dc_tblock=False:
+    one FP32 iteration per launch in 2D (FP32_DC, FP32_RB) instead of two."""
     p = _abi.PtdParams()
     _abi.check(_abi.lib().ptd_params_init(C.byref(p), script.ndim, script.model), "ptd_params_init")
     p.nx = shape[0]

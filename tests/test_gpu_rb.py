@@ -145,3 +145,44 @@ def test_rebased_fp32_expm_model_matches_fp64(shape):
     rms = float(np.sqrt(np.mean(np.square(H64))))
     assert rel_l2(H32, H64) <= 2 * s.dt * s.tol / rms
     assert np.all(np.abs(it32.astype(int) - it64.astype(int)) <= 3 * s.nout)
+
+
+# 2D FP32 iterations run two per launch (temporal blocking) when the check
+# cadence is even; each iteration's arithmetic is the one-per-launch
+# kernel's, so the two agree to the order of the residual reduction.
+@pytest.mark.parametrize("name,shape,kw", [
+    ("diff_2D_lin", (64, 64), {}), ("diff_2D_linstep", (66, 33), {}), ("diff_2D_nonlin", (97, 130), {}),
+    ("diff_2D_nonlin", (3, 3), {}), ("diff_2D_linstep", (200, 7), {}), ("diff_2D_lin", (31, 250), {}),
+    ("diff_2D_react", (64, 64), {}), ("diff_2D_nonlin", (58, 60), {"nchk": 2}),
+    ("diff_2D_nonlin", (64, 64), {"nchk": 10, "itmax": 95}), ("diff_2D_nonlin_perf", (64, 64), {"itmax": 33})])
+def test_rebased_fp32_temporal_blocking_matches_one_iteration_per_launch(name, shape, kw):
+    s = S.SCRIPTS[name]
+    H2, _, it2, _, st2 = run(s, shape, **kw)
+    H1, _, it1, _, st1 = run(s, shape, dc_tblock=False, **kw)
+    assert st1 == 0 and st2 == 0
+    assert list(it1) == list(it2)
+    assert rel_l2(H2, H1) <= 1e-12
+
+
+def test_rebased_fp32_temporal_blocking_expm_and_iterate():
+    """D = exp(m) H^3 with temporal blocking, and odd fixed-iteration counts
+    (a single-iteration launch finishes them)."""
+    base = S.SCRIPTS["diff_2D_nonlin"]
+    s = base.with_(name="expm", model=S.NONLIN_EXPM, shift=1.0, dirichlet=1.0, ic="linrange", ttot=0.4)
+    shape = (61, 47)
+    m = np.asfortranarray(S.log_coefficient_field(shape, lengths=(10.0, 10.0), seed=5))
+    out = []
+    for tblock in (True, False):
+        H = S.initial_condition(s, *shape)
+        with ptdiff.Solver(ptdiff.make_params(s, shape, precision="fp32_rb", dc_tblock=tblock)) as sol:
+            iters, _, st = sol.solve(H, m)
+            assert st == 0
+            H2 = S.initial_condition(s, *shape)
+            sol.set_state(H2, m)
+            sol.iterate(37)
+            Hi = sol.get_state()
+        out.append((H, iters, Hi))
+    (Ha, ia, Hia), (Hb, ib, Hib) = out
+    assert list(ia) == list(ib)
+    assert rel_l2(Ha, Hb) <= 1e-12
+    assert rel_l2(Hia, Hib) <= 1e-12
