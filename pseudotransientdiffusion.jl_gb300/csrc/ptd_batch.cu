@@ -464,8 +464,8 @@ void build_work(ptd_batch* b, std::vector<int4>& work)
     work.clear();
     const int W = b->cfg.warps2d, ch = b->cfg.chunk2d;
     for (int i = 0; i < b->ninst; ++i) {
-        // x tiles of 31 updated columns, or 29 for the temporally blocked kernel
-        const int tiles = (b->dc && b->tb == 2) ? (b->inst[i].nx - 1 + 28) / 29 : (b->inst[i].nx - 2 + 30) / 31;
+        // x tiles of 31 updated columns, or 28 for the temporally blocked kernel
+        const int tiles = (b->dc && b->tb == 2) ? (b->inst[i].nx - 2 + 27) / 28 : (b->inst[i].nx - 2 + 30) / 31;
         const int bx = (tiles + W - 1) / W;
         const int by = (b->inst[i].ny - 2 + ch - 1) / ch;
         for (int y = 0; y < by; ++y)

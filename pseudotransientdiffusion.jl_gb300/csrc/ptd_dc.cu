@@ -231,7 +231,7 @@ static cudaError_t dc_launch_model(const DcArgs& a, int ndim, const LaunchCfg& c
         dc1d_kernel<MODEL, CHECK><<<(a.nx + 255) / 256, 256, 0, s>>>(a);
     } else if (ndim == 2 && tb == 2) {
         const int W = cfg.warps2d;
-        const int tiles = (a.nx - 1 + 28) / 29;
+        const int tiles = (a.nx - 2 + 27) / 28;
         dim3 grid((tiles + W - 1) / W, (a.ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);
         dc2d_tb2_kernel<MODEL, CHECK><<<grid, dim3(32, W), 0, s>>>(a, cfg.chunk2d);
     } else if (ndim == 2) {

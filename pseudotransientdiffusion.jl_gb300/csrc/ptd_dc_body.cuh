@@ -191,113 +191,102 @@ __device__ __forceinline__ float dc_update(const DcArgs& a, float d, float wx, f
 // level-2 values are written: level-1 values live in registers (the rows the
 // level-2 stencil needs) and in warp shuffles (the x neighbours).
 //
-// x: lane L of warp-tile t holds column i = 29t + L - 1.  Level-1 x faces are
-// valid on lanes 0..31 (lane 31 loads its right neighbour), level-1 cells on
-// lanes 1..31 (the left face comes from lane L-1), level-2 x faces on lanes
-// 1..30 and level-2 cells on lanes 2..30: each tile updates 29 columns, and
-// stores the x faces of lanes 1..29 (every face i+1/2, i = 0..nx-2, has one
-// owner).  y: a chunk of level-2 rows [j0, j1) first recomputes level 1 for
-// rows j0-1 and j0 (the halo), then each march step s computes level 1 for
-// row s+1 and level 2 for row s.  Boundary rows and columns are never
-// updated (their level-1 and level-2 values are the input).  The check
-// variant forms the mixed residual of the second iteration: undamped flux
-// from the level-1 state, time term from the level-2 state.
+// x: lane L of warp-tile t holds column i = 28t + L - 1.  Level-1 x faces
+// are used on lanes 0..30 (the right neighbour is lane L+1's column, so no
+// lane loads beyond its own), level-1 cells on lanes 1..30, level-2 x faces
+// on lanes 1..29 and level-2 cells on lanes 2..29: each tile updates 28
+// columns and stores the x faces of lanes 1..28, and of lane 29 when it is
+// the last face (every face i+1/2, i = 0..nx-2, has one owner).  y: a chunk
+// of level-2 rows [j0, j1) first recomputes level 1 for rows j0-1 and j0
+// (the halo), then each march step s computes level 1 for row s+1 and
+// level 2 for row s.  Boundary rows and columns are never updated (their
+// level-1 and level-2 values are the input).  The check variant forms the
+// mixed residual of the second iteration: undamped flux from the level-1
+// state, time term from the level-2 state.
+template <int MODEL>
+__device__ __forceinline__ float dc_star(float Dc, float Db, float Dn)
+{
+    if (MODEL != LINSTEP) return 0.0f;
+    const float Dr = __shfl_down_sync(FULL, Dc, 1);
+    const float Dl = __shfl_up_sync(FULL, Dc, 1);
+    return fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Db)), Dn);
+}
+
 template <int MODEL, bool CHECK>
 __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy, int chunk, double& part,
                                               unsigned long long& pmax)
 {
+    constexpr bool LS = MODEL == LINSTEP;
     const int lane = threadIdx.x;
     const int nx = a.nx, ny = a.ny;
     const int j0 = 1 + cy * chunk;
     const int j1 = min(j0 + chunk, ny - 1);
-    if (29 * tile >= nx - 1 || j0 >= j1) return;   // uniform over the warp
-    const int i = 29 * tile + lane - 1;
+    if (28 * tile >= nx - 2 || j0 >= j1) return;   // uniform over the warp
+    const int i = 28 * tile + lane - 1;
     const int ic = min(max(i, 0), nx - 1);          // clamped column of this lane's loads
-    const int icr = min(ic + 1, nx - 1);            // lane 31's right neighbour
     const bool colin = i >= 1 && i <= nx - 2;       // interior column
-    const bool xf = i >= 0 && i <= nx - 2;          // face i+1/2 exists
-    const bool upd1 = colin && lane >= 1;
-    const bool xf2 = xf && lane >= 1 && lane <= 30;
-    const bool upd2 = colin && lane >= 2 && lane <= 30;
-    const bool own_x = xf && lane >= 1 && lane <= 29;
-    const bool L31 = lane == 31;
-    constexpr bool LS = MODEL == LINSTEP;
+    const bool upd1 = colin && lane >= 1 && lane <= 30;
+    const bool xf2 = i >= 0 && i <= nx - 2 && lane >= 1 && lane <= 29;
+    const bool upd2 = colin && lane >= 2 && lane <= 29;
+    const bool own_x = xf2 && (lane <= 28 || i == nx - 2);
     const long long sy = a.sy;
-    auto at = [&](int row) { return (long long)row * sy + ic; };
-    auto atr = [&](int row) { return (long long)row * sy + icr; };
-
-    // level-1 x face of row m (w' = face of the input state): all lanes
-    auto x1 = [&](int m, float d, float h, float D) {
-        float dr = __shfl_down_sync(FULL, d, 1);
-        float hr = __shfl_down_sync(FULL, h, 1);
-        float Dr = LS ? __shfl_down_sync(FULL, D, 1) : 0.0f;
-        if (L31) {
-            dr = a.din[atr(m)];
-            hr = a.Hf[atr(m)];
-            if (LS) Dr = a.Df[atr(m)];
-        }
-        float u;
-        return xf ? face32<MODEL, false>(a, d, dr, h, hr, D, Dr, a.win[0][at(m)], u) : 0.0f;
-    };
-    // star maximum of D around a cell (LINSTEP's iteration parameter)
-    auto dstar = [&](float Dc, float Db, float Dn, int m) {
-        if (!LS) return 0.0f;
-        float Dr = __shfl_down_sync(FULL, Dc, 1);
-        const float Dl = __shfl_up_sync(FULL, Dc, 1);
-        if (L31) Dr = a.Df[atr(m)];
-        return fmaxf(fmaxf(fmaxf(Dc, Dl), fmaxf(Dr, Db)), Dn);
-    };
-
-    // ---- prologue: level 1 of rows j0-1 and j0, level-2 face (j0-1/2)
-    const float dA = a.din[at(j0 - 1)], hA = a.Hf[at(j0 - 1)];
-    const float DA = LS ? a.Df[at(j0 - 1)] : 0.0f;
-    const float dB = a.din[at(j0)], hB = a.Hf[at(j0)];
-    const float DB = LS ? a.Df[at(j0)] : 0.0f;
-    float d1 = a.din[at(j0 + 1)], h1 = a.Hf[at(j0 + 1)];
-    float D1 = LS ? a.Df[at(j0 + 1)] : 0.0f;
     float u;
-    // w'_y(j0 - 1/2)
-    const float wyAB = upd1 ? face32<MODEL, false>(a, dA, dB, hA, hB, DA, DB, a.win[1][at(j0 - 1)], u) : 0.0f;
-    float pA = dA;   // delta'(j0 - 1)
-    float DZ = 0.0f; // D(j0 - 2)
-    if (j0 >= 2) {   // row j0 - 1 is interior: level 1 there
-        const float dZ = a.din[at(j0 - 2)], hZ = a.Hf[at(j0 - 2)];
-        DZ = LS ? a.Df[at(j0 - 2)] : 0.0f;
-        const float wyZA = upd1 ? face32<MODEL, false>(a, dZ, dA, hZ, hA, DZ, DA, a.win[1][at(j0 - 2)], u) : 0.0f;
-        const float wxA = x1(j0 - 1, dA, hA, DA);
+
+    // level-1 x face of the row at offset o (flux of the input state)
+    auto x1 = [&](long long o, float d, float h, float D) {
+        const float dr = __shfl_down_sync(FULL, d, 1);
+        const float hr = __shfl_down_sync(FULL, h, 1);
+        const float Dr = LS ? __shfl_down_sync(FULL, D, 1) : 0.0f;
+        return face32<MODEL, false>(a, d, dr, h, hr, D, Dr, a.win[0][o], u);
+    };
+
+    // ---- prologue: level 1 of rows j0-1 (A) and j0 (B), level-2 face (j0-1/2)
+    const long long oA = (long long)(j0 - 1) * sy + ic, oB = oA + sy, oC = oB + sy;
+    const float dA = a.din[oA], hA = a.Hf[oA];
+    const float DA = LS ? a.Df[oA] : 0.0f;
+    const float dB = a.din[oB], hB = a.Hf[oB];
+    const float DB = LS ? a.Df[oB] : 0.0f;
+    float d1 = a.din[oC], h1 = a.Hf[oC];   // row j0+1 <= ny-1
+    float D1 = LS ? a.Df[oC] : 0.0f;
+    const float wyAB = face32<MODEL, false>(a, dA, dB, hA, hB, DA, DB, a.win[1][oA], u);   // w'_y(j0-1/2)
+    float pA = dA;   // delta'(j0-1)
+    if (j0 >= 2) {   // row j0-1 is interior: level 1 there
+        const long long oZ = oA - sy;
+        const float dZ = a.din[oZ], hZ = a.Hf[oZ];
+        const float DZ = LS ? a.Df[oZ] : 0.0f;
+        const float wyZA = face32<MODEL, false>(a, dZ, dA, hZ, hA, DZ, DA, a.win[1][oZ], u);
+        const float wxA = x1(oA, dA, hA, DA);
         const float wxAl = __shfl_up_sync(FULL, wxA, 1);
-        const float eA = cell_e32<MODEL>(a, hA, dstar(DA, DZ, DB, j0 - 1));
-        if (upd1) pA = dc_update(a, dA, wxA, wxAl, wyAB, wyZA, a.r[at(j0 - 1)], eA);
+        const float eA = cell_e32<MODEL>(a, hA, dc_star<MODEL>(DA, DZ, DB));
+        if (upd1) pA = dc_update(a, dA, wxA, wxAl, wyAB, wyZA, a.r[oA], eA);
     }
-    // level 1 of row j0
-    float wx1p = x1(j0, dB, hB, DB);                                         // w'_x(j0)
-    float wy1p = upd1 ? face32<MODEL, false>(a, dB, d1, hB, h1, DB, D1, a.win[1][at(j0)], u) : 0.0f;  // w'_y(j0+1/2)
-    float p0 = dB;                                                           // delta'(j0)
+    float wx1p = x1(oB, dB, hB, DB);                                                  // w'_x(j0)
+    float wy1p = face32<MODEL, false>(a, dB, d1, hB, h1, DB, D1, a.win[1][oB], u);     // w'_y(j0+1/2)
+    float r0 = a.r[oB];
+    float p0 = dB;                                                                    // delta'(j0)
     {
         const float wxl = __shfl_up_sync(FULL, wx1p, 1);
-        const float eB = cell_e32<MODEL>(a, hB, dstar(DB, DA, D1, j0));
-        if (upd1) p0 = dc_update(a, dB, wx1p, wxl, wy1p, wyAB, a.r[at(j0)], eB);
+        const float eB = cell_e32<MODEL>(a, hB, dc_star<MODEL>(DB, DA, D1));
+        if (upd1) p0 = dc_update(a, dB, wx1p, wxl, wy1p, wyAB, r0, eB);
     }
-    // level-2 face w''_y(j0 - 1/2)
     float uy2b = 0.0f;
-    float wy2b = upd2 ? face32<MODEL, CHECK>(a, pA, p0, hA, hB, DA, DB, wyAB, uy2b) : 0.0f;
-    if (j0 == 1 && upd2) a.wout[1][at(0)] = wy2b;
+    float wy2b = face32<MODEL, CHECK>(a, pA, p0, hA, hB, DA, DB, wyAB, uy2b);   // w''_y(j0-1/2)
+    if (j0 == 1 && upd2) a.wout[1][oA] = wy2b;
     float h0 = hB, D0 = DB, Dm1 = DA;
-    float r0 = a.r[at(j0)];
 
     // ---- march: level 1 of row s+1, level 2 of row s
-    for (int s = j0; s < j1; ++s) {
-        const int m = s + 1;
+    long long o = oC;   // offset of row s+1
+    for (int s = j0; s < j1; ++s, o += sy) {
         float p1 = d1, wx1 = 0.0f, wy1 = 0.0f, r1 = 0.0f, h2 = h1, D2 = D1;
-        if (m <= ny - 2) {   // interior: level 1 of row m
-            const float d2 = a.din[at(m + 1)];
-            h2 = a.Hf[at(m + 1)];
-            if (LS) D2 = a.Df[at(m + 1)];
-            r1 = a.r[at(m)];
-            wx1 = x1(m, d1, h1, D1);
-            wy1 = upd1 ? face32<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][at(m)], u) : 0.0f;
+        if (s + 1 <= ny - 2) {   // row s+1 interior (uniform): level 1 there
+            const float d2 = a.din[o + sy];
+            h2 = a.Hf[o + sy];
+            if (LS) D2 = a.Df[o + sy];
+            r1 = a.r[o];
+            wx1 = x1(o, d1, h1, D1);
+            wy1 = face32<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], u);
             const float wx1l = __shfl_up_sync(FULL, wx1, 1);
-            const float e1 = cell_e32<MODEL>(a, h1, dstar(D1, D0, D2, m));
+            const float e1 = cell_e32<MODEL>(a, h1, dc_star<MODEL>(D1, D0, D2));
             if (upd1) p1 = dc_update(a, d1, wx1, wx1l, wy1, wy1p, r1, e1);
             d1 = d2;
         }
@@ -306,16 +295,17 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
         const float h0r = __shfl_down_sync(FULL, h0, 1);
         const float D0r = LS ? __shfl_down_sync(FULL, D0, 1) : 0.0f;
         float ux2 = 0.0f, uy2 = 0.0f;
-        const float wx2 = xf2 ? face32<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, ux2) : 0.0f;
-        const float wy2 = upd2 ? face32<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, uy2) : 0.0f;
+        const float wx2 = face32<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, ux2);
+        const float wy2 = face32<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, uy2);
         const float wx2l = __shfl_up_sync(FULL, wx2, 1);
         const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
-        const float e0 = cell_e32<MODEL>(a, h0, dstar(D0, Dm1, D1, s));
-        if (own_x) a.wout[0][at(s)] = wx2;
+        const float e0 = cell_e32<MODEL>(a, h0, dc_star<MODEL>(D0, Dm1, D1));
+        const long long os = o - sy;
+        if (own_x) a.wout[0][os] = wx2;
         if (upd2) {
             const float q = dc_update(a, p0, wx2, wx2l, wy2, wy2b, r0, e0);
-            a.dout[at(s)] = q;
-            a.wout[1][at(s)] = wy2;
+            a.dout[os] = q;
+            a.wout[1][os] = wy2;
             if (CHECK) {
                 const float divu = fmaf(uy2 - uy2b, a.sig[1], (ux2 - ux2l) * a.sig[0]);
                 accumulate_residual((double)fmaf(-q, a.rdt, r0 + divu), part, pmax);
