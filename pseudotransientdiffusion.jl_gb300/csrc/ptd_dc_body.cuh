@@ -60,9 +60,10 @@ __device__ __forceinline__ float face32(const DcArgs& a, float dL, float dR, flo
     } else {
         const float s = hL + hR;
         const float s2 = s * s;
-        uu = s2 * s * gd;
+        const float s3 = s2 * s;
+        uu = s3 * gd;
         uu = fmaf(3.0f * s2 * (hR - hL), dL + dR, uu);
-        c = nonlin_face_c(a.f, s);
+        c = nonlin_face_c3(a.f, 0.125f * s3);   // = nonlin_face_c(a.f, s)
     }
     if (U) u = uu;
     return fmaf(-c, w + uu, w);

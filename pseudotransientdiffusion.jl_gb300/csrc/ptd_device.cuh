@@ -119,14 +119,20 @@ __device__ __forceinline__ float fsqrt(float x)
 // NONLIN face: c = 1/(1+theta), theta = L*Resc/(Vpdtau*Re_f),
 // Re_f = pi + sqrt(pi^2 + L^2/(D_f dt)), D_f = ((h_L+h_R)/2)^3
 // (scripts/diff_2D_nonlin.jl:145-151).  D_f -> 0 gives Re_f -> inf, c -> 1.
-__device__ __forceinline__ float nonlin_face_c(const FParams& a, float hsum, float efac = 1.0f)
+__device__ __forceinline__ float nonlin_face_c3(const FParams& a, float df)
 {
-    float m = 0.5f * hsum;
-    float df = efac * m * m * m;
     float re = a.fpi + fsqrt(a.fpi2 + a.fA * frcp(df));
     float th = a.fk2 * frcp(re);
     return frcp(1.0f + th);
 }
+
+__device__ __forceinline__ float nonlin_face_c(const FParams& a, float hsum, float efac = 1.0f)
+{
+    float m = 0.5f * hsum;
+    return nonlin_face_c3(a, efac * m * m * m);
+}
+// (With s^3 = (s*s)*s already formed, 0.125f * s^3 is bit for bit the
+// D_f = m*m*m of m = s/2: scaling by powers of two commutes with rounding.)
 
 // NONLIN cell: e = 1/(1/dtau + 1/dt) with
 // 1/dtau = H^3 Re / (Vpdtau L Resc) = (pi H^3 + sqrt(pi^2 H^6 + L^2 H^3/dt)) * k1

@@ -93,13 +93,14 @@ __device__ __forceinline__ float rb_face(const RbArgs& a, float dL, float dR, fl
     } else {   // NONLIN, NONLIN_EXPM (D holds exp(m): K = (E_L + E_R) s^3, kappa 1/16)
         const float sb = hL + hR, sd = dL + dR, gb = hR - hL;
         const float st = sb + sd;
-        ud = fmaf(sd * fmaf(3.0f * sb, st, sd * sd), gb, st * st * st * gd);
+        const float st3 = st * st * st;
+        ud = fmaf(sd * fmaf(3.0f * sb, st, sd * sd), gb, st3 * gd);
         if (MODEL == NONLIN_EXPM) {
             const float e2 = DL + DR;
             ud *= e2;
             c = nonlin_face_c(a.f, st, 0.5f * e2);
         } else {
-            c = nonlin_face_c(a.f, st);
+            c = nonlin_face_c3(a.f, 0.125f * st3);   // = nonlin_face_c(a.f, st)
         }
     }
     if (U) u = ud;
@@ -262,11 +263,12 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     const float s0 = a.sig[0], s1 = a.sig[1], rdt = a.rdt;
     float u;
 
-    // level-1 x face of a row at offset o (flux omega of the input state)
-    auto x1 = [&](long long o, float d, float h, float D, float& tbx) {
+    // level-1 x face of a row at offset o (flux omega of the input state);
+    // hr, Dr: the right neighbour's H_b and D, reused by level 2
+    auto x1 = [&](long long o, float d, float h, float D, float& tbx, float& hr, float& Dr) {
         const float dr = __shfl_down_sync(FULL, d, 1);
-        const float hr = __shfl_down_sync(FULL, h, 1);
-        const float Dr = HASD ? __shfl_down_sync(FULL, D, 1) : 0.0f;
+        hr = __shfl_down_sync(FULL, h, 1);
+        Dr = HASD ? __shfl_down_sync(FULL, D, 1) : 0.0f;
         tbx = a.tb[0][o];
         return rb_face<MODEL, false>(a, d, dr, h, hr, D, Dr, a.win[0][o], tbx, u);
     };
@@ -290,14 +292,14 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         const float dZ = a.din[oZ], hZ = a.Hf[oZ];
         const float DZ = HASD ? a.Df[oZ] : 0.0f;
         const float wyZA = rb_face<MODEL, false>(a, dZ, dA, hZ, hA, DZ, DA, a.win[1][oZ], a.tb[1][oZ], u);
-        float tbxA;
-        const float wxA = x1(oA, dA, hA, DA, tbxA);
+        float tbxA, hAr, DAr;
+        const float wxA = x1(oA, dA, hA, DA, tbxA, hAr, DAr);
         const float wxAl = __shfl_up_sync(FULL, wxA, 1);
         const float eA = rb_cell_e<MODEL>(a, hA + dA, rb_star<MODEL>(DA, DZ, DB));
         if (upd1) pA = cell(dA, eA, a.Rb[oA], wxA, wxAl, wyAB, wyZA);
     }
-    float tbx0;
-    float wx1p = x1(oB, dB, hB, DB, tbx0);                 // omega'_x(j0)
+    float tbx0, h0r, D0r;
+    float wx1p = x1(oB, dB, hB, DB, tbx0, h0r, D0r);       // omega'_x(j0)
     float tby0 = a.tb[1][oB];
     float wy1p = rb_face<MODEL, false>(a, dB, d1, hB, h1, DB, D1, a.win[1][oB], tby0, u);  // omega'_y(j0+1/2)
     float r0 = a.Rb[oB];
@@ -316,13 +318,14 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     long long o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float p1 = d1, wx1 = 0.0f, wy1 = 0.0f, r1 = 0.0f, h2 = h1, D2 = D1, tbx1 = 0.0f, tby1 = 0.0f;
+        float h1r = h1, D1r = D1;
         if (s + 1 <= ny - 2) {   // row s+1 interior (uniform): level 1 there
             const float d2 = a.din[o + sy];
             h2 = a.Hf[o + sy];
             if (HASD) D2 = a.Df[o + sy];
             r1 = a.Rb[o];
             tby1 = a.tb[1][o];
-            wx1 = x1(o, d1, h1, D1, tbx1);
+            wx1 = x1(o, d1, h1, D1, tbx1, h1r, D1r);
             wy1 = rb_face<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], tby1, u);
             const float wx1l = __shfl_up_sync(FULL, wx1, 1);
             const float e1 = rb_cell_e<MODEL>(a, h1 + d1, rb_star<MODEL>(D1, D0, D2));
@@ -331,8 +334,6 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         }
         // level 2 of row s
         const float p0r = __shfl_down_sync(FULL, p0, 1);
-        const float h0r = __shfl_down_sync(FULL, h0, 1);
-        const float D0r = HASD ? __shfl_down_sync(FULL, D0, 1) : 0.0f;
         float ux2 = 0.0f, uy2 = 0.0f;
         const float wx2 = rb_face<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, tbx0, ux2);
         const float wy2 = rb_face<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, tby0, uy2);
@@ -360,9 +361,11 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         wy2b = wy2;
         uy2b = uy2;
         h0 = h1;
+        h0r = h1r;
         h1 = h2;
         Dm1 = D0;
         D0 = D1;
+        D0r = D1r;
         D1 = D2;
     }
 }
