@@ -1,7 +1,7 @@
 """Benchmark of the accelerated PT diffusion solver (T_eff, the reference's metric).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload 2d_nonlin_4096]
-                    [--precision fp64|dfh|df64|fp32_dc] [--impl ours|reference]
+                    [--precision fp64|dfh|df64|fp32_dc|fp32_rb] [--impl ours|reference]
 
 Workload (default): 2D nonlinear diffusion D = H^3 on 4096^2 cells, 10x10
 domain, H0 = 1 + exp(-r^2), H = 1 on the boundary, dt = 0.2, tol = 1e-8,
@@ -73,9 +73,9 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(workload: str):
+def profile_traffic(workload: str, summary: str = None):
     """dram bytes per launch of the dominant kernel, from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"pt_kernel_{workload}.md")
+    path = os.path.join(ROOT, "profiles", summary or f"pt_kernel_{workload}.md")
     try:
         with open(path) as fh:
             for ln in fh:
@@ -458,6 +458,17 @@ def run_ours(args, world, rank, local, pg):
     achieved = A / t_launch / 1e9
     peak, peak_kind = read_peaks()
     traffic = profile_traffic(args.workload)
+    kernel_name, kernel_bytes, launch_t = f"pt{s.ndim}d_kernel (fused PT iteration)", A, t_launch
+    if args.precision == "fp32_rb":
+        # the rebased FP32 kernel: 40 B per cell in 2D (52 in 3D) per launch,
+        # two iterations per launch in 2D when the check cadence is even
+        ipl = 2 if (s.ndim == 2 and params.nchk % 2 == 0) else 1
+        kernel_bytes = (2 + 3 * s.ndim + 2) * 4 * float(np.prod(shape))
+        launch_t = t_launch * ipl
+        achieved = kernel_bytes / launch_t / 1e9
+        kernel_name = f"rb{s.ndim}d{'_tb2' if ipl == 2 else ''}_kernel ({ipl} FP32 iterations per launch)"
+        traffic = profile_traffic(args.workload, "rb2d_fp32rb_nonlin_4096.md") if (
+            args.workload == "2d_nonlin_4096" and ipl == 2) else None
     sol.close()
     # the native-FP64 kernel's own roofline: FP64 instructions per cell x
     # cells / launch time against this GPU's FP64 FMA rate, measured now
@@ -552,24 +563,34 @@ def run_ours(args, world, rank, local, pg):
         ttt["speedup"] = ttt["fp32_rb"]["speedup"]
 
     # ---- e2e: ptd_solve on pinned host buffers, one physical step per call
-    pe = ptdiff.make_params(s, shape, nt=1, precision=args.precision)
-    sol2 = ptdiff.Solver(pe)
     pin = torch.empty(H0.size, dtype=torch.float64, pin_memory=True)
     Hh = pin.numpy()
-    for _ in range(args.warmup):
-        Hh[:] = np.ravel(H0, order="F")
-        sol2.solve(Hh)
-    barrier(pg)
-    e2e_time, e2e_iters = 0.0, 0
-    for _ in range(args.steps):
-        Hh[:] = np.ravel(H0, order="F")
-        t0 = time.perf_counter()
-        its, _, _ = sol2.solve(Hh)
-        e2e_time += time.perf_counter() - t0
-        e2e_iters += int(its.sum())
-    sol2.close()
-    e2e_t = reduce_max(pg, e2e_time)
+
+    def e2e_run(precision):
+        sol2 = ptdiff.Solver(ptdiff.make_params(s, shape, nt=1, precision=precision))
+        for _ in range(args.warmup):
+            Hh[:] = np.ravel(H0, order="F")
+            sol2.solve(Hh)
+        barrier(pg)
+        e2e_time, e2e_iters = 0.0, 0
+        for _ in range(args.steps):
+            Hh[:] = np.ravel(H0, order="F")
+            t0 = time.perf_counter()
+            its, _, _ = sol2.solve(Hh)
+            e2e_time += time.perf_counter() - t0
+            e2e_iters += int(its.sum())
+        sol2.close()
+        return reduce_max(pg, e2e_time), e2e_iters
+
+    e2e_t, e2e_iters = e2e_run(args.precision)
     e2e_val = reduce_sum(pg, A * e2e_iters) / e2e_t / 1e9
+    if ttt is not None:
+        # time to tol end to end: H0 uploaded from and H downloaded to pinned
+        # host memory inside every timed ptd_solve call
+        t_rb, _ = e2e_run("fp32_rb")
+        ttt["fp32_rb"]["e2e_ms_per_step"] = round(t_rb / args.steps * 1e3, 3)
+        ttt["fp64_e2e_ms_per_step"] = round(e2e_t / args.steps * 1e3, 3)
+        ttt["e2e_speedup"] = round(e2e_t / t_rb, 3)
 
     if rank != 0:
         return 0
@@ -583,7 +604,7 @@ def run_ours(args, world, rank, local, pg):
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": round(value / pub, 3) if pub else None,
         "dtype": {"fp64": "f64", "df64": "df64 (f32x2)", "dfh": "f64 state, df64 (f32x2) arithmetic",
-                  "fp32_dc": "f32 inner + f64 outer"}[args.precision],
+                  "fp32_dc": "f32 inner + f64 outer", "fp32_rb": "f32 changes on an f64 base"}[args.precision],
         "data": "synthetic",
         "config": {"workload": args.workload, "shape": list(shape), "precision": args.precision,
                    "nchk": s.nout, "tol": s.tol, "dt": s.dt, "step": "one physical time step to tol",
@@ -591,8 +612,8 @@ def run_ours(args, world, rank, local, pg):
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "peak_kind": peak_kind, "kernel": f"pt{s.ndim}d_kernel (fused PT iteration)",
-                     "launch_us": round(t_launch * 1e6, 2), "algorithmic_bytes_per_launch": A},
+                     "peak_kind": peak_kind, "kernel": kernel_name,
+                     "launch_us": round(launch_t * 1e6, 2), "algorithmic_bytes_per_launch": kernel_bytes},
         "fp64_pipe": fp64_pipe,
         "cpu_baseline": cb,
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": int(H0.size * 8),
@@ -615,7 +636,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="2d_nonlin_4096")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "dfh", "fp32_dc"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "dfh", "fp32_dc", "fp32_rb"])
     ap.add_argument("--n", type=int, default=0, help="override the grid size (testing)")
     ap.add_argument("--fixed-iters", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
