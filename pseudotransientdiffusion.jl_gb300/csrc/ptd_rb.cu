@@ -259,13 +259,13 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     const bool xf2 = i >= 0 && i <= nx - 2 && lane >= 1 && lane <= 29;
     const bool upd2 = colin && lane >= 2 && lane <= 29;
     const bool own_x = xf2 && (lane <= 28 || i == nx - 2);   // face i+1/2 of lane 29: the next tile's lane 1
-    const long long sy = a.sy;
+    const int sy = (int)a.sy;   // 32-bit offsets: the host runs this body only for fields below 2^31 cells
     const float s0 = a.sig[0], s1 = a.sig[1], rdt = a.rdt;
     float u;
 
     // level-1 x face of a row at offset o (flux omega of the input state);
     // hr, Dr: the right neighbour's H_b and D, reused by level 2
-    auto x1 = [&](long long o, float d, float h, float D, float& tbx, float& hr, float& Dr) {
+    auto x1 = [&](int o, float d, float h, float D, float& tbx, float& hr, float& Dr) {
         const float dr = __shfl_down_sync(FULL, d, 1);
         hr = __shfl_down_sync(FULL, h, 1);
         Dr = HASD ? __shfl_down_sync(FULL, D, 1) : 0.0f;
@@ -277,7 +277,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     };
 
     // ---- prologue: level 1 of rows j0-1 (A) and j0 (B), level-2 face j0-1/2
-    const long long oA = (long long)(j0 - 1) * sy + ic, oB = oA + sy, oC = oB + sy;
+    const int oA = (j0 - 1) * sy + ic, oB = oA + sy, oC = oB + sy;
     const float dA = a.din[oA], hA = a.Hf[oA];
     const float DA = HASD ? a.Df[oA] : 0.0f;
     const float dB = a.din[oB], hB = a.Hf[oB];
@@ -288,7 +288,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     const float wyAB = rb_face<MODEL, false>(a, dA, dB, hA, hB, DA, DB, a.win[1][oA], tbyA, u);  // omega'_y(j0-1/2)
     float pA = dA;                          // delta'(j0-1)
     if (j0 >= 2) {                          // row j0-1 is interior: level 1 there
-        const long long oZ = oA - sy;
+        const int oZ = oA - sy;
         const float dZ = a.din[oZ], hZ = a.Hf[oZ];
         const float DZ = HASD ? a.Df[oZ] : 0.0f;
         const float wyZA = rb_face<MODEL, false>(a, dZ, dA, hZ, hA, DZ, DA, a.win[1][oZ], a.tb[1][oZ], u);
@@ -315,7 +315,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     float h0 = hB, D0 = DB, Dm1 = DA;
 
     // ---- march: level 1 of row s+1, level 2 of row s
-    long long o = oC;   // offset of row s+1
+    int o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float p1 = d1, wx1 = 0.0f, wy1 = 0.0f, r1 = 0.0f, h2 = h1, D2 = D1, tbx1 = 0.0f, tby1 = 0.0f;
         float h1r = h1, D1r = D1;
@@ -340,7 +340,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         const float wx2l = __shfl_up_sync(FULL, wx2, 1);
         const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
         const float e0 = rb_cell_e<MODEL>(a, h0 + p0, rb_star<MODEL>(D0, Dm1, D1));
-        const long long os = o - sy;
+        const int os = o - sy;
         if (own_x) a.wout[0][os] = wx2;
         if (upd2) {
             const float q = cell(p0, e0, r0, wx2, wx2l, wy2, wy2b);
@@ -945,7 +945,9 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     rb->cfg = tuned_config(p);
     // a phase: the check blocks of ~200 PT iterations between two FP64 rebases
     rb->blocks_per_phase = std::max(1, (200 + p.nchk - 1) / p.nchk);
-    rb->tblk = (p.ndim == 2 && p.nchk % 2 == 0 && !(p.flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
+    rb->tblk = (p.ndim == 2 && p.nchk % 2 == 0 && !(p.flags & PTD_FLAG_DC_NO_TBLOCK) && g.nfield < (1ll << 31))
+                   ? 2
+                   : 1;
     rb->errcap = (p.nchk <= p.itmax ? p.itmax / p.nchk : 0) + 2;
     const size_t fb = (size_t)g.nfield * sizeof(float);
     auto alloc = [&](void** ptr, size_t n) -> int {
