@@ -77,6 +77,26 @@ struct RbDev {
     double err64;     // last FP64 err
 };
 
+// Iteration parameters of the rebased kernels, every operation explicit (no
+// contraction left to the compiler), so that the scalar forms below and the
+// packed two-lane forms (f32x2, rb2d_tb2_body) round identically.
+// Face: c = 1/(1 + fk2/Re_f), Re_f = pi + sqrt(pi^2 + fA/D_f); cell:
+// e = 1/((pi H^3 + sqrt(pi^2 H^6 + fA H^3)) k1 + 1/dt) (the formulas of
+// nonlin_face_c / nonlin_cell_e, scripts/diff_2D_nonlin.jl:145-152).
+__device__ __forceinline__ float rb_c(const FParams& f, float df)
+{
+    const float q = __fmaf_rn(f.fA, frcp(df), f.fpi2);
+    const float re = __fadd_rn(f.fpi, fsqrt(q));
+    return frcp(__fmaf_rn(f.fk2, frcp(re), 1.0f));
+}
+
+__device__ __forceinline__ float rb_e(const FParams& f, float h3)
+{
+    const float q = __fmaf_rn(__fmul_rn(f.fpi2, h3), h3, __fmul_rn(f.fA, h3));
+    const float p = __fmaf_rn(f.fpi, h3, fsqrt(q));
+    return frcp(__fmaf_rn(p, f.fk1, f.frdt));
+}
+
 // One face: new omega, and u_d (the change of the undamped flux) when U.
 template <int MODEL, bool U>
 __device__ __forceinline__ float rb_face(const RbArgs& a, float dL, float dR, float hL, float hR, float DL,
@@ -88,23 +108,25 @@ __device__ __forceinline__ float rb_face(const RbArgs& a, float dL, float dR, fl
         ud = gd;
         c = a.c_lin;
     } else if (MODEL == LINSTEP) {
-        ud = (DL + DR) * gd;
+        ud = __fmul_rn(DL + DR, gd);
         c = a.c_lin;
     } else {   // NONLIN, NONLIN_EXPM (D holds exp(m): K = (E_L + E_R) s^3, kappa 1/16)
         const float sb = hL + hR, sd = dL + dR, gb = hR - hL;
         const float st = sb + sd;
-        const float st3 = st * st * st;
-        ud = fmaf(sd * fmaf(3.0f * sb, st, sd * sd), gb, st3 * gd);
+        const float st3 = __fmul_rn(__fmul_rn(st, st), st);
+        ud = __fmaf_rn(__fmul_rn(sd, __fmaf_rn(__fmul_rn(3.0f, sb), st, __fmul_rn(sd, sd))), gb,
+                       __fmul_rn(st3, gd));
         if (MODEL == NONLIN_EXPM) {
             const float e2 = DL + DR;
-            ud *= e2;
-            c = nonlin_face_c(a.f, st, 0.5f * e2);
+            ud = __fmul_rn(ud, e2);
+            const float m = __fmul_rn(0.5f, st);
+            c = rb_c(a.f, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(0.5f, e2), m), m), m));
         } else {
-            c = nonlin_face_c3(a.f, 0.125f * st3);   // = nonlin_face_c(a.f, st)
+            c = rb_c(a.f, __fmul_rn(0.125f, st3));   // D_f = (st/2)^3
         }
     }
     if (U) u = ud;
-    return fmaf(-c, w + (tb + ud), w);
+    return __fmaf_rn(-c, w + (tb + ud), w);
 }
 
 template <int MODEL>
@@ -112,8 +134,73 @@ __device__ __forceinline__ float rb_cell_e(const RbArgs& a, float h, float dmax)
 {
     if (MODEL == LIN) return a.e_lin;
     if (MODEL == LINSTEP) return linstep_cell_e(a.f, dmax);
-    if (MODEL == NONLIN_EXPM) return nonlin_cell_e(a.f, h, dmax);   // dmax carries exp(m) of the cell
-    return nonlin_cell_e(a.f, h);
+    float h3 = __fmul_rn(__fmul_rn(h, h), h);
+    if (MODEL == NONLIN_EXPM) h3 = __fmul_rn(__fmul_rn(__fmul_rn(dmax, h), h), h);   // dmax carries exp(m)
+    return rb_e(a.f, h3);
+}
+
+// ---- the same on two lanes at once (FP32x2 instructions: two faces or two
+// cells per instruction, each component rounded exactly like the scalar form)
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }   // a - b
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rcp2(float2 x) { return f2(frcp(x.x), frcp(x.y)); }
+__device__ __forceinline__ float2 sqrt2(float2 x) { return f2(fsqrt(x.x), fsqrt(x.y)); }
+
+__device__ __forceinline__ float2 rb_c2(const FParams& f, float2 df)
+{
+    const float2 q = fma2(f2(f.fA), rcp2(df), f2(f.fpi2));
+    const float2 re = add2(f2(f.fpi), sqrt2(q));
+    return rcp2(fma2(f2(f.fk2), rcp2(re), f2(1.0f)));
+}
+
+__device__ __forceinline__ float2 rb_e2(const FParams& f, float2 h3)
+{
+    const float2 q = fma2(mul2(f2(f.fpi2), h3), h3, mul2(f2(f.fA), h3));
+    const float2 p = fma2(f2(f.fpi), h3, sqrt2(q));
+    return rcp2(fma2(p, f2(f.fk1), f2(f.frdt)));
+}
+
+template <int MODEL, bool U>
+__device__ __forceinline__ float2 rb_face2(const RbArgs& a, float2 dL, float2 dR, float2 hL, float2 hR, float2 DL,
+                                           float2 DR, float2 w, float2 tb, float2& u)
+{
+    const float2 gd = sub2(dR, dL);
+    float2 ud, c;
+    if (MODEL == LIN) {
+        ud = gd;
+        c = f2(a.c_lin);
+    } else if (MODEL == LINSTEP) {
+        ud = mul2(add2(DL, DR), gd);
+        c = f2(a.c_lin);
+    } else {
+        const float2 sb = add2(hL, hR), sd = add2(dL, dR), gb = sub2(hR, hL);
+        const float2 st = add2(sb, sd);
+        const float2 st3 = mul2(mul2(st, st), st);
+        ud = fma2(mul2(sd, fma2(mul2(f2(3.0f), sb), st, mul2(sd, sd))), gb, mul2(st3, gd));
+        if (MODEL == NONLIN_EXPM) {
+            const float2 e2 = add2(DL, DR);
+            ud = mul2(ud, e2);
+            const float2 m = mul2(f2(0.5f), st);
+            c = rb_c2(a.f, mul2(mul2(mul2(mul2(f2(0.5f), e2), m), m), m));
+        } else {
+            c = rb_c2(a.f, mul2(f2(0.125f), st3));
+        }
+    }
+    if (U) u = ud;
+    return fma2(f2(-c.x, -c.y), add2(w, add2(tb, ud)), w);
+}
+
+// e of two cells (NONLIN, NONLIN_EXPM; E: exp(m) of the cells)
+template <int MODEL>
+__device__ __forceinline__ float2 rb_cell_e2(const RbArgs& a, float2 h, float2 E)
+{
+    float2 h3 = mul2(mul2(h, h), h);
+    if (MODEL == NONLIN_EXPM) h3 = mul2(mul2(mul2(E, h), h), h);
+    return rb_e2(a.f, h3);
 }
 
 __device__ __forceinline__ bool rb_skip(const int* skip) { return __ldcg(skip) != 0; }
@@ -314,32 +401,65 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     if (j0 == 1 && upd2) a.wout[1][oA] = wy2b;
     float h0 = hB, D0 = DB, Dm1 = DA;
 
-    // ---- march: level 1 of row s+1, level 2 of row s
+    // ---- march: level 1 of row s+1, level 2 of row s.  LIN, NONLIN: the x
+    // and y faces of a level are one two-lane (f32x2) evaluation, as is the
+    // pair of cell parameters e of the two levels (NONLIN); the models with a
+    // coefficient field keep the scalar forms (the packed ones did not
+    // reproduce the one-iteration kernel bit for bit there).
+    constexpr bool PACKF = MODEL == LIN || MODEL == NONLIN;
+    constexpr bool PACKE = MODEL == NONLIN;
     int o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float p1 = d1, wx1 = 0.0f, wy1 = 0.0f, r1 = 0.0f, h2 = h1, D2 = D1, tbx1 = 0.0f, tby1 = 0.0f;
-        float h1r = h1, D1r = D1;
+        float h1r = h1, D1r = D1, e1 = 0.0f, e0 = 0.0f;
+        if (PACKE) {   // e of row s+1 (level 1, unused on the last row) and of row s (level 2)
+            const float2 ee = rb_cell_e2<MODEL>(a, add2(f2(h1, h0), f2(d1, p0)), f2(D1, D0));
+            e1 = ee.x;
+            e0 = ee.y;
+        }
         if (s + 1 <= ny - 2) {   // row s+1 interior (uniform): level 1 there
             const float d2 = a.din[o + sy];
             h2 = a.Hf[o + sy];
             if (HASD) D2 = a.Df[o + sy];
             r1 = a.Rb[o];
+            tbx1 = a.tb[0][o];
             tby1 = a.tb[1][o];
-            wx1 = x1(o, d1, h1, D1, tbx1, h1r, D1r);
-            wy1 = rb_face<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], tby1, u);
+            const float d1r = __shfl_down_sync(FULL, d1, 1);
+            h1r = __shfl_down_sync(FULL, h1, 1);
+            if (HASD) D1r = __shfl_down_sync(FULL, D1, 1);
+            if (PACKF) {
+                float2 uu;
+                const float2 w1 = rb_face2<MODEL, false>(a, f2(d1), f2(d1r, d2), f2(h1), f2(h1r, h2), f2(D1),
+                                                         f2(D1r, D2), f2(a.win[0][o], a.win[1][o]), f2(tbx1, tby1), uu);
+                wx1 = w1.x;
+                wy1 = w1.y;
+            } else {
+                wx1 = rb_face<MODEL, false>(a, d1, d1r, h1, h1r, D1, D1r, a.win[0][o], tbx1, u);
+                wy1 = rb_face<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], tby1, u);
+            }
             const float wx1l = __shfl_up_sync(FULL, wx1, 1);
-            const float e1 = rb_cell_e<MODEL>(a, h1 + d1, rb_star<MODEL>(D1, D0, D2));
+            if (!PACKE) e1 = rb_cell_e<MODEL>(a, h1 + d1, rb_star<MODEL>(D1, D0, D2));
             if (upd1) p1 = cell(d1, e1, r1, wx1, wx1l, wy1, wy1p);
             d1 = d2;
         }
         // level 2 of row s
         const float p0r = __shfl_down_sync(FULL, p0, 1);
-        float ux2 = 0.0f, uy2 = 0.0f;
-        const float wx2 = rb_face<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, tbx0, ux2);
-        const float wy2 = rb_face<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, tby0, uy2);
+        float wx2, wy2, ux2 = 0.0f, uy2 = 0.0f;
+        if (PACKF) {
+            float2 u2 = f2(0.0f);
+            const float2 w2 = rb_face2<MODEL, CHECK>(a, f2(p0), f2(p0r, p1), f2(h0), f2(h0r, h1), f2(D0), f2(D0r, D1),
+                                                     f2(wx1p, wy1p), f2(tbx0, tby0), u2);
+            wx2 = w2.x;
+            wy2 = w2.y;
+            ux2 = u2.x;
+            uy2 = u2.y;
+        } else {
+            wx2 = rb_face<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, tbx0, ux2);
+            wy2 = rb_face<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, tby0, uy2);
+        }
         const float wx2l = __shfl_up_sync(FULL, wx2, 1);
         const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
-        const float e0 = rb_cell_e<MODEL>(a, h0 + p0, rb_star<MODEL>(D0, Dm1, D1));
+        if (!PACKE) e0 = rb_cell_e<MODEL>(a, h0 + p0, rb_star<MODEL>(D0, Dm1, D1));
         const int os = o - sy;
         if (own_x) a.wout[0][os] = wx2;
         if (upd2) {
