@@ -139,68 +139,39 @@ __device__ __forceinline__ float rb_cell_e(const RbArgs& a, float h, float dmax)
     return rb_e(a.f, h3);
 }
 
-// ---- the same on two lanes at once (FP32x2 instructions: two faces or two
-// cells per instruction, each component rounded exactly like the scalar form)
+// ---- the same on two lanes at once (FP32x2 instructions: two faces per
+// instruction, each component rounded exactly like the scalar form)
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }   // a - b
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 rcp2(float2 x) { return f2(frcp(x.x), frcp(x.y)); }
-__device__ __forceinline__ float2 sqrt2(float2 x) { return f2(fsqrt(x.x), fsqrt(x.y)); }
 
-__device__ __forceinline__ float2 rb_c2(const FParams& f, float2 df)
-{
-    const float2 q = fma2(f2(f.fA), rcp2(df), f2(f.fpi2));
-    const float2 re = add2(f2(f.fpi), sqrt2(q));
-    return rcp2(fma2(f2(f.fk2), rcp2(re), f2(1.0f)));
-}
-
-__device__ __forceinline__ float2 rb_e2(const FParams& f, float2 h3)
-{
-    const float2 q = fma2(mul2(f2(f.fpi2), h3), h3, mul2(f2(f.fA), h3));
-    const float2 p = fma2(f2(f.fpi), h3, sqrt2(q));
-    return rcp2(fma2(p, f2(f.fk1), f2(f.frdt)));
-}
-
+// Two faces: the flux arithmetic packed, the iteration parameters c (MUFU
+// work with constant operands, which scalar instructions take for free)
+// scalar.  3 sb is formed as (sb + sb) + sb: sb + sb is exact, so the sum
+// rounds once, like the scalar 3.0f * sb.
 template <int MODEL, bool U>
 __device__ __forceinline__ float2 rb_face2(const RbArgs& a, float2 dL, float2 dR, float2 hL, float2 hR, float2 DL,
                                            float2 DR, float2 w, float2 tb, float2& u)
 {
     const float2 gd = sub2(dR, dL);
-    float2 ud, c;
+    float2 ud;
+    float cx, cy;
     if (MODEL == LIN) {
         ud = gd;
-        c = f2(a.c_lin);
-    } else if (MODEL == LINSTEP) {
-        ud = mul2(add2(DL, DR), gd);
-        c = f2(a.c_lin);
-    } else {
+        cx = cy = a.c_lin;
+    } else {   // NONLIN
         const float2 sb = add2(hL, hR), sd = add2(dL, dR), gb = sub2(hR, hL);
         const float2 st = add2(sb, sd);
         const float2 st3 = mul2(mul2(st, st), st);
-        ud = fma2(mul2(sd, fma2(mul2(f2(3.0f), sb), st, mul2(sd, sd))), gb, mul2(st3, gd));
-        if (MODEL == NONLIN_EXPM) {
-            const float2 e2 = add2(DL, DR);
-            ud = mul2(ud, e2);
-            const float2 m = mul2(f2(0.5f), st);
-            c = rb_c2(a.f, mul2(mul2(mul2(mul2(f2(0.5f), e2), m), m), m));
-        } else {
-            c = rb_c2(a.f, mul2(f2(0.125f), st3));
-        }
+        ud = fma2(mul2(sd, fma2(add2(add2(sb, sb), sb), st, mul2(sd, sd))), gb, mul2(st3, gd));
+        cx = rb_c(a.f, __fmul_rn(0.125f, st3.x));
+        cy = rb_c(a.f, __fmul_rn(0.125f, st3.y));
     }
     if (U) u = ud;
-    return fma2(f2(-c.x, -c.y), add2(w, add2(tb, ud)), w);
-}
-
-// e of two cells (NONLIN, NONLIN_EXPM; E: exp(m) of the cells)
-template <int MODEL>
-__device__ __forceinline__ float2 rb_cell_e2(const RbArgs& a, float2 h, float2 E)
-{
-    float2 h3 = mul2(mul2(h, h), h);
-    if (MODEL == NONLIN_EXPM) h3 = mul2(mul2(mul2(E, h), h), h);
-    return rb_e2(a.f, h3);
+    return fma2(f2(-cx, -cy), add2(w, add2(tb, ud)), w);
 }
 
 __device__ __forceinline__ bool rb_skip(const int* skip) { return __ldcg(skip) != 0; }
@@ -346,13 +317,13 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     const bool xf2 = i >= 0 && i <= nx - 2 && lane >= 1 && lane <= 29;
     const bool upd2 = colin && lane >= 2 && lane <= 29;
     const bool own_x = xf2 && (lane <= 28 || i == nx - 2);   // face i+1/2 of lane 29: the next tile's lane 1
-    const int sy = (int)a.sy;   // 32-bit offsets: the host runs this body only for fields below 2^31 cells
+    const long long sy = a.sy;
     const float s0 = a.sig[0], s1 = a.sig[1], rdt = a.rdt;
     float u;
 
     // level-1 x face of a row at offset o (flux omega of the input state);
     // hr, Dr: the right neighbour's H_b and D, reused by level 2
-    auto x1 = [&](int o, float d, float h, float D, float& tbx, float& hr, float& Dr) {
+    auto x1 = [&](long long o, float d, float h, float D, float& tbx, float& hr, float& Dr) {
         const float dr = __shfl_down_sync(FULL, d, 1);
         hr = __shfl_down_sync(FULL, h, 1);
         Dr = HASD ? __shfl_down_sync(FULL, D, 1) : 0.0f;
@@ -364,7 +335,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     };
 
     // ---- prologue: level 1 of rows j0-1 (A) and j0 (B), level-2 face j0-1/2
-    const int oA = (j0 - 1) * sy + ic, oB = oA + sy, oC = oB + sy;
+    const long long oA = (long long)(j0 - 1) * sy + ic, oB = oA + sy, oC = oB + sy;
     const float dA = a.din[oA], hA = a.Hf[oA];
     const float DA = HASD ? a.Df[oA] : 0.0f;
     const float dB = a.din[oB], hB = a.Hf[oB];
@@ -375,7 +346,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     const float wyAB = rb_face<MODEL, false>(a, dA, dB, hA, hB, DA, DB, a.win[1][oA], tbyA, u);  // omega'_y(j0-1/2)
     float pA = dA;                          // delta'(j0-1)
     if (j0 >= 2) {                          // row j0-1 is interior: level 1 there
-        const int oZ = oA - sy;
+        const long long oZ = oA - sy;
         const float dZ = a.din[oZ], hZ = a.Hf[oZ];
         const float DZ = HASD ? a.Df[oZ] : 0.0f;
         const float wyZA = rb_face<MODEL, false>(a, dZ, dA, hZ, hA, DZ, DA, a.win[1][oZ], a.tb[1][oZ], u);
@@ -402,21 +373,16 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
     float h0 = hB, D0 = DB, Dm1 = DA;
 
     // ---- march: level 1 of row s+1, level 2 of row s.  LIN, NONLIN: the x
-    // and y faces of a level are one two-lane (f32x2) evaluation, as is the
-    // pair of cell parameters e of the two levels (NONLIN); the models with a
-    // coefficient field keep the scalar forms (the packed ones did not
-    // reproduce the one-iteration kernel bit for bit there).
+    // and y faces of a level are one two-lane (f32x2) evaluation of the flux
+    // arithmetic; the models with a coefficient field keep the scalar faces
+    // (the packed ones did not reproduce the one-iteration kernel bit for bit
+    // there).  (Packing the iteration parameters too, whose constant operands
+    // scalar instructions take for free, was slower: 81.2 against 77.9 us.)
     constexpr bool PACKF = MODEL == LIN || MODEL == NONLIN;
-    constexpr bool PACKE = MODEL == NONLIN;
-    int o = oC;   // offset of row s+1
+    long long o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float p1 = d1, wx1 = 0.0f, wy1 = 0.0f, r1 = 0.0f, h2 = h1, D2 = D1, tbx1 = 0.0f, tby1 = 0.0f;
-        float h1r = h1, D1r = D1, e1 = 0.0f, e0 = 0.0f;
-        if (PACKE) {   // e of row s+1 (level 1, unused on the last row) and of row s (level 2)
-            const float2 ee = rb_cell_e2<MODEL>(a, add2(f2(h1, h0), f2(d1, p0)), f2(D1, D0));
-            e1 = ee.x;
-            e0 = ee.y;
-        }
+        float h1r = h1, D1r = D1;
         if (s + 1 <= ny - 2) {   // row s+1 interior (uniform): level 1 there
             const float d2 = a.din[o + sy];
             h2 = a.Hf[o + sy];
@@ -438,7 +404,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
                 wy1 = rb_face<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], tby1, u);
             }
             const float wx1l = __shfl_up_sync(FULL, wx1, 1);
-            if (!PACKE) e1 = rb_cell_e<MODEL>(a, h1 + d1, rb_star<MODEL>(D1, D0, D2));
+            const float e1 = rb_cell_e<MODEL>(a, h1 + d1, rb_star<MODEL>(D1, D0, D2));
             if (upd1) p1 = cell(d1, e1, r1, wx1, wx1l, wy1, wy1p);
             d1 = d2;
         }
@@ -459,8 +425,8 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         }
         const float wx2l = __shfl_up_sync(FULL, wx2, 1);
         const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
-        if (!PACKE) e0 = rb_cell_e<MODEL>(a, h0 + p0, rb_star<MODEL>(D0, Dm1, D1));
-        const int os = o - sy;
+        const float e0 = rb_cell_e<MODEL>(a, h0 + p0, rb_star<MODEL>(D0, Dm1, D1));
+        const long long os = o - sy;
         if (own_x) a.wout[0][os] = wx2;
         if (upd2) {
             const float q = cell(p0, e0, r0, wx2, wx2l, wy2, wy2b);
@@ -1065,9 +1031,7 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     rb->cfg = tuned_config(p);
     // a phase: the check blocks of ~200 PT iterations between two FP64 rebases
     rb->blocks_per_phase = std::max(1, (200 + p.nchk - 1) / p.nchk);
-    rb->tblk = (p.ndim == 2 && p.nchk % 2 == 0 && !(p.flags & PTD_FLAG_DC_NO_TBLOCK) && g.nfield < (1ll << 31))
-                   ? 2
-                   : 1;
+    rb->tblk = (p.ndim == 2 && p.nchk % 2 == 0 && !(p.flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
     rb->errcap = (p.nchk <= p.itmax ? p.itmax / p.nchk : 0) + 2;
     const size_t fb = (size_t)g.nfield * sizeof(float);
     auto alloc = [&](void** ptr, size_t n) -> int {
