@@ -45,6 +45,8 @@ struct DcDev {
 
 // One face of the linearised flux (scaled like ptd_device.cuh):
 // u = K_f (d_R - d_L) [+ 3 s^2 (h_R - h_L) (d_L + d_R)],  w <- w - c (w + u).
+// Every operation explicit, so that the packed two-face form below rounds
+// identically (D_f = (s/2)^3 = s^3/8 exactly).
 template <int MODEL, bool U>
 __device__ __forceinline__ float face32(const DcArgs& a, float dL, float dR, float hL, float hR, float DL,
                                         float DR, float w, float& u)
@@ -55,18 +57,42 @@ __device__ __forceinline__ float face32(const DcArgs& a, float dL, float dR, flo
         uu = gd;
         c = a.c_lin;
     } else if (MODEL == LINSTEP) {
-        uu = (DL + DR) * gd;
+        uu = __fmul_rn(DL + DR, gd);
         c = a.c_lin;
     } else {
         const float s = hL + hR;
-        const float s2 = s * s;
-        const float s3 = s2 * s;
-        uu = s3 * gd;
-        uu = fmaf(3.0f * s2 * (hR - hL), dL + dR, uu);
-        c = nonlin_face_c3(a.f, 0.125f * s3);   // = nonlin_face_c(a.f, s)
+        const float s2 = __fmul_rn(s, s);
+        const float s3 = __fmul_rn(s2, s);
+        uu = __fmaf_rn(__fmul_rn(__fmul_rn(3.0f, s2), hR - hL), dL + dR, __fmul_rn(s3, gd));
+        c = face_c_rn(a.f, __fmul_rn(0.125f, s3));
     }
     if (U) u = uu;
-    return fmaf(-c, w + uu, w);
+    return __fmaf_rn(-c, w + uu, w);
+}
+
+// Two faces (LIN, NONLIN) with FP32x2 flux arithmetic; c stays scalar (its
+// constant operands are free in scalar instructions).  3 s^2 is formed as
+// (s^2 + s^2) + s^2, which rounds once like 3.0f * s^2.
+template <int MODEL, bool U>
+__device__ __forceinline__ float2 face32x2(const DcArgs& a, float2 dL, float2 dR, float2 hL, float2 hR, float2 w,
+                                           float2& u)
+{
+    const float2 gd = sub2(dR, dL);
+    float2 uu;
+    float cx, cy;
+    if (MODEL == LIN) {
+        uu = gd;
+        cx = cy = a.c_lin;
+    } else {
+        const float2 s = add2(hL, hR);
+        const float2 s2 = mul2(s, s);
+        const float2 s3 = mul2(s2, s);
+        uu = fma2(mul2(add2(add2(s2, s2), s2), sub2(hR, hL)), add2(dL, dR), mul2(s3, gd));
+        cx = face_c_rn(a.f, __fmul_rn(0.125f, s3.x));
+        cy = face_c_rn(a.f, __fmul_rn(0.125f, s3.y));
+    }
+    if (U) u = uu;
+    return fma2(f2(-cx, -cy), add2(w, uu), w);
 }
 
 template <int MODEL>
@@ -275,7 +301,9 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
     if (j0 == 1 && upd2) a.wout[1][oA] = wy2b;
     float h0 = hB, D0 = DB, Dm1 = DA;
 
-    // ---- march: level 1 of row s+1, level 2 of row s
+    // ---- march: level 1 of row s+1, level 2 of row s (LIN, NONLIN: the x
+    // and y faces of a level as one FP32x2 evaluation)
+    constexpr bool PACKF = MODEL == LIN || MODEL == NONLIN;
     long long o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float p1 = d1, wx1 = 0.0f, wy1 = 0.0f, r1 = 0.0f, h2 = h1, D2 = D1;
@@ -284,8 +312,18 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
             h2 = a.Hf[o + sy];
             if (LS) D2 = a.Df[o + sy];
             r1 = a.r[o];
-            wx1 = x1(o, d1, h1, D1);
-            wy1 = face32<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], u);
+            if (PACKF) {
+                const float d1r = __shfl_down_sync(FULL, d1, 1);
+                const float h1r = __shfl_down_sync(FULL, h1, 1);
+                float2 uu;
+                const float2 w1 = face32x2<MODEL, false>(a, f2(d1), f2(d1r, d2), f2(h1), f2(h1r, h2),
+                                                         f2(a.win[0][o], a.win[1][o]), uu);
+                wx1 = w1.x;
+                wy1 = w1.y;
+            } else {
+                wx1 = x1(o, d1, h1, D1);
+                wy1 = face32<MODEL, false>(a, d1, d2, h1, h2, D1, D2, a.win[1][o], u);
+            }
             const float wx1l = __shfl_up_sync(FULL, wx1, 1);
             const float e1 = cell_e32<MODEL>(a, h1, dc_star<MODEL>(D1, D0, D2));
             if (upd1) p1 = dc_update(a, d1, wx1, wx1l, wy1, wy1p, r1, e1);
@@ -295,9 +333,18 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
         const float p0r = __shfl_down_sync(FULL, p0, 1);
         const float h0r = __shfl_down_sync(FULL, h0, 1);
         const float D0r = LS ? __shfl_down_sync(FULL, D0, 1) : 0.0f;
-        float ux2 = 0.0f, uy2 = 0.0f;
-        const float wx2 = face32<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, ux2);
-        const float wy2 = face32<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, uy2);
+        float ux2 = 0.0f, uy2 = 0.0f, wx2, wy2;
+        if (PACKF) {
+            float2 u2 = f2(0.0f);
+            const float2 w2 = face32x2<MODEL, CHECK>(a, f2(p0), f2(p0r, p1), f2(h0), f2(h0r, h1), f2(wx1p, wy1p), u2);
+            wx2 = w2.x;
+            wy2 = w2.y;
+            ux2 = u2.x;
+            uy2 = u2.y;
+        } else {
+            wx2 = face32<MODEL, CHECK>(a, p0, p0r, h0, h0r, D0, D0r, wx1p, ux2);
+            wy2 = face32<MODEL, CHECK>(a, p0, p1, h0, h1, D0, D1, wy1p, uy2);
+        }
         const float wx2l = __shfl_up_sync(FULL, wx2, 1);
         const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
         const float e0 = cell_e32<MODEL>(a, h0, dc_star<MODEL>(D0, Dm1, D1));

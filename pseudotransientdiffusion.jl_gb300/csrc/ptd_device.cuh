@@ -147,6 +147,26 @@ __device__ __forceinline__ float nonlin_cell_e(const FParams& a, float h, float 
 // (NONLIN_EXPM: D = exp(m) H^3 -- efac = exp(m) at the cell, the arithmetic
 // mean of exp(m) at a face.)
 
+// The face parameter c with every operation explicit (no contraction left to
+// the compiler), for the FP32 kernels whose scalar and packed two-lane forms
+// must round identically (ptd_rb.cu, ptd_dc_body.cuh): c = 1/(1 + fk2/Re_f),
+// Re_f = pi + sqrt(pi^2 + fA/D_f).
+__device__ __forceinline__ float face_c_rn(const FParams& f, float df)
+{
+    const float q = __fmaf_rn(f.fA, frcp(df), f.fpi2);
+    const float re = __fadd_rn(f.fpi, fsqrt(q));
+    return frcp(__fmaf_rn(f.fk2, frcp(re), 1.0f));
+}
+
+// Two lanes at once (FP32x2 instructions, sm_100 and later: two faces per
+// instruction, each component rounded exactly like the scalar operation).
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }   // a - b
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 // LINSTEP cell: 1/dtau = maxloc(D) * Re / (Vpdtau L) (compute_iter_params!,
 // scripts/diff_2D_linstep.jl:18-21).
 __device__ __forceinline__ float linstep_cell_e(const FParams& a, float dmax)

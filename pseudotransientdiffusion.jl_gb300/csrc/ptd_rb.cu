@@ -77,19 +77,10 @@ struct RbDev {
     double err64;     // last FP64 err
 };
 
-// Iteration parameters of the rebased kernels, every operation explicit (no
-// contraction left to the compiler), so that the scalar forms below and the
-// packed two-lane forms (f32x2, rb2d_tb2_body) round identically.
-// Face: c = 1/(1 + fk2/Re_f), Re_f = pi + sqrt(pi^2 + fA/D_f); cell:
-// e = 1/((pi H^3 + sqrt(pi^2 H^6 + fA H^3)) k1 + 1/dt) (the formulas of
-// nonlin_face_c / nonlin_cell_e, scripts/diff_2D_nonlin.jl:145-152).
-__device__ __forceinline__ float rb_c(const FParams& f, float df)
-{
-    const float q = __fmaf_rn(f.fA, frcp(df), f.fpi2);
-    const float re = __fadd_rn(f.fpi, fsqrt(q));
-    return frcp(__fmaf_rn(f.fk2, frcp(re), 1.0f));
-}
-
+// Cell parameter of the rebased kernels, every operation explicit (the face
+// parameter is face_c_rn, ptd_device.cuh), so that every kernel variant
+// rounds identically: e = 1/((pi H^3 + sqrt(pi^2 H^6 + fA H^3)) k1 + 1/dt)
+// (nonlin_cell_e, scripts/diff_2D_nonlin.jl:149-152).
 __device__ __forceinline__ float rb_e(const FParams& f, float h3)
 {
     const float q = __fmaf_rn(__fmul_rn(f.fpi2, h3), h3, __fmul_rn(f.fA, h3));
@@ -120,9 +111,9 @@ __device__ __forceinline__ float rb_face(const RbArgs& a, float dL, float dR, fl
             const float e2 = DL + DR;
             ud = __fmul_rn(ud, e2);
             const float m = __fmul_rn(0.5f, st);
-            c = rb_c(a.f, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(0.5f, e2), m), m), m));
+            c = face_c_rn(a.f, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(0.5f, e2), m), m), m));
         } else {
-            c = rb_c(a.f, __fmul_rn(0.125f, st3));   // D_f = (st/2)^3
+            c = face_c_rn(a.f, __fmul_rn(0.125f, st3));   // D_f = (st/2)^3
         }
     }
     if (U) u = ud;
@@ -138,15 +129,6 @@ __device__ __forceinline__ float rb_cell_e(const RbArgs& a, float h, float dmax)
     if (MODEL == NONLIN_EXPM) h3 = __fmul_rn(__fmul_rn(__fmul_rn(dmax, h), h), h);   // dmax carries exp(m)
     return rb_e(a.f, h3);
 }
-
-// ---- the same on two lanes at once (FP32x2 instructions: two faces per
-// instruction, each component rounded exactly like the scalar form)
-__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
-__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }   // a - b
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
 // Two faces: the flux arithmetic packed, the iteration parameters c (MUFU
 // work with constant operands, which scalar instructions take for free)
@@ -167,8 +149,8 @@ __device__ __forceinline__ float2 rb_face2(const RbArgs& a, float2 dL, float2 dR
         const float2 st = add2(sb, sd);
         const float2 st3 = mul2(mul2(st, st), st);
         ud = fma2(mul2(sd, fma2(add2(add2(sb, sb), sb), st, mul2(sd, sd))), gb, mul2(st3, gd));
-        cx = rb_c(a.f, __fmul_rn(0.125f, st3.x));
-        cy = rb_c(a.f, __fmul_rn(0.125f, st3.y));
+        cx = face_c_rn(a.f, __fmul_rn(0.125f, st3.x));
+        cy = face_c_rn(a.f, __fmul_rn(0.125f, st3.y));
     }
     if (U) u = ud;
     return fma2(f2(-cx, -cy), add2(w, add2(tb, ud)), w);
