@@ -109,10 +109,10 @@ __global__ void __launch_bounds__(256) dc2d_batch_kernel(const DcArgs* __restric
     const int4 w = work[blockIdx.x];
     const DcArgs a = tab[w.x];
     if (dc_done(a.done)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     dc2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 // two inner iterations per launch (temporal blocking, ptd_dc_body.cuh)
@@ -123,10 +123,10 @@ __global__ void __launch_bounds__(256) dc2d_tb2_batch_kernel(const DcArgs* __res
     const int4 w = work[blockIdx.x];
     const DcArgs a = tab[w.x];
     if (dc_done(a.done)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     dc2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 __global__ void inner_judge_batch_kernel(BDev* st, int ninst, int nchk, int itmax, int norm_max, int stall)

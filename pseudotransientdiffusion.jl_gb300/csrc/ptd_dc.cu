@@ -36,20 +36,20 @@ template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) dc1d_kernel(DcArgs a)
 {
     if (dc_done(a.done)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     dc1d_body<MODEL, CHECK>(a, blockIdx.x, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) dc2d_kernel(DcArgs a, int chunk)
 {
     if (dc_done(a.done)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     dc2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 // two inner iterations per launch (temporal blocking), see dc2d_tb2_body
@@ -57,20 +57,20 @@ template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) dc2d_tb2_kernel(DcArgs a, int chunk)
 {
     if (dc_done(a.done)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     dc2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 template <int MODEL, bool CHECK, int R>
 __global__ void __launch_bounds__(32 * R) dc3d_kernel(DcArgs a, int chunk)
 {
     if (dc_done(a.done)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     dc3d_body<MODEL, CHECK, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 // ---------------------------------------------------------------------------

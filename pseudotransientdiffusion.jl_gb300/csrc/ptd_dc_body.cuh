@@ -107,7 +107,7 @@ __device__ __forceinline__ bool dc_done(const int* done) { return __ldcg(done) !
 
 // ---------------------------------------------------------------------------
 template <int MODEL, bool CHECK>
-__device__ __forceinline__ void dc1d_body(const DcArgs& a, int bx, double& part, unsigned long long& pmax)
+__device__ __forceinline__ void dc1d_body(const DcArgs& a, int bx, float& part, unsigned& pmax)
 {
     const int i = bx * blockDim.x + threadIdx.x;
     const int nx = a.nx;
@@ -129,14 +129,14 @@ __device__ __forceinline__ void dc1d_body(const DcArgs& a, int bx, double& part,
             const float div = (wr - wl) * a.sig[0];
             const float dn = fmaf(-e, fmaf(dc, a.rdt, div - rr), dc);
             a.dout[i] = dn;
-            if (CHECK) accumulate_residual((double)fmaf(-dn, a.rdt, rr + (ur - ul) * a.sig[0]), part, pmax);
+            if (CHECK) accumulate_residual32(fmaf(-dn, a.rdt, rr + (ur - ul) * a.sig[0]), part, pmax);
         }
     }
 }
 
 template <int MODEL, bool CHECK>
-__device__ __forceinline__ void dc2d_body(const DcArgs& a, int tile, int cy, int chunk, double& part,
-                                          unsigned long long& pmax)
+__device__ __forceinline__ void dc2d_body(const DcArgs& a, int tile, int cy, int chunk, float& part,
+                                          unsigned& pmax)
 {
     const int lane = threadIdx.x;
     const int i = 31 * tile + lane;
@@ -186,7 +186,7 @@ __device__ __forceinline__ void dc2d_body(const DcArgs& a, int tile, int cy, int
                 a.dout[idx] = dnew;
                 if (CHECK) {
                     const float divu = fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]);
-                    accumulate_residual((double)fmaf(-dnew, a.rdt, rr + divu), part, pmax);
+                    accumulate_residual32(fmaf(-dnew, a.rdt, rr + divu), part, pmax);
                 }
             }
             dc = dn;
@@ -240,8 +240,8 @@ __device__ __forceinline__ float dc_star(float Dc, float Db, float Dn)
 }
 
 template <int MODEL, bool CHECK>
-__device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy, int chunk, double& part,
-                                              unsigned long long& pmax)
+__device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy, int chunk, float& part,
+                                              unsigned& pmax)
 {
     constexpr bool LS = MODEL == LINSTEP;
     const int lane = threadIdx.x;
@@ -356,7 +356,7 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
             a.wout[1][os] = wy2;
             if (CHECK) {
                 const float divu = fmaf(uy2 - uy2b, a.sig[1], (ux2 - ux2l) * a.sig[0]);
-                accumulate_residual((double)fmaf(-q, a.rdt, r0 + divu), part, pmax);
+                accumulate_residual32(fmaf(-q, a.rdt, r0 + divu), part, pmax);
             }
         }
         // shift the windows
@@ -375,8 +375,8 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
 }
 
 template <int MODEL, bool CHECK, int R>
-__device__ __forceinline__ void dc3d_body(const DcArgs& a, int bx, int by, int bz, int chunk, double& part,
-                                          unsigned long long& pmax)
+__device__ __forceinline__ void dc3d_body(const DcArgs& a, int bx, int by, int bz, int chunk, float& part,
+                                          unsigned& pmax)
 {
     __shared__ float sd[2][R][32];
     __shared__ float sh[2][R][32];
@@ -463,7 +463,7 @@ __device__ __forceinline__ void dc3d_body(const DcArgs& a, int bx, int by, int b
                 if (CHECK) {
                     const float uyb = su[p][r - 1][lane];
                     const float divu = fmaf(uz - uzb, a.sig[2], fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]));
-                    accumulate_residual((double)fmaf(-dnew, a.rdt, rr + divu), part, pmax);
+                    accumulate_residual32(fmaf(-dnew, a.rdt, rr + divu), part, pmax);
                 }
             }
             dc = dn;

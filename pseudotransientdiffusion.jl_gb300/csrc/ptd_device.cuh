@@ -236,6 +236,28 @@ __device__ __forceinline__ void accumulate_residual(double r, double& sum, unsig
     mx = b > mx ? b : mx;
 }
 
+// FP32 form for the FP32 inner iterations of the defect correction: their
+// residual is an FP32 value, so one thread's sum of squares and max |r| over
+// its cells (one march of at most a few hundred) stay in FP32 and are widened
+// once per thread (widen_max32) for the FP64 block reduction.  A per-cell
+// f32->f64 conversion and DFMA run on the FP64 pipe, 1/64 of the FP32 rate
+// on this GPU: measured on the 256-instance batch, a check launch of the
+// two-iteration kernel took 532 us with them and 483 us without (a plain
+// launch 213 us; the rest of the gap is the check variant's register count).
+__device__ __forceinline__ void accumulate_residual32(float r, float& sum, unsigned& mx)
+{
+    sum = fmaf(r, r, sum);
+    const unsigned b = __float_as_uint(r) & 0x7fffffffu;
+    mx = b > mx ? b : mx;
+}
+
+// An FP32 max |r| (bit pattern) as the FP64 bit pattern block_reduce_residual
+// compares; NaN stays NaN, so it still wins the max.
+__device__ __forceinline__ unsigned long long widen_max32(unsigned mx)
+{
+    return (unsigned long long)__double_as_longlong((double)__uint_as_float(mx));
+}
+
 __device__ __forceinline__ bool step_done(const int* done)
 {
     return __ldcg(done) != 0;
