@@ -569,8 +569,13 @@ __global__ void __launch_bounds__(256) rb2d_kernel(RbArgs a, int chunk)
     if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
+// The plain NONLIN variant is capped at 32 registers (8 CTAs of 256 threads
+// per SM; ptxas spills 16 bytes): at its natural 40 the march, bound by
+// memory latency, ran at most 48 of 64 warps per SM.  Measured at 4096^2:
+// 77.9 -> 76.8 us per iteration.  A minimum of 0 blocks leaves the other
+// variants' register allocation as without the bound.
 template <int MODEL, bool CHECK>
-__global__ void __launch_bounds__(256) rb2d_tb2_kernel(RbArgs a, int chunk)
+__global__ void __launch_bounds__(256, (MODEL == NONLIN && !CHECK) ? 8 : 0) rb2d_tb2_kernel(RbArgs a, int chunk)
 {
     if (rb_skip(a.skip)) return;
     double part = 0.0;
