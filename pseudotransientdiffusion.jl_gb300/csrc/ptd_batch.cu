@@ -69,8 +69,8 @@ __global__ void __launch_bounds__(256) pt2d_batch_kernel(const PTArgs* __restric
     if (step_done(a.done)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
+    // the body flushes its check partials into a.acc (last step of its march)
     pt2d_body<N, MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a, part, pmax);
 }
 
 __global__ void judge_batch_kernel(DevState* st, int ninst, int nchk, int itmax, double tol,
@@ -111,8 +111,8 @@ __global__ void __launch_bounds__(256) dc2d_batch_kernel(const DcArgs* __restric
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
+    // the body flushes its check partials into a.acc (last step of its march)
     dc2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 // two inner iterations per launch (temporal blocking, ptd_dc_body.cuh)
@@ -125,8 +125,8 @@ __global__ void __launch_bounds__(256) dc2d_tb2_batch_kernel(const DcArgs* __res
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
+    // the body flushes its check partials into a.acc (last step of its march)
     dc2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 __global__ void inner_judge_batch_kernel(BDev* st, int ninst, int nchk, int itmax, int norm_max, int stall)

@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(256) dc2d_kernel(DcArgs a, int chunk)
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
+    // the body flushes its check partials into a.acc (last step of its march)
     dc2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 // two inner iterations per launch (temporal blocking), see dc2d_tb2_body
@@ -59,8 +59,8 @@ __global__ void __launch_bounds__(256) dc2d_tb2_kernel(DcArgs a, int chunk)
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
+    // the body flushes its check partials into a.acc (last step of its march)
     dc2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
 }
 
 template <int MODEL, bool CHECK, int R>

@@ -197,6 +197,7 @@ __device__ __forceinline__ void dc2d_body(const DcArgs& a, int tile, int cy, int
                 Db = Dc;
                 Dc = Dn;
             }
+            if (CHECK && j == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane);
         }
     }
 }
@@ -371,6 +372,7 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
         D0 = D1;
         D1 = D2;
         r0 = r1;
+        if (CHECK && s == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane);
     }
 }
 

@@ -258,6 +258,45 @@ __device__ __forceinline__ unsigned long long widen_max32(unsigned mx)
     return (unsigned long long)__double_as_longlong((double)__uint_as_float(mx));
 }
 
+// Warp-level flush of the FP32 partials into acc (the encoding of
+// block_reduce_residual: sum of squares, or the max |r| bit pattern), one
+// atomic per warp.  The 2D inner kernels call it from inside the last step
+// of their y march, with all 32 lanes converged: a reduction after the march
+// made ptxas give their check variants 52-98 registers (32-40 this way),
+// halving the resident warps of a latency-bound kernel.
+__device__ __forceinline__ void warp_flush_residual32(double* acc, int norm_max, float part_sum, unsigned part_max,
+                                                      int lane)
+{
+    if (norm_max) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned w = __shfl_xor_sync(FULL, part_max, o);
+            part_max = w > part_max ? w : part_max;
+        }
+        if (lane == 0 && part_max) atomicMax(reinterpret_cast<unsigned long long*>(acc), widen_max32(part_max));
+    } else {
+        const double v = warp_sum((double)part_sum);
+        if (lane == 0) atomicAdd(acc, v);
+    }
+}
+
+// FP64 form of warp_flush_residual32 for the 2D kernels whose check partials
+// are doubles (FP64, DF64, DFH, and the rebased FP32 form, whose check
+// residual carries the FP64 base residual): same encoding, one atomic per
+// warp, called from inside the last step of the y march with all 32 lanes
+// converged (after the march, the check variants held 61-97 registers).
+__device__ __forceinline__ void warp_flush_residual(double* acc, int norm_max, double part_sum,
+                                                    unsigned long long part_max, int lane)
+{
+    if (norm_max) {
+        part_max = warp_max_u64(part_max);
+        if (lane == 0 && part_max) atomicMax(reinterpret_cast<unsigned long long*>(acc), part_max);
+    } else {
+        part_sum = warp_sum(part_sum);
+        if (lane == 0) atomicAdd(acc, part_sum);
+    }
+}
+
 __device__ __forceinline__ bool step_done(const int* done)
 {
     return __ldcg(done) != 0;

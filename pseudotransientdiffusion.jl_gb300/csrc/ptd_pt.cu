@@ -45,8 +45,8 @@ __global__ void __launch_bounds__(256) pt2d_kernel(PTArgs a, int chunk)
     if (step_done(a.done)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
+    // the body flushes its check partials into a.acc (last step of its march)
     pt2d_body<N, MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a, part, pmax);
 }
 
 template <class N, int MODEL, bool CHECK, int R>

@@ -247,6 +247,7 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
                 Dc = Dn;
                 dcf = dnf;
             }
+            if (CHECK && j == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane);
         }
     }
 }

@@ -259,6 +259,7 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
                 Db = Dc;
                 Dc = Dn;
             }
+            if (CHECK && j == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane);
         }
     }
 }
@@ -435,6 +436,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         D0 = D1;
         D0r = D1r;
         D1 = D2;
+        if (CHECK && s == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane);
     }
 }
 
@@ -565,8 +567,8 @@ __global__ void __launch_bounds__(256) rb2d_kernel(RbArgs a, int chunk)
     if (rb_skip(a.skip)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
+    // the body flushes its check partials into a.acc (last step of its march)
     rb2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
 // The plain NONLIN variant is capped at 32 registers (8 CTAs of 256 threads
@@ -580,8 +582,8 @@ __global__ void __launch_bounds__(256, (MODEL == NONLIN && !CHECK) ? 8 : 0) rb2d
     if (rb_skip(a.skip)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
+    // the body flushes its check partials into a.acc (last step of its march)
     rb2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
 }
 
 template <int MODEL, bool CHECK>
