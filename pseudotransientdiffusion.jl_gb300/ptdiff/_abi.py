@@ -41,6 +41,29 @@ class PtdParams(C.Structure):
     ]
 
 
+def check_field(a, n: int, name: str, out: bool = False):
+    """A field handed to the library by address must hold exactly n float64
+    values in x-fastest order: the library reads (or, out=True, writes) 8*n
+    bytes at the address, so a wrong dtype or size would run past the buffer.
+    Host arrays: float64, n elements, contiguous in Fortran order (a 1D array
+    contiguous), writeable when out.  Tensors (anything with data_ptr(), on
+    the host or the GPU): float64, n elements, contiguous.  Returns a
+    unchanged; raises ValueError otherwise."""
+    if hasattr(a, "data_ptr"):
+        if str(a.dtype) != "torch.float64" or a.numel() != n or not a.is_contiguous():
+            raise ValueError(f"{name}: expected a contiguous float64 tensor of {n} elements "
+                             f"(got {a.dtype}, {a.numel()} elements)")
+        return a
+    if not hasattr(a, "dtype") or a.dtype != "float64" or a.size != n:
+        raise ValueError(f"{name}: expected {n} float64 values (got {getattr(a, 'dtype', type(a).__name__)}, "
+                         f"{getattr(a, 'size', '?')} values)")
+    if not a.flags.f_contiguous or not a.flags.aligned:
+        raise ValueError(f"{name}: expected contiguous x-fastest (Fortran-ordered) storage")
+    if out and not a.flags.writeable:
+        raise ValueError(f"{name}: the array is read-only")
+    return a
+
+
 class PtdError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str):
         self.status = status

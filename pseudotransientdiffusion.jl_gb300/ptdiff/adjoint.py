@@ -72,15 +72,17 @@ class AdjointSolver:
         except Exception:
             pass
 
-    def _f(self, a):
+    def _n(self):
+        return self.shape[0] * self.shape[1] * self.shape[2]
+
+    def _f(self, a, name):
         if a is None:
             return None
-        if hasattr(a, "data_ptr"):
-            return a.contiguous()
-        return np.asfortranarray(a, dtype=np.float64)
+        a = a.contiguous() if hasattr(a, "data_ptr") else np.asfortranarray(a, dtype=np.float64)
+        return _abi.check_field(a, self._n(), name)
 
     def forward(self, H0, m, Ht, want_HN=False):
-        H0, m, Ht = self._f(H0), self._f(m), self._f(Ht)
+        H0, m, Ht = self._f(H0, "H0"), self._f(m, "m"), self._f(Ht, "Ht")
         loss = C.c_double(0.0)
         HN = np.zeros(self.shape, dtype=np.float64, order="F") if want_HN else None
         iters = np.zeros(max(self.params.nt, 1), dtype=np.int32)
@@ -96,6 +98,9 @@ class AdjointSolver:
         gm = out_m if out_m is not None else (np.zeros(self.shape, dtype=np.float64, order="F") if want_m else None)
         gh = out_H0 if out_H0 is not None else (np.zeros(self.shape, dtype=np.float64, order="F") if want_H0
                                                  else None)
+        for g, name in ((gm, "out_m"), (gh, "out_H0")):
+            if g is not None:
+                _abi.check_field(g, self._n(), name, out=True)
         iters = np.zeros(max(self.params.nt, 1), dtype=np.int32)
         _abi.check(_lib().ptd_adj_gradient(self._h, _ptr(gm), _ptr(gh),
                                            iters.ctypes.data_as(C.POINTER(C.c_int32))), "ptd_adj_gradient")

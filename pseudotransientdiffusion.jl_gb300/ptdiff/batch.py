@@ -74,7 +74,8 @@ class BatchSolver:
         self.params = params
         self.nx = np.ascontiguousarray(nx, dtype=np.int32)
         self.ny = np.ascontiguousarray(ny, dtype=np.int32)
-        assert len(self.nx) == params.ninst == len(self.ny)
+        if not len(self.nx) == params.ninst == len(self.ny):
+            raise ValueError(f"nx, ny: expected {params.ninst} sizes each (got {len(self.nx)}, {len(self.ny)})")
         self._h = C.c_void_p()
         _abi.check(_lib().ptd_batch_create(C.byref(self._h), C.byref(params),
                                            self.nx.ctypes.data_as(C.POINTER(C.c_int32)),
@@ -112,12 +113,16 @@ class BatchSolver:
         """Solve in place on the list of Fortran-ordered arrays Hs.  Returns
         (iters[ninst, nt], err_last[ninst])."""
         n = self.params.ninst
-        for H in Hs:
-            assert H.dtype == np.float64 and (H.flags.f_contiguous or H.ndim == 1)
+        cells = [int(a) * int(b) for a, b in zip(self.nx, self.ny)]
+        if len(Hs) != n or (Ds is not None and len(Ds) != n):
+            raise ValueError(f"expected {n} H arrays{' and D arrays' if Ds is not None else ''}")
+        for i, H in enumerate(Hs):
+            _abi.check_field(H, cells[i], f"H[{i}]", out=True)
         hp = (C.c_void_p * n)(*[H.ctypes.data for H in Hs])
         dp = None
         if Ds is not None:
-            Ds = [np.asfortranarray(D, dtype=np.float64) for D in Ds]
+            Ds = [_abi.check_field(np.asfortranarray(D, dtype=np.float64), cells[i], f"D[{i}]")
+                  for i, D in enumerate(Ds)]
             dp = (C.c_void_p * n)(*[D.ctypes.data for D in Ds])
         iters = np.zeros(n * max(self.params.nt, 1), dtype=np.int32)
         err = np.zeros(n, dtype=np.float64)

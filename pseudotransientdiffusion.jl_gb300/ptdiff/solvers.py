@@ -94,24 +94,14 @@ class Solver:
     def handle(self):
         return self._h
 
-    def _check_array(self, a, name):
-        n = self.params.nx * self.params.ny * self.params.nz
-        if hasattr(a, "data_ptr"):
-            if a.numel() != n or not a.is_contiguous():
-                raise ValueError(f"{name}: expected a contiguous tensor of {n} elements")
-            return a
-        a = np.asarray(a)
-        if a.dtype != np.float64 or a.size != n:
-            raise ValueError(f"{name}: expected {n} float64 values")
-        if not (a.flags.f_contiguous or a.ndim == 1):
-            raise ValueError(f"{name}: expected x-fastest (Fortran-ordered) storage")
-        return a
+    def _check_array(self, a, name, out=False):
+        return _abi.check_field(a, self.params.nx * self.params.ny * self.params.nz, name, out)
 
     def solve(self, H, D=None, err_cap: int = 100000, raise_on_nan: bool = True, Hold=None):
         """Solve nt steps in place on H (numpy Fortran array or device tensor).
         Hold: the first step's previous state (default H).
         Returns (iters_per_step, errhist, status)."""
-        H = self._check_array(H, "H")
+        H = self._check_array(H, "H", out=True)
         if D is not None:
             D = self._check_array(D, "D")
         if Hold is not None:
@@ -142,6 +132,8 @@ class Solver:
 
     def set_state(self, H, D=None):
         H = self._check_array(H, "H")
+        if D is not None:
+            D = self._check_array(D, "D")
         _abi.check(_abi.lib().ptd_set_state(self._h, _ptr(H), _ptr(D)), "ptd_set_state")
 
     def step(self, nsteps: int, err_cap: int = 100000):
@@ -160,6 +152,7 @@ class Solver:
         if out is None:
             shape = (self.params.nx, self.params.ny, self.params.nz)
             out = np.zeros(shape, dtype=np.float64, order="F")
+        self._check_array(out, "out", out=True)
         _abi.check(_abi.lib().ptd_get_state(self._h, _ptr(out)), "ptd_get_state")
         return out
 

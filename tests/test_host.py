@@ -5,6 +5,8 @@
 * ptd_params_init restates the reference scripts' defaults;
 * ptd_create validates its parameters before touching the GPU;
 * the scripts table, grids and initial conditions follow the reference.
+* the wrappers reject fields whose dtype, size or layout would make the
+  library read or write past the buffer, before calling it.
 """
 import ctypes as C
 import os
@@ -191,3 +193,51 @@ def test_rebased_fp32_rejections(kw, msg):
     h = C.c_void_p()
     assert _abi.lib().ptd_create(C.byref(h), C.byref(p)) == _abi.PTD_EINVAL
     assert msg in _abi.last_error()
+
+
+def test_field_check_rejects_what_would_run_past_the_buffer():
+    """Fields go to the library by address (8*n bytes read or written), so
+    the wrappers reject a wrong dtype, size or layout before the call."""
+    n = 6 * 5
+    good = np.zeros((6, 5), order="F")
+    assert _abi.check_field(good, n, "H", out=True) is good
+    assert _abi.check_field(np.zeros(n), n, "H") is not None             # 1D contiguous
+    bad = [np.zeros((6, 5), dtype=np.float32, order="F"),                # 4-byte values
+           np.zeros((6, 4), order="F"),                                  # too few values
+           np.zeros((6, 5), order="C"),                                  # y fastest
+           np.zeros(2 * n)[::2],                                         # strided view
+           [0.0] * n]                                                    # not an array
+    for a in bad:
+        with pytest.raises(ValueError):
+            _abi.check_field(a, n, "H")
+    ro = np.zeros((6, 5), order="F")
+    ro.flags.writeable = False
+    assert _abi.check_field(ro, n, "D") is ro                           # read-only input is fine
+    with pytest.raises(ValueError, match="read-only"):
+        _abi.check_field(ro, n, "H", out=True)
+    torch = pytest.importorskip("torch")
+    assert _abi.check_field(torch.zeros(n, dtype=torch.float64), n, "H") is not None
+    for t in (torch.zeros(n, dtype=torch.float32), torch.zeros(n + 1, dtype=torch.float64),
+              torch.zeros(5, 6, dtype=torch.float64).t()):
+        with pytest.raises(ValueError):
+            _abi.check_field(t, n, "H")
+
+
+def test_batch_solve_checks_counts_and_sizes_before_the_call():
+    from ptdiff import batch as B
+
+    b = object.__new__(B.BatchSolver)   # no ptd_batch_create: the checks run first
+    b.params = B.PtdBatchParams()
+    b.params.ninst = 2
+    b.nx = np.array([4, 5], dtype=np.int32)
+    b.ny = np.array([4, 6], dtype=np.int32)
+    b._h = C.c_void_p()
+    H = [np.zeros((4, 4), order="F"), np.zeros((5, 6), order="F")]
+    with pytest.raises(ValueError, match="expected 2 H arrays"):
+        b.solve(H[:1])
+    with pytest.raises(ValueError, match=r"H\[1\]"):
+        b.solve([H[0], np.zeros((5, 5), order="F")])
+    with pytest.raises(ValueError, match=r"D\[0\]"):
+        b.solve(H, [np.zeros((3, 4)), np.zeros((5, 6))])
+    with pytest.raises(ValueError):
+        B.BatchSolver(B.batch_params(2, model=1), [4, 5], [4])
