@@ -206,7 +206,7 @@ def run_reference(args, world, rank, pg):
                           "workload (batched and adjoint solvers are new here)"}), flush=True)
         return 0
     s = ptdiff.scripts.CONFIGS[args.workload]
-    shape = (s.default_n,) * s.ndim
+    shape = (args.n or s.default_n,) * s.ndim
     cb = None
     vals = []
     budget = max(4.0, 60.0 / max(args.steps, 1))
