@@ -142,7 +142,8 @@ typedef struct ptd_ctx ptd_ctx;
  * diff_2D_nonlin.jl:48-62, diff_3D/diff_3D_nonlin_multixpu.jl:59-74 (and siblings). */
 PTD_API int ptd_params_init(ptd_params* p, int32_t ndim, int32_t model);
 
-/* Validate p and allocate the device buffers of one grid.
+/* Validate p and allocate the device buffers of one grid (PTD_EINVAL for a
+ * grid above 2^40 cells, rows padded to 32 elements).
  * Replaces: the @zeros/@ones allocations of the driver (e.g.
  * scripts/diff_2D_nonlin.jl:65-73). */
 PTD_API int ptd_create(ptd_ctx** ctx, const ptd_params* p);

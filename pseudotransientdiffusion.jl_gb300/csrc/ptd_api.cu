@@ -129,6 +129,10 @@ int ptd::validate(const ptd_params* p)
             return fail(PTD_EINVAL, "n[%d] = %d must be 1 for a %dD grid", d, n[d], p->ndim);
         if (n[d] > (1 << 30)) return fail(PTD_EINVAL, "n[%d] too large", d);
     }
+    // padded cells, formed in floating point so that the test cannot overflow
+    const double nxp = p->ndim == 1 ? (double)p->nx : std::ceil(p->nx / 32.0) * 32.0;
+    if (nxp * (double)p->ny * (double)p->nz > (double)kMaxCells)
+        return fail(PTD_EINVAL, "grid of %d x %d x %d cells too large (limit 2^40 cells)", p->nx, p->ny, p->nz);
     const double l[3] = {p->lx, p->ly, p->lz};
     for (int d = 0; d < p->ndim; ++d)
         if (!(l[d] > 0.0) || !std::isfinite(l[d])) return fail(PTD_EINVAL, "domain length %d must be > 0", d);

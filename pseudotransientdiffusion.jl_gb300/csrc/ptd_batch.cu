@@ -763,6 +763,7 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
         I.nfield = I.sy * ny[i];
         I.off = off;
         off += ((I.nfield + 63) / 64) * 64;
+        if (off > kMaxCells) rc = bfail(PTD_EINVAL, "batch: the instances hold more than 2^40 cells in all");
     }
     if (rc) {
         delete b;

@@ -28,6 +28,11 @@ struct ptd_ctx_base {
     long long sy = 0, sz = 0, nfield = 0;
 };
 
+// Largest grid accepted, in cells including the padding of each row to 32
+// elements: 2^40 (8.8 TB per FP64 field, far beyond any device), so that no
+// byte count or offset derived from a grid's size overflows 64 bits.
+constexpr long long kMaxCells = 1LL << 40;
+
 int set_error(int status, const char* msg);
 int cuda_fail(cudaError_t e, const char* where);
 int validate(const ptd_params* p);

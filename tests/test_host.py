@@ -86,6 +86,11 @@ def test_batch_create_rejects_invalid_params():
     p = B.batch_params(2, precision="fp64")
     p.precision = _abi.PREC_DFH   # single grids only
     assert B._lib().ptd_batch_create(C.byref(h), C.byref(p), n, n) == _abi.PTD_EINVAL
+    # three instances of 2^39 cells each: every one valid, together above 2^40
+    p = B.batch_params(3, precision="fp64")
+    nx3, ny3 = (C.c_int32 * 3)(1 << 20, 1 << 20, 1 << 20), (C.c_int32 * 3)(1 << 19, 1 << 19, 1 << 19)
+    assert B._lib().ptd_batch_create(C.byref(h), C.byref(p), nx3, ny3) == _abi.PTD_EINVAL
+    assert "2^40 cells in all" in _abi.last_error()
 
 
 @pytest.mark.parametrize("ndim,model", [(1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2), (3, 0), (3, 1), (3, 2)])
@@ -123,6 +128,9 @@ def _create(**kw):
     (dict(flags=0x100), "unknown flags"),
     (dict(model=0, D=0.0), "D must be > 0"),
     (dict(ndim=4), "ndim must be"),
+    (dict(nx=1 << 21, ny=1 << 20), "too large (limit 2^40 cells)"),
+    (dict(ndim=3, nx=1 << 14, ny=1 << 13, nz=1 << 14), "too large (limit 2^40 cells)"),
+    (dict(ndim=3, nx=1 << 30, ny=1 << 30, nz=1 << 30), "too large (limit 2^40 cells)"),   # 2^90: no wrap
 ])
 def test_create_rejects_invalid_params(kw, msg):
     st, err = _create(**kw)
