@@ -125,3 +125,18 @@ def test_reference_adjoint_matches_finite_differences(ndim):
         dh = rng.standard_normal(shape)
         fd = (loss(m, H0 + eps * dh) - loss(m, H0 - eps * dh)) / (2 * eps)
         assert abs(fd - np.sum(gh * dh)) <= 1e-6 * abs(fd)
+
+
+def test_1d_benchmark_is_the_shifted_reference_problem():
+    """The 1D benchmark (H0 = 1 + exp(-(x-5)^2), Dirichlet H = 1, nx = 512)
+    is the reference's diff_1D_lin problem shifted by one: same PT counts per
+    step, summing to the published 2020 (output/out_diff_1D_lin.txt), and the
+    same H up to the reference's frozen boundary value exp(-25) ~ 1.4e-11."""
+    published = {row[0]: row[1] for row in COUNTS["1D_lin"]}
+    s = S.CONFIGS["1d_lin_512"]
+    H, it, _, st = O.solve(s, S.initial_condition(s, 512))
+    r = S.SCRIPTS["diff_1D_lin"]
+    Hr, it_r, _, st_r = O.solve(r, S.initial_condition(r, 512))
+    assert st == 0 and st_r == 0
+    assert list(it) == list(it_r) and int(it.sum()) == published[512] == 2020
+    assert np.max(np.abs((H - 1.0) - Hr)) <= 2e-11
