@@ -94,3 +94,19 @@ def test_base_residual_vanishes_at_a_fixed_point():
     wb = [-u_nonlin(Hb, k) for k in range(2)]
     tb = [wb[k] + u_nonlin(Hb, k) for k in range(2)]
     assert all(np.max(np.abs(t)) == 0.0 for t in tb)
+
+
+def test_defect_correction_jacobian_is_the_linear_part():
+    """The FP32_DC inner iteration applies the linearised flux
+    J d = 3 s^2 g (d_L + d_R) + s^3 (d_R - d_L) (ptd_dc_body.cuh, face32):
+    u(H_b + eps d) - u(H_b) - eps J d shrinks like eps^2."""
+    rng = np.random.default_rng(4)
+    Hb = 1.0 + rng.random((9, 7))
+    d = rng.standard_normal((9, 7))
+    for axis in (0, 1):
+        L, R = faces(Hb, axis)
+        dL, dR = faces(d, axis)
+        s, g = L + R, R - L
+        Jd = 3 * s ** 2 * g * (dL + dR) + s ** 3 * (dR - dL)
+        rem = [np.max(np.abs(u_delta(Hb, eps * d, axis) - eps * Jd)) for eps in (1e-2, 1e-3)]
+        assert rem[1] < rem[0] / 50   # ~ eps^2: a 10x smaller eps gives ~100x smaller remainder
