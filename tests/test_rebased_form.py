@@ -8,7 +8,9 @@ and for D = H^3 (faces: s = H_L + H_R, g = H_R - H_L, u = s^3 g)
   u_delta = u(H_b + delta) - u(H_b) = s_d (3 s (s + s_d) + s_d^2) g + (s + s_d)^3 g_d.
 These tests check that one such iteration equals one plain iteration
   w <- w - c (w + u(H)),   H <- H - e ((H - Hold)/dt + sum_d (w_R - w_L) sigma_d)
-on the summed state, so the form changes only where rounding happens."""
+on the summed state, so the form changes only where rounding happens.  The
+last test checks the defect-correction form's linearised flux (FP32_DC)
+against the same flux change."""
 import numpy as np
 
 
