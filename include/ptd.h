@@ -95,11 +95,11 @@ enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH 
 
 /* Residual used for the stopping test.  MIXED is the reference's: the
  * undamped flux from the H the fluxes of that iteration were computed on, the
- * time term from the updated H (scripts/diff_2D_nonlin.jl:157-158,167-170). */
+ * time term from the updated H (scripts/diff_2D_nonlin.jl:31-32,41-44). */
 enum { PTD_RESID_MIXED = 0, PTD_RESID_CONSISTENT = 1 };
 
 /* Norm of the residual: RMS = norm(ResH)/sqrt(length(ResH)) (the reference,
- * scripts/diff_2D_nonlin.jl:211), or MAX = max|R|. */
+ * scripts/diff_2D_nonlin.jl:85), or MAX = max|R|. */
 enum { PTD_NORM_RMS = 0, PTD_NORM_MAX = 1 };
 
 /* Flags */
@@ -263,17 +263,25 @@ PTD_API void ptd_adj_destroy(ptd_adj* a);
  * its lock, drivers that must not grow their footprint after start-up).  It
  * has no counterpart in the reference.  It runs the fused FP64 PT kernel on
  * the caller's device buffers and takes all scratch from one fixed device
- * array compiled into the library (24 MiB, held on every GPU that loads the
- * library until the process exits); it calls no cudaMalloc/cudaFree, creates
+ * array compiled into the library (24 MiB, held from the first call on a GPU
+ * until the process exits); it calls no cudaMalloc/cudaFree, creates
  * no stream or graph and launches on `stream` (a cudaStream_t, NULL = legacy
  * default stream).
  *   p      2D, PTD_PREC_FP64, models LIN/LINSTEP/NONLIN, mixed residual;
  *          nx*ny <= PTD_NOALLOC_MAX_CELLS, else PTD_EINVAL.
- *   H      device memory, nx*ny doubles, x fastest: in H0, out H after p->nt steps.
- *   D      device memory (LINSTEP) or NULL.
+ *   H      device memory of the current device (cudaMalloc'ed or from a
+ *          pool; not managed, host or another GPU's memory, PTD_EINVAL), nx*ny
+ *          doubles, x fastest: in H0, out H after p->nt steps.
+ *   D      device memory of the current device (LINSTEP) or NULL.
  *   iters_per_step  host, p->nt entries (nullable).
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * The array is reserved on a device by the first call there (the CUDA
+ * runtime loads the library's device code lazily; that call also looks up the
+ * array's device address with cudaGetSymbolAddress).  A caller that cannot
+ * allocate later therefore makes one call at start-up, before its own
+ * allocator takes the device and before any stream capture: with p->nt = 0
+ * the call only reserves the array, loads the kernels a solve launches and
+ * returns (H may then be NULL).  Later calls change no device memory
+ * reservation.
  * Every call uses the same array: calls that overlap on the GPU (from two
  * streams or two threads) race and must be serialised by the caller. */
 #define PTD_NOALLOC_MAX_CELLS 524288

@@ -15,6 +15,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libptd_oracle.so")
+# the same source built for the host CPU (Makefile); only the timed CPU
+# baseline of bench.py loads it
+NATIVE_LIB_PATH = os.path.join(HERE, "libptd_oracle_native.so")
 
 
 class OraParams(C.Structure):
@@ -32,19 +35,22 @@ class OraParams(C.Structure):
 
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "ptd_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    stale = [p for p in (LIB_PATH, NATIVE_LIB_PATH)
+             if not os.path.exists(p) or os.path.getmtime(p) < os.path.getmtime(src)]
+    if force or stale:
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(native: bool = False):
+    """The oracle library: the portable build (the checker), or with
+    native=True the host-tuned build of the same source (CPU timing only)."""
+    if native not in _libs:
         build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(NATIVE_LIB_PATH if native else LIB_PATH)
         dp = C.POINTER(C.c_double)
         ip = C.POINTER(C.c_int32)
         L.ora_solve.argtypes = [C.POINTER(OraParams), dp, dp, ip, dp, C.c_int32, ip]
@@ -57,8 +63,8 @@ def lib():
         L.ora_residual_norm.restype = C.c_double
         L.ora_adjoint.argtypes = [C.POINTER(OraParams), dp, dp, dp, dp, dp, C.c_double]
         L.ora_adjoint.restype = C.c_int
-        _lib = L
-    return _lib
+        _libs[native] = L
+    return _libs[native]
 
 
 def _dptr(a):
@@ -96,11 +102,12 @@ def solve(script, H0, D=None, *, nt=None, itmax=None, nout=None, resid=0, norm=0
     return H, iters[: p.nt].copy(), eh[: min(ne.value, errcap)].copy(), st
 
 
-def iterate(script, H, Hold, q, niter, D=None, nthreads=0):
-    """Fixed-iteration kernel loop (timed CPU baseline): updates H and q (3 arrays) in place."""
+def iterate(script, H, Hold, q, niter, D=None, nthreads=0, native=False):
+    """Fixed-iteration kernel loop (timed CPU baseline): updates H and q (3 arrays) in place.
+    native=True runs the host-tuned build."""
     p = params(script, H.shape, nthreads=nthreads)
     Dv = None if D is None else np.asfortranarray(D, dtype=np.float64)
-    st = lib().ora_iterate(C.byref(p), _dptr(H), _dptr(Hold), _dptr(Dv),
+    st = lib(native).ora_iterate(C.byref(p), _dptr(H), _dptr(Hold), _dptr(Dv),
                            _dptr(q[0]), _dptr(q[1]), _dptr(q[2]), niter)
     if st:
         raise RuntimeError(f"ora_iterate failed ({st})")

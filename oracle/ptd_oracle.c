@@ -15,7 +15,7 @@
  *              scripts/diff_3D/diff_3D_nonlin_multixpu.jl:24-55, :71-74
  *   reciprocal scripts/diff_2D_nonlin_perf.jl:19-49, :74 and
  *   ("perf")   scripts/diff_3D/diff_3D_nonlin_perf.jl:19-55, :78
- *   driver     scripts/diff_2D_nonlin.jl:200-217 (physical-time + PT loop,
+ *   driver     scripts/diff_2D_nonlin.jl:76-91 (physical-time + PT loop,
  *              check every nout-th iteration, RMS norm, NaN check)
  *
  * Finite-difference macros of ParallelStencil.jl (third-party, not vendored,
@@ -86,7 +86,7 @@ static int setup(octx* c, const ora_params* p)
     c->pipi = c->pi * c->pi;
     c->rdt = 1.0 / p->dt;
     if (p->model < 2) {
-        /* Re = pi + sqrt(pi^2 + (L^2 / D / dt)) -- diff_2D_lin.jl:152, diff_2D_linstep.jl:70 */
+        /* Re = pi + sqrt(pi^2 + (L^2 / D / dt)) -- diff_2D_lin.jl:51, diff_2D_linstep.jl:70 */
         c->re = c->pi + sqrt(c->pipi + ((c->L2 / p->D) / p->dt));
         c->theta = (c->L / c->vpdt) / c->re;
         c->dtau = ((c->vpdt * c->L) / p->D) / c->re;
@@ -109,7 +109,7 @@ static void face_range(const octx* c, int d, int e, long* lo, long* hi)
 }
 
 /* Face diffusivity and damping ratio theta for the face (c, c+s).
- * nonlinear: diff_2D_nonlin.jl:145-151, perf form diff_2D_nonlin_perf.jl:20-26 */
+ * nonlinear: diff_2D_nonlin.jl:19-25, perf form diff_2D_nonlin_perf.jl:20-26 */
 static inline void face_coef(const octx* c, const double* H, const double* Df, long i, long ir,
                              double* Dface, double* th)
 {
@@ -126,32 +126,50 @@ static inline void face_coef(const octx* c, const double* H, const double* Df, l
 }
 
 /* compute_flux!: damped flux q (and, when q2 != NULL, the undamped flux q2)
- * diff_2D_nonlin.jl:154-160, diff_2D_lin.jl:119-125, diff_2D_linstep.jl:23-29,
- * perf form diff_2D_nonlin_perf.jl:29-44 */
-static void flux_dim(const octx* c, int d, double* q, double* q2, const double* H, const double* Df)
+ * of every direction in one parallel pass, as the reference evaluates all of
+ * its flux arrays in one kernel over the union of their index ranges, each
+ * guarded by its own size (diff_2D_nonlin.jl:28-34, diff_2D_lin.jl:18-24,
+ * diff_2D_linstep.jl:23-29, perf form diff_2D_nonlin_perf.jl:29-33).  Every
+ * face is independent of the others, so the pass order does not change a
+ * result bit. */
+static void flux_all(const octx* c, double* const q[3], double* const q2[3], const double* H, const double* Df)
 {
-    long lo[3], hi[3];
-    for (int e = 0; e < 3; ++e) face_range(c, d, e, &lo[e], &hi[e]);
-    const long sd = c->s[d];
-    const double hd = c->h[d], rhd = c->rh[d];
-    const int recip = c->p->recip;
+    const long n0 = c->n[0], n1 = c->n[1], n2 = c->n[2];
+    const int ndim = c->ndim, recip = c->p->recip;
+    /* k and j span the union of the face ranges: 0..n-2 along a face's own
+     * dimension, 1..n-2 along the others */
+    const long k1 = ndim > 2 ? n2 - 1 : 1;
+    const long j1 = ndim > 1 ? n1 - 1 : 1;
 #pragma omp parallel for collapse(2) schedule(static) num_threads(c->nth)
-    for (long k = lo[2]; k < hi[2]; ++k)
-        for (long j = lo[1]; j < hi[1]; ++j)
-            for (long i = lo[0]; i < hi[0]; ++i) {
-                long ic = i + c->s[1] * j + c->s[2] * k;
-                long ir = ic + sd;
-                double Dface, th;
-                face_coef(c, H, Df, ic, ir, &Dface, &th);
-                double dH = H[ir] - H[ic];
-                if (recip) {
-                    q[ic] = (q[ic] * th - Dface * rhd * dH) / (1.0 + th);
-                    if (q2) q2[ic] = -Dface * rhd * dH;
-                } else {
-                    q[ic] = (q[ic] * th - Dface * dH / hd) / (1.0 + th);
-                    if (q2) q2[ic] = -Dface * dH / hd;
+    for (long k = 0; k < k1; ++k)
+        for (long j = 0; j < j1; ++j) {
+            const int kin = ndim < 3 || k >= 1;   /* k inside 1..n2-2 */
+            const int jin = ndim < 2 || j >= 1;
+            for (int d = 0; d < ndim; ++d) {
+                /* face range of direction d: its own index 0..n-2, the others 1..n-2 */
+                if (d != 2 && !kin) continue;
+                if (d != 1 && !jin) continue;
+                const long i0 = d == 0 ? 0 : 1, i1 = n0 - 1;
+                const long sd = c->s[d];
+                const double hd = c->h[d], rhd = c->rh[d];
+                double* qd = q[d];
+                double* q2d = q2 ? q2[d] : NULL;
+                for (long i = i0; i < i1; ++i) {
+                    long ic = i + n0 * j + n0 * n1 * k;
+                    long ir = ic + sd;
+                    double Dface, th;
+                    face_coef(c, H, Df, ic, ir, &Dface, &th);
+                    double dH = H[ir] - H[ic];
+                    if (recip) {
+                        qd[ic] = (qd[ic] * th - Dface * rhd * dH) / (1.0 + th);
+                        if (q2d) q2d[ic] = -Dface * rhd * dH;
+                    } else {
+                        qd[ic] = (qd[ic] * th - Dface * dH / hd) / (1.0 + th);
+                        if (q2d) q2d[ic] = -Dface * dH / hd;
+                    }
                 }
             }
+        }
 }
 
 /* Undamped flux only (consistent residual; compute_flux_res!, diff_2D_nonlin_perf.jl:40-44). */
@@ -187,7 +205,7 @@ static int is_inner(const octx* c, long idx)
 }
 
 /* Divergence of the three face arrays at inner cell i, in the reference's
- * order ((qx/dx + qy/dy) + qz/dz) -- diff_2D_nonlin.jl:163. */
+ * order ((qx/dx + qy/dy) + qz/dz) -- diff_2D_nonlin.jl:37,42. */
 static inline double divergence(const octx* c, double* const q[3], long i)
 {
     double acc = 0.0;
@@ -199,8 +217,8 @@ static inline double divergence(const octx* c, double* const q[3], long i)
     return acc;
 }
 
-/* Pseudo-time step per cell: linear diff_2D_lin.jl:154, step (compute_iter_params!)
- * diff_2D_linstep.jl:18-21, nonlinear diff_2D_nonlin.jl:149,152 (perf :24,27). */
+/* Pseudo-time step per cell: linear diff_2D_lin.jl:53, step (compute_iter_params!)
+ * diff_2D_linstep.jl:18-21, nonlinear diff_2D_nonlin.jl:23,26 (perf :24,27). */
 static inline double cell_dtau(const octx* c, const double* H, const double* dtau_arr, long i)
 {
     const ora_params* p = c->p;
@@ -213,7 +231,7 @@ static inline double cell_dtau(const octx* c, const double* H, const double* dta
     return (((c->vpdt * c->L) / h3) / re) * p->resc;
 }
 
-/* compute_update!: diff_2D_nonlin.jl:162-165 (division form),
+/* compute_update!: diff_2D_nonlin.jl:36-39 (division form),
  * diff_2D_nonlin_perf.jl:35-38 (reciprocal form). */
 static void update(const octx* c, double* H, const double* Hold, double* const q[3], const double* dtau_arr)
 {
@@ -235,7 +253,7 @@ static void update(const octx* c, double* H, const double* Hold, double* const q
             }
 }
 
-/* check_res! + norm: diff_2D_nonlin.jl:167-170,210-211; 3D norm_g
+/* check_res! + norm: diff_2D_nonlin.jl:41-44,83-86; 3D norm_g
  * diff_3D_nonlin_multixpu.jl:20,113 (one rank: identical to norm/sqrt(length)). */
 static double residual_norm(const octx* c, const double* H, const double* Hold, double* const q2[3])
 {
@@ -317,8 +335,7 @@ int ora_solve2(const ora_params* p, double* H, const double* Hold0, const double
         double err = 2.0 * p->tol;
         while (err > p->tol && iter < p->itmax) {
             int check = ((iter + 1) % p->nout) == 0;
-            for (int d = 0; d < c.ndim; ++d)
-                flux_dim(&c, d, q[d], (check && p->resid == 0) ? q2[d] : NULL, H, Dcoef);
+            flux_all(&c, q, (check && p->resid == 0) ? q2 : NULL, H, Dcoef);
             update(&c, H, Hold, q, dtau_arr);
             iter += 1;
             if (check) {
@@ -358,7 +375,7 @@ int ora_iterate(const ora_params* p, double* H, const double* Hold, const double
     }
     const double* Dcoef = p->model == 3 ? dtau_arr : Dfield;
     for (int32_t it = 0; it < niter; ++it) {
-        for (int d = 0; d < c.ndim; ++d) flux_dim(&c, d, q[d], NULL, H, Dcoef);
+        flux_all(&c, q, NULL, H, Dcoef);
         update(&c, H, Hold, q, dtau_arr);
     }
     free(dtau_arr);

@@ -778,11 +778,11 @@ cudaError_t adj_rebase(ptd_adj* A)
         f.wb[d] = A->wb[d];
         for (int q = 0; q < 2; ++q) f.w[d][q] = static_cast<float*>(A->w[d][q]);
     }
-    adj_rb_fold_kernel<<<152 * 8, 256, 0, A->s>>>(f, A->rbst);
+    adj_rb_fold_kernel<<<fill_blocks(), 256, 0, A->s>>>(f, A->rbst);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    if (A->expm) adj_rb_base_kernel<true><<<152 * 8, 256, 0, A->s>>>(adj_base_args(A), A->rbst);
-    else adj_rb_base_kernel<false><<<152 * 8, 256, 0, A->s>>>(adj_base_args(A), A->rbst);
+    if (A->expm) adj_rb_base_kernel<true><<<fill_blocks(), 256, 0, A->s>>>(adj_base_args(A), A->rbst);
+    else adj_rb_base_kernel<false><<<fill_blocks(), 256, 0, A->s>>>(adj_base_args(A), A->rbst);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     adj_rb_base_judge_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->dv.norm_den);
@@ -979,7 +979,7 @@ static int adj_loss(ptd_adj* A, double* loss)
 {
     const double* HN = A->ck + (size_t)A->p.nt * A->g.nfield;
     ACK(cudaMemsetAsync(&A->st->acc, 0, sizeof(double), A->s));
-    adj_misfit_kernel<<<152 * 8, 256, 0, A->s>>>(HN, A->Ht, nullptr, &A->st->acc, A->g.nx, A->g.ny, A->g.nz, A->g.sy,
+    adj_misfit_kernel<<<fill_blocks(), 256, 0, A->s>>>(HN, A->Ht, nullptr, &A->st->acc, A->g.nx, A->g.ny, A->g.nz, A->g.sy,
                                                   A->g.sz, 0);
     ACK(cudaGetLastError());
     ACK(cudaMemcpyAsync(A->h_st, A->st, sizeof(AdjState), cudaMemcpyDeviceToHost, A->s));
@@ -1003,10 +1003,10 @@ extern "C" int ptd_adj_forward(ptd_adj* A, const double* H0, const double* m, co
     if (A->expm) {
         rc = copy_field_in(A->g, A->stage, m, A->s);
         if (rc) return rc;
-        expd_kernel<<<152 * 8, 256, 0, A->s>>>(A->stage, A->Ed, A->g.nfield);
+        expd_kernel<<<fill_blocks(), 256, 0, A->s>>>(A->stage, A->Ed, A->g.nfield);
         ACK(cudaGetLastError());
         if (A->rb) {   // exp(m) as FP32 for the rebased adjoint iteration
-            adj_tofloat_kernel<<<152 * 8, 256, 0, A->s>>>(A->Ed, static_cast<float*>(A->E), A->g.nfield);
+            adj_tofloat_kernel<<<fill_blocks(), 256, 0, A->s>>>(A->Ed, static_cast<float*>(A->E), A->g.nfield);
             ACK(cudaGetLastError());
         } else {
             ACK(launch_expm(A->stage, A->E, A->g.nfield, A->df64, A->s));
@@ -1050,7 +1050,7 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
     // g = H^nt - Ht on inner cells
     ACK(cudaMemsetAsync(A->gbuf, 0, b, A->s));
     const double* HN = A->ck + (size_t)A->p.nt * A->g.nfield;
-    adj_misfit_kernel<<<152 * 8, 256, 0, A->s>>>(HN, A->Ht, A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
+    adj_misfit_kernel<<<fill_blocks(), 256, 0, A->s>>>(HN, A->Ht, A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
                                                   A->g.sy, A->g.sz, A->df64);
     ACK(cudaGetLastError());
     ACK(cudaMemsetAsync(&A->st->acc, 0, sizeof(double), A->s));
@@ -1059,7 +1059,7 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         // rebased FP32 adjoint solve of step n
         const double* Hn = A->ck + (size_t)n * A->g.nfield;
         ACK(cudaMemcpyAsync(A->Hk64, Hn, b, cudaMemcpyDeviceToDevice, A->s));
-        adj_tofloat_kernel<<<152 * 8, 256, 0, A->s>>>(Hn, static_cast<float*>(A->Hk), A->g.nfield);
+        adj_tofloat_kernel<<<fill_blocks(), 256, 0, A->s>>>(Hn, static_cast<float*>(A->Hk), A->g.nfield);
         ACK(cudaGetLastError());
         ACK(cudaMemsetAsync(A->lamb, 0, b, A->s));
         for (int d = 0; d < 3; ++d) ACK(cudaMemsetAsync(A->wb[d], 0, b, A->s));
@@ -1068,7 +1068,7 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
             for (int d = 0; d < 3; ++d) ACK(cudaMemsetAsync(A->w[d][q], 0, b, A->s));
         }
         ACK(cudaMemsetAsync(&A->rbst->acc, 0, sizeof(double), A->s));
-        adj_sumsq_kernel<F64><<<152 * 8, 256, 0, A->s>>>(A->gbuf, &A->rbst->acc, A->g.nx, A->g.ny, A->g.nz, A->g.sy,
+        adj_sumsq_kernel<F64><<<fill_blocks(), 256, 0, A->s>>>(A->gbuf, &A->rbst->acc, A->g.nx, A->g.ny, A->g.nz, A->g.sy,
                                                          A->g.sz);
         ACK(cudaGetLastError());
         adj_rb_init_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->rtol, A->accept_rtol, A->dv.norm_den);
@@ -1099,8 +1099,8 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         AdjArgs a;
         adj_fill(A, 0, a);
         a.lin = A->lamb;   // the FP64 base holds the solution
-        if (A->expm) adj_grad_kernel<F64, true><<<152 * 8, 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells);
-        else adj_grad_kernel<F64, false><<<152 * 8, 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells);
+        if (A->expm) adj_grad_kernel<F64, true><<<fill_blocks(), 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells);
+        else adj_grad_kernel<F64, false><<<fill_blocks(), 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells);
         ACK(cudaGetLastError());
         A->launches += 1;
     }
@@ -1114,10 +1114,10 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         }
         // target: rtol * ||g||_rms
         if (A->df64)
-            adj_sumsq_kernel<DF64><<<152 * 8, 256, 0, A->s>>>(A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
+            adj_sumsq_kernel<DF64><<<fill_blocks(), 256, 0, A->s>>>(A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
                                                               A->g.sy, A->g.sz);
         else
-            adj_sumsq_kernel<F64><<<152 * 8, 256, 0, A->s>>>(A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
+            adj_sumsq_kernel<F64><<<fill_blocks(), 256, 0, A->s>>>(A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
                                                              A->g.sy, A->g.sz);
         ACK(cudaGetLastError());
         adj_target_kernel<<<1, 1, 0, A->s>>>(A->st, A->rtol, A->accept_rtol, A->dv.norm_den, 1e-300);
@@ -1145,7 +1145,7 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         if (A->h_st->done == 2) A->any_capped = true;   // 3 (stalled below accept_rtol) is accepted
         AdjArgs a;
         adj_fill(A, iters & 1, a);
-#define AGK(NT, EX) adj_grad_kernel<NT, EX><<<152 * 8, 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells)
+#define AGK(NT, EX) adj_grad_kernel<NT, EX><<<fill_blocks(), 256, 0, A->s>>>(a, Hn, A->Ed, A->gm, A->gh, A->gbuf, cells)
         if (A->df64) {
             if (A->expm) AGK(DF64, true);
             else AGK(DF64, false);

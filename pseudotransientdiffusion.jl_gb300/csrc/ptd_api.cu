@@ -162,7 +162,7 @@ int ptd::validate(const ptd_params* p)
 }
 
 // Scalar iteration parameters, restating the reference's a1 block
-// (scripts/diff_2D_lin.jl:49-53, diff_2D_linstep.jl:67-71, diff_2D_nonlin.jl:185-188):
+// (scripts/diff_2D_lin.jl:49-53, diff_2D_linstep.jl:67-71, diff_2D_nonlin.jl:59-62):
 // dx = lx/nx, Vpdtau = CFL*min(dx..), L = max(lx..), Re = pi + sqrt(pi^2 + L^2/D/dt),
 // theta = L/Vpdtau/Re, dtau = Vpdtau*L/D/Re.
 void ptd::derive(const ptd_params& p, Derived& dv)
@@ -402,11 +402,11 @@ static int autotune(ptd_ctx* c)
             }
     }
     for (double* f : {c->H[0], c->H[1], c->Hold}) {
-        fill_one_kernel<<<152 * 8, 256, 0, c->stream>>>(f, c->nfield, c->df64 ? 1 : 0);
+        fill_one_kernel<<<fill_blocks(), 256, 0, c->stream>>>(f, c->nfield, c->df64 ? 1 : 0);
         CK(cudaGetLastError());
     }
     if (c->D) {
-        fill_one_kernel<<<152 * 8, 256, 0, c->stream>>>(c->D, c->nfield, c->ddf ? 1 : 0);
+        fill_one_kernel<<<fill_blocks(), 256, 0, c->stream>>>(c->D, c->nfield, c->ddf ? 1 : 0);
         CK(cudaGetLastError());
     }
     cudaEvent_t e0, e1;

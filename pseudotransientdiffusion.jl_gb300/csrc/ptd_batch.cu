@@ -1013,12 +1013,12 @@ extern "C" int ptd_batch_solve(ptd_batch* b, double* const* H, const double* con
         BCK(cudaMemsetAsync(b->H64, 0, db, b->s));
         if ((rc = upload(b, b->H64, H))) return rc;
         BCK(cudaMemcpyAsync(b->Hold64, b->H64, db, cudaMemcpyDeviceToDevice, b->s));
-        tofloat_batch_kernel<<<152 * 8, 256, 0, b->s>>>(b->H64, b->Hf, b->total);
+        tofloat_batch_kernel<<<fill_blocks(), 256, 0, b->s>>>(b->H64, b->Hf, b->total);
         BCK(cudaGetLastError());
         if (b->D64) {
             BCK(cudaMemsetAsync(b->D64, 0, db, b->s));
             if ((rc = upload(b, b->D64, D))) return rc;
-            tofloat_batch_kernel<<<152 * 8, 256, 0, b->s>>>(b->D64, b->Df, b->total);
+            tofloat_batch_kernel<<<fill_blocks(), 256, 0, b->s>>>(b->D64, b->Df, b->total);
             BCK(cudaGetLastError());
         }
         BCK(cudaMemsetAsync(b->rf, 0, (size_t)b->total * sizeof(float), b->s));

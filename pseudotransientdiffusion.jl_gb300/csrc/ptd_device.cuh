@@ -3,7 +3,7 @@
 // The reference evaluates the damped flux and the H update as
 //   q_new = (q*theta - D_f*dH/dx) / (1 + theta)                 (compute_flux!)
 //   H_new = (H + dtau*(Hold/dt - div q)) / (1 + dtau/dt)          (compute_update!)
-// (scripts/diff_2D_nonlin.jl:154-165).  Both are rewritten here in the
+// (scripts/diff_2D_nonlin.jl:28-39).  Both are rewritten here in the
 // algebraically identical fixed-point-preserving form
 //   w_new = w - c * (w + K_f * g)          c = 1/(1+theta),  g = H_R - H_L
 //   H_new = H - e * ((H - Hold)/dt + sum_d (w_R - w_L) * sigma_d)
@@ -118,7 +118,7 @@ __device__ __forceinline__ float fsqrt(float x)
 
 // NONLIN face: c = 1/(1+theta), theta = L*Resc/(Vpdtau*Re_f),
 // Re_f = pi + sqrt(pi^2 + L^2/(D_f dt)), D_f = ((h_L+h_R)/2)^3
-// (scripts/diff_2D_nonlin.jl:145-151).  D_f -> 0 gives Re_f -> inf, c -> 1.
+// (scripts/diff_2D_nonlin.jl:19-25).  D_f -> 0 gives Re_f -> inf, c -> 1.
 __device__ __forceinline__ float nonlin_face_c3(const FParams& a, float df)
 {
     float re = a.fpi + fsqrt(a.fpi2 + a.fA * frcp(df));
@@ -136,7 +136,7 @@ __device__ __forceinline__ float nonlin_face_c(const FParams& a, float hsum, flo
 
 // NONLIN cell: e = 1/(1/dtau + 1/dt) with
 // 1/dtau = H^3 Re / (Vpdtau L Resc) = (pi H^3 + sqrt(pi^2 H^6 + L^2 H^3/dt)) * k1
-// (scripts/diff_2D_nonlin.jl:149,152); finite for H^3 -> 0 (e -> dt).
+// (scripts/diff_2D_nonlin.jl:23,26); finite for H^3 -> 0 (e -> dt).
 __device__ __forceinline__ float nonlin_cell_e(const FParams& a, float h, float efac = 1.0f)
 {
     float h3 = efac * h * h * h;

@@ -34,6 +34,12 @@ struct LaunchCfg {
 // number types of the PT kernels (ptd_num.cuh)
 enum { NUM_F64 = 0, NUM_DF64 = 1, NUM_DFH = 2 };
 
+// Streaming multiprocessors of the current device (queried once per device,
+// ptd_tune.cu), and the grid of the grid-stride helper kernels: 8 CTAs of 256
+// threads per SM.
+int sm_count();
+inline int fill_blocks() { return 8 * sm_count(); }
+
 cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, int num, const LaunchCfg& cfg,
                       cudaStream_t s);
 cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, int num, cudaStream_t s);
@@ -43,5 +49,6 @@ cudaError_t launch_from_df64(const void* src, double* dst, long long n, cudaStre
 cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
                          double norm_den, int norm_max, cudaStream_t s);
 cudaError_t launch_reset_state(DevState* st, cudaStream_t s);
+cudaError_t preload_pt2d_f64();
 
 }  // namespace ptd

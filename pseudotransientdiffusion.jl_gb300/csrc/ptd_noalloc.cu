@@ -13,8 +13,14 @@
 // either: it launches on the caller's stream and reads its few control words
 // back into pageable host memory.
 //
-// The array is part of the library image: every GPU on which the library is
-// loaded holds it until the process exits.
+// The array belongs to this file's device module.  The CUDA runtime loads a
+// module on a device lazily (the default module loading of CUDA 12.2 and
+// later), so the array's 24 MiB are reserved on a device the first time this
+// entry point runs there (its cudaGetSymbolAddress), and stay reserved until
+// the process exits; the kernels a solve launches are loaded the same way.  A
+// caller that cannot allocate later makes that first call at start-up, before
+// its own allocator takes the device: a call with p->nt = 0 maps the array,
+// loads the kernels and returns.
 #include <cstring>
 #include <mutex>
 
@@ -68,6 +74,17 @@ extern "C" int ptd_solve_2d_noalloc(const ptd_params* p, double* H, const double
 {
     int rc = validate(p);
     if (rc) return rc;
+    // map the array on this device first, so that a call with nt = 0 (the
+    // start-up call) reserves it and touches nothing else
+    double* base = nullptr;
+    rc = scratch_address(&base);
+    if (rc) return rc;
+    if (p->nt == 0) {
+        // the start-up call: also load the kernels a solve launches, so that
+        // later calls leave the device's memory reservation unchanged
+        NCK(preload_pt2d_f64());
+        return PTD_OK;
+    }
     if (p->ndim != 2) return set_error(PTD_EINVAL, "ptd_solve_2d_noalloc: 2D grids only");
     if (p->precision != PTD_PREC_FP64) return set_error(PTD_EINVAL, "ptd_solve_2d_noalloc: FP64 only");
     if (p->model != PTD_MODEL_LIN && p->model != PTD_MODEL_LINSTEP && p->model != PTD_MODEL_NONLIN)
@@ -78,14 +95,22 @@ extern "C" int ptd_solve_2d_noalloc(const ptd_params* p, double* H, const double
         return set_error(PTD_EINVAL, "ptd_solve_2d_noalloc: nx*ny exceeds PTD_NOALLOC_MAX_CELLS (524288)");
     if (!H) return set_error(PTD_EINVAL, "ptd_solve_2d_noalloc: H is NULL");
     if (p->model == PTD_MODEL_LINSTEP && !D) return set_error(PTD_EINVAL, "ptd_solve_2d_noalloc: the step model needs D");
-    cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, H) != cudaSuccess || at.type != cudaMemoryTypeDevice) {
-        cudaGetLastError();
-        return set_error(PTD_EINVAL, "ptd_solve_2d_noalloc: H must be device memory");
+    // H (and D) must be plain device memory of the current device, the device
+    // whose copy of the array the kernels use (managed or host memory, or
+    // memory of another GPU, would be read across the interconnect)
+    int dev = 0;
+    NCK(cudaGetDevice(&dev));
+    const double* const ptrs[2] = {H, p->model == PTD_MODEL_LINSTEP ? D : nullptr};
+    for (int k = 0; k < 2; ++k) {
+        if (!ptrs[k]) continue;
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, ptrs[k]) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+            at.device != dev) {
+            cudaGetLastError();
+            return set_error(PTD_EINVAL, k == 0 ? "ptd_solve_2d_noalloc: H must be device memory of the current device"
+                                                : "ptd_solve_2d_noalloc: D must be device memory of the current device");
+        }
     }
-    double* base = nullptr;
-    rc = scratch_address(&base);
-    if (rc) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // carve the array: H1 | Hold | wx0 | wx1 | wy0 | wy1 | control block

@@ -6,12 +6,12 @@
 // One launch computes, for every face, the damped flux of iteration k+1 from
 // H^k and the flux of iteration k, and for every inner cell H^{k+1} from those
 // new fluxes: the reference's compute_flux! + compute_update! pair
-// (scripts/diff_2D_nonlin.jl:154-165, diff_3D/diff_3D_nonlin_multixpu.jl:37-50,
+// (scripts/diff_2D_nonlin.jl:28-39, diff_3D/diff_3D_nonlin_multixpu.jl:37-50,
 // diff_1D_nonlin.jl:24-33 and the lin/linstep siblings) in a single pass over
 // memory.  H and the fluxes are double-buffered (read k, write k+1), which
 // keeps the reference's Jacobi semantics across tile boundaries.  On a check
 // iteration (template CHECK) the same pass also forms the reference's mixed
-// residual (check_res!, scripts/diff_2D_nonlin.jl:167-170): undamped flux from
+// residual (check_res!, scripts/diff_2D_nonlin.jl:41-44): undamped flux from
 // H^k, time term from H^{k+1}, reduced to sum R^2 / max|R| in the same launch.
 //
 // Tiling (2D and 3D): a warp owns 32 consecutive x cells of which lanes 1..31
@@ -150,7 +150,7 @@ __global__ void expm_kernel(const double* m, void* E, long long n, int df64)
 
 cudaError_t launch_expm(const double* m, void* E, long long n, bool df64, cudaStream_t s)
 {
-    expm_kernel<<<152 * 8, 256, 0, s>>>(m, E, n, df64 ? 1 : 0);
+    expm_kernel<<<fill_blocks(), 256, 0, s>>>(m, E, n, df64 ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -223,7 +223,7 @@ cudaError_t launch_pt(const PTArgs& a, int ndim, int model, bool check, int num,
 template <class N>
 static void resid_consistent_type(const PTArgs& a, int ndim, int model, cudaStream_t s)
 {
-    const int bs = 256, nb = 152 * 8;
+    const int bs = 256, nb = fill_blocks();
     if (model == LIN) resid_consistent_kernel<N, LIN><<<nb, bs, 0, s>>>(a, ndim);
     else if (model == LINSTEP) resid_consistent_kernel<N, LINSTEP><<<nb, bs, 0, s>>>(a, ndim);
     else if (model == NONLIN) resid_consistent_kernel<N, NONLIN><<<nb, bs, 0, s>>>(a, ndim);
@@ -236,6 +236,26 @@ cudaError_t launch_resid_consistent(const PTArgs& a, int ndim, int model, int nu
     else if (num == NUM_DFH) resid_consistent_type<DFH>(a, ndim, model, s);
     else resid_consistent_type<F64>(a, ndim, model, s);
     return cudaGetLastError();
+}
+
+// Load every kernel the FP64 2D solve launches (the six model x check
+// variants of the fused kernel, the judge and the state reset) on the current
+// device.  The runtime loads device code lazily, on a kernel's first launch;
+// a caller that must not see device memory change during later solves calls
+// this once up front.
+cudaError_t preload_pt2d_f64()
+{
+    cudaFuncAttributes fa;
+    const void* fns[] = {
+        (const void*)pt2d_kernel<F64, LIN, false>,     (const void*)pt2d_kernel<F64, LIN, true>,
+        (const void*)pt2d_kernel<F64, LINSTEP, false>, (const void*)pt2d_kernel<F64, LINSTEP, true>,
+        (const void*)pt2d_kernel<F64, NONLIN, false>,  (const void*)pt2d_kernel<F64, NONLIN, true>,
+        (const void*)judge_kernel,                     (const void*)reset_state_kernel};
+    for (const void* f : fns) {
+        const cudaError_t e = cudaFuncGetAttributes(&fa, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
@@ -253,7 +273,7 @@ cudaError_t launch_reset_state(DevState* st, cudaStream_t s)
 
 cudaError_t launch_to_df64(const double* src, void* dst, long long n, cudaStream_t s)
 {
-    to_df64_kernel<<<152 * 8, 256, 0, s>>>(src, reinterpret_cast<float2*>(dst), n);
+    to_df64_kernel<<<fill_blocks(), 256, 0, s>>>(src, reinterpret_cast<float2*>(dst), n);
     return cudaGetLastError();
 }
 
@@ -266,13 +286,13 @@ __global__ void add_fields_kernel(double* dst, const double* src, long long n)
 
 cudaError_t add_fields(double* dst, const double* src, long long n, cudaStream_t s)
 {
-    add_fields_kernel<<<152 * 8, 256, 0, s>>>(dst, src, n);
+    add_fields_kernel<<<fill_blocks(), 256, 0, s>>>(dst, src, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_from_df64(const void* src, double* dst, long long n, cudaStream_t s)
 {
-    from_df64_kernel<<<152 * 8, 256, 0, s>>>(reinterpret_cast<const float2*>(src), dst, n);
+    from_df64_kernel<<<fill_blocks(), 256, 0, s>>>(reinterpret_cast<const float2*>(src), dst, n);
     return cudaGetLastError();
 }
 

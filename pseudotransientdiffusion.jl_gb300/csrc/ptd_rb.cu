@@ -28,7 +28,7 @@
 // step grows only logarithmically with the residual reduction.
 //
 // Stopping: every nchk iterations the mixed residual of the reference's check
-// (check_res!, scripts/diff_2D_nonlin.jl:167-170) is formed from the base's
+// (check_res!, scripts/diff_2D_nonlin.jl:41-44) is formed from the base's
 // FP64 check residual C_b = div u(H_b) - (H_b - Hold)/dt and the FP32
 // changes; when its norm is <= tol the phase ends early, the base is rebased
 // and the step stops if the FP64 residual of the rebased state is <= tol too
@@ -80,7 +80,7 @@ struct RbDev {
 // Cell parameter of the rebased kernels, every operation explicit (the face
 // parameter is face_c_rn, ptd_device.cuh), so that every kernel variant
 // rounds identically: e = 1/((pi H^3 + sqrt(pi^2 H^6 + fA H^3)) k1 + 1/dt)
-// (nonlin_cell_e, scripts/diff_2D_nonlin.jl:149-152).
+// (nonlin_cell_e, scripts/diff_2D_nonlin.jl:23,26).
 __device__ __forceinline__ float rb_e(const FParams& f, float h3)
 {
     const float q = __fmaf_rn(__fmul_rn(f.fpi2, h3), h3, __fmul_rn(f.fA, h3));
@@ -981,11 +981,11 @@ int rb_capture(RbState* rb)
         }
     }
     if (err == cudaSuccess) {
-        rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, -1, rb->tblk);
+        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, -1, rb->tblk);
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) {
-        rb_base_kernel<<<152 * 8, 256, 0, rb->s>>>(base_args(rb), rb->dev);
+        rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) {
@@ -1104,7 +1104,7 @@ int rb_set_state(RbState* rb, double* H, double* Hold, double* const* wb, const 
     for (int d = 0; d < rb->p.ndim; ++d)
         for (int q = 0; q < 2; ++q) RCK(cudaMemsetAsync(rb->w[d][q], 0, fb, s));
     if (rb->Df) {
-        rb_tofloat_kernel<<<152 * 8, 256, 0, s>>>(D, rb->Df, rb->g.nfield);
+        rb_tofloat_kernel<<<fill_blocks(), 256, 0, s>>>(D, rb->Df, rb->g.nfield);
         RCK(cudaGetLastError());
     }
     if (!rb->gphase) {
@@ -1119,7 +1119,7 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
 {
     rb_reset_kernel<<<1, 1, 0, rb->s>>>(rb->dev);
     RCK(cudaGetLastError());
-    rb_base_kernel<<<152 * 8, 256, 0, rb->s>>>(base_args(rb), rb->dev);
+    rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
     RCK(cudaGetLastError());
     rb_base_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX);
     RCK(cudaGetLastError());
@@ -1155,7 +1155,7 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
         int par = 0;
         long long nl = 0;
         RCK(rb_run_plain(rb, tail, rb->zero_flag, par, nl));
-        rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
+        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
         RCK(cudaGetLastError());
         rb->k.launches += nl + 1;
         iter = rb->p.itmax;
@@ -1179,12 +1179,12 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
 // Fixed FP32 iterations without checks (perf protocol), then one rebase.
 int rb_iterate(RbState* rb, int32_t niter)
 {
-    rb_base_kernel<<<152 * 8, 256, 0, rb->s>>>(base_args(rb), nullptr);
+    rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), nullptr);
     RCK(cudaGetLastError());
     int par = 0;
     long long nl = 0;
     RCK(rb_run_plain(rb, niter, rb->zero_flag, par, nl));
-    rb_fold_kernel<<<152 * 8, 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
+    rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
     RCK(cudaGetLastError());
     rb->k.launches += nl + 2;
     rb->k.iterations += niter;

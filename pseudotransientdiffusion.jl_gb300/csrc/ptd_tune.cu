@@ -1,7 +1,30 @@
 // ptd_tune.cu -- launch-shape choice for the fused kernels.
+#include <mutex>
+
 #include "ptd_internal.h"
 
 namespace ptd {
+
+int sm_count()
+{
+    static std::mutex mu;
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 152;   // only reached when no device is usable; launches then fail anyway
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+            cudaGetLastError();
+            n = 152;
+        }
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
 
 LaunchCfg tuned_config(const ptd_params& p)
 {
@@ -16,11 +39,12 @@ LaunchCfg tuned_config(const ptd_params& p)
         c.warps2d = 2;
         c.chunk2d = 16;
     } else if (p.ndim == 3) {
-        // 512-thread CTAs, 3 resident per SM at <= 40 registers: 456 slots.
+        // 512-thread CTAs, 3 resident per SM at <= 40 registers (456 slots on
+        // the 152 SMs of a GB300).
         // Take the longest z march whose CTA count fills the slots in whole
         // waves to >= 90 % (wave quantization), else the best filling one.
         const int rows = 16;
-        const long long slots = 152 * 3;
+        const long long slots = 3LL * sm_count();
         const long long bxy = (long long)((p.nx - 2 + 30) / 31) * ((p.ny - 2 + rows - 2) / (rows - 1));
         int best = 16;
         double best_eff = -1.0;

@@ -207,7 +207,7 @@ def sample_indices(n: int, k: int = 12) -> np.ndarray:
 
 def iteration_parameters(s: Script, shape) -> dict:
     """The scalar iteration parameters of the script (reference a1 block,
-    e.g. scripts/diff_2D_lin.jl:150-154): dx, Vpdtau, L, Re, theta, dtau."""
+    e.g. scripts/diff_2D_lin.jl:49-53): dx, Vpdtau, L, Re, theta, dtau."""
     lengths = (s.lx, s.ly, s.lz)[: s.ndim]
     h = [lengths[d] / shape[d] for d in range(s.ndim)]
     vpdt = s.cfl * min(h)

@@ -57,6 +57,46 @@ def test_noalloc_matches_allocating_solve_on_two_calls():
         assert np.linalg.norm(H - H_r) <= 1e-12 * np.linalg.norm(H_r)
 
 
+def test_noalloc_leaves_device_memory_unchanged_after_the_startup_call():
+    """The start-up call (nt = 0) reserves the array and loads the kernels;
+    the solves after it, first and second, change no device memory
+    reservation (cudaMemGetInfo's free bytes stay equal)."""
+    torch = pytest.importorskip("torch")
+    s = S.SCRIPTS["diff_2D_nonlin"]
+    shape = (300, 200)
+    p = ptdiff.make_params(s, shape)
+    p0 = ptdiff.make_params(s, shape, nt=0)
+    H0 = S.initial_condition(s, *shape)
+    Hd = torch.from_numpy(np.ravel(H0, order="F").copy()).cuda()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert _lib().ptd_solve_2d_noalloc(C.byref(p0), None, None, stream, None) == 0, _abi.last_error()
+    free = [torch.cuda.mem_get_info()[0]]
+    for _ in range(2):
+        Hd.copy_(torch.from_numpy(np.ravel(H0, order="F").copy()))
+        torch.cuda.synchronize()
+        st = _lib().ptd_solve_2d_noalloc(C.byref(p), C.c_void_p(Hd.data_ptr()), None, stream, None)
+        torch.cuda.synchronize()
+        assert st == 0, _abi.last_error()
+        free.append(torch.cuda.mem_get_info()[0])
+    assert free[0] == free[1] == free[2], free
+
+
+def test_noalloc_rejects_host_memory():
+    s = S.SCRIPTS["diff_2D_linstep"]
+    shape = (64, 64)
+    p = ptdiff.make_params(s, shape)
+    torch = pytest.importorskip("torch")
+    Hd = torch.ones(64 * 64, dtype=torch.float64, device="cuda")
+    Dh = np.ones(64 * 64)
+    st = _lib().ptd_solve_2d_noalloc(C.byref(p), C.c_void_p(Hd.data_ptr()), Dh.ctypes.data_as(C.c_void_p),
+                                     None, None)
+    assert st == _abi.PTD_EINVAL and "D must be device memory" in _abi.last_error()
+    Hh = np.ones(64 * 64)
+    st = _lib().ptd_solve_2d_noalloc(C.byref(p), Hh.ctypes.data_as(C.c_void_p), None, None, None)
+    assert st == _abi.PTD_EINVAL and "H must be device memory" in _abi.last_error()
+
+
 def test_noalloc_rejects_grids_above_the_limit():
     torch = pytest.importorskip("torch")
     s = S.SCRIPTS["diff_2D_nonlin"]
