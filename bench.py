@@ -312,19 +312,26 @@ class GridBench:
         return {"t": times, "iters": iters, "launches": l1 - l0, "iterations": i1 - i0, "H": H_cycle}
 
     def kernel_time(self, sol, n):
-        """Mean launch time of the fused kernel alone: n fixed PT iterations (no checks)."""
+        """Mean time of one PT iteration of the fused kernel alone (fixed
+        iterations, no checks): the time of 2n iterations minus that of n, over
+        n, so that what a call does once (the rebased form's FP64 rebase around
+        its FP32 iterations) drops out."""
         import torch
 
         st = torch.cuda.ExternalStream(sol.stream)
         sol.set_state(self.H0)
         sol.iterate(8)
         sol.sync()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        sol.iterate(n)
-        e1.record(st)
-        e1.synchronize()
-        return e0.elapsed_time(e1) / 1e3 / n
+
+        def run(k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            sol.iterate(k)
+            e1.record(st)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / 1e3
+
+        return (run(2 * n) - run(n)) / n
 
     def e2e(self, precision, K, W):
         """ptd_solve on pinned host buffers, one physical step per call, wall clock."""

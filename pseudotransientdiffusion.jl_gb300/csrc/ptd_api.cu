@@ -8,12 +8,11 @@
 //       if iter % nout == 0: err = norm(ResH)/sqrt(length(ResH))
 //     Hold = H; NaN check
 // with the iterations, the checks and the stopping decision all on the GPU:
-// a CUDA graph holds one check block (nchk fused PT kernels, the last one
-// also forming the residual, then a one-thread judge kernel that computes err
-// and sets a done flag), and the host replays it in growing batches, reading
-// the small device state between batches.  Kernels that find the done flag
-// set return at entry, so the iteration count is exactly the reference's
-// (the first multiple of nchk at which err <= tol).
+// one check block (nchk fused PT kernels, the last one also forming the
+// residual, then a one-thread judge kernel that computes err and sets a done
+// flag) is the body of a WHILE node of a CUDA graph, which the judge ends, so one graph launch runs a whole physical step and the host reads the
+// small device state once per step.  The iteration count is exactly the
+// reference's (the first multiple of nchk at which err <= tol).
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -273,8 +272,9 @@ struct ptd_ctx : ptd_ctx_base {
     double* errhist = nullptr;
     int errcap = 0;
     DevState* h_st = nullptr;     // pinned mirror of *st
-    cudaGraphExec_t gblock[2] = {nullptr, nullptr};
+    cudaGraphExec_t gstep[2] = {nullptr, nullptr};   // one physical step's check loop, per start parity
     cudaGraphExec_t gplain[2] = {nullptr, nullptr};
+    int blocks_per_pass = 1;      // check blocks in the body of the step graph's loop
     int plain_len = 32;
     int cur = 0;                  // buffer holding the current H
     bool have_state = false;
@@ -305,42 +305,70 @@ static void args_for(const ptd_ctx* c, int parity, const int* done, PTArgs& a)
     a.acc = &c->st->acc;
 }
 
-static int capture_block(ptd_ctx* c, int parity, cudaGraphExec_t* out)
+// The PT iteration of one physical step as one CUDA graph: a WHILE node whose
+// body is one check block (nchk fused PT kernels, the last one also forming
+// the residual, then the judge), two blocks when nchk is odd so that every
+// pass of the body starts on the same buffer parity.  The judge ends the loop
+// when the step stops (err <= tol, NaN, or no full block left before itmax),
+// so the graph runs exactly the reference's check blocks, and the host waits
+// once per step.  Every pass of the body raises the iteration count by nchk
+// until the judge stops the loop, so the loop ends within itmax/nchk passes.
+static int capture_step(ptd_ctx* c, int parity, cudaGraphExec_t* out)
 {
     cudaGraph_t g = nullptr;
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    int par = parity;
-    const int nchk = c->p.nchk;
-    int nk = 0;
-    cudaError_t err = cudaSuccess;
-    for (int it = 0; it < nchk && err == cudaSuccess; ++it) {
-        PTArgs a;
-        args_for(c, par, &c->st->done, a);
-        const bool check = it == nchk - 1;
-        if (check && c->p.resid_mode == PTD_RESID_CONSISTENT) {
-            err = launch_pt(a, c->p.ndim, c->p.model, false, c->num, c->cfg, c->stream);
-            if (err == cudaSuccess) err = launch_resid_consistent(a, c->p.ndim, c->p.model, c->num, c->stream);
-            nk += 2;
-        } else {
-            err = launch_pt(a, c->p.ndim, c->p.model, check, c->num, c->cfg, c->stream);
-            nk += 1;
-        }
-        par ^= 1;
-    }
-    if (err == cudaSuccess)
-        err = launch_judge(c->st, c->errhist, c->errcap, nchk, c->p.itmax, c->p.tol, c->dv.norm_den,
-                           c->p.norm == PTD_NORM_MAX, c->stream);
-    nk += 1;
-    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle loop;
+    cudaError_t err = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
     if (err != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
-        return cuda_fail(err, "capture check block");
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "conditional graph node");
     }
-    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    err = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "cudaStreamBeginCaptureToGraph");
+    }
+    const int nchk = c->p.nchk;
+    const int nblk = (nchk & 1) ? 2 : 1;
+    int par = parity;
+    int nk = 0;
+    for (int b = 0; b < nblk && err == cudaSuccess; ++b) {
+        for (int it = 0; it < nchk && err == cudaSuccess; ++it) {
+            PTArgs a;
+            args_for(c, par, &c->st->done, a);
+            const bool check = it == nchk - 1;
+            if (check && c->p.resid_mode == PTD_RESID_CONSISTENT) {
+                err = launch_pt(a, c->p.ndim, c->p.model, false, c->num, c->cfg, c->stream);
+                if (err == cudaSuccess) err = launch_resid_consistent(a, c->p.ndim, c->p.model, c->num, c->stream);
+                nk += 2;
+            } else {
+                err = launch_pt(a, c->p.ndim, c->p.model, check, c->num, c->cfg, c->stream);
+                nk += 1;
+            }
+            par ^= 1;
+        }
+        if (err == cudaSuccess)
+            err = launch_judge_cond(c->st, c->errhist, c->errcap, nchk, c->p.itmax, c->p.tol, c->dv.norm_den,
+                                    c->p.norm == PTD_NORM_MAX, loop, c->stream);
+        nk += 1;
+    }
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &body);
+    if (err != cudaSuccess || e2 != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err != cudaSuccess ? err : e2, "capture the check block of the step graph");
+    }
     cudaError_t e3 = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
-    c->kernels_per_block = nk;
+    c->kernels_per_block = nk / nblk;
+    c->blocks_per_pass = nblk;
     return PTD_OK;
 }
 
@@ -447,7 +475,7 @@ static void free_ctx(ptd_ctx* c)
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (int q = 0; q < 2; ++q) {
-        if (c->gblock[q]) cudaGraphExecDestroy(c->gblock[q]);
+        if (c->gstep[q]) cudaGraphExecDestroy(c->gstep[q]);
         if (c->gplain[q]) cudaGraphExecDestroy(c->gplain[q]);
     }
     if (c->dc) dc_destroy(c->dc);
@@ -543,7 +571,7 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
     } else {
         if ((p->flags & PTD_FLAG_AUTOTUNE) && p->ndim > 1) rc = autotune(c);
         for (int q = 0; q < 2 && !rc; ++q) {
-            if (p->nchk <= p->itmax) rc = capture_block(c, q, &c->gblock[q]);
+            if (p->nchk <= p->itmax) rc = capture_step(c, q, &c->gstep[q]);
             if (!rc) rc = capture_plain(c, q, &c->gplain[q]);
         }
         if (rc) {
@@ -591,11 +619,11 @@ extern "C" int ptd_set_launch_config(ptd_ctx* c, const int32_t cfg[4])
         rc = rb_set_config(c->rb, k);
     } else {
         for (int q = 0; q < 2 && !rc; ++q) {
-            if (c->gblock[q]) cudaGraphExecDestroy(c->gblock[q]);
+            if (c->gstep[q]) cudaGraphExecDestroy(c->gstep[q]);
             if (c->gplain[q]) cudaGraphExecDestroy(c->gplain[q]);
-            c->gblock[q] = nullptr;
+            c->gstep[q] = nullptr;
             c->gplain[q] = nullptr;
-            if (c->p.nchk <= c->p.itmax) rc = capture_block(c, q, &c->gblock[q]);
+            if (c->p.nchk <= c->p.itmax) rc = capture_step(c, q, &c->gstep[q]);
             if (!rc) rc = capture_plain(c, q, &c->gplain[q]);
         }
     }
@@ -750,25 +778,18 @@ static int fp64_step(ptd_ctx* c, int32_t* iters, double* err_hist, int32_t err_c
     CK(launch_reset_state(c->st, c->stream));
     c->launches += 1;
     const long long blocks_max = p.nchk <= p.itmax ? p.itmax / p.nchk : 0;
-    long long launched = 0;
-    long long batch = 1;
     const int start = c->cur;
     int done = DONE_RUNNING, iter = 0, nchecks = 0;
-    while (launched < blocks_max) {
-        const long long nb = std::min(batch, blocks_max - launched);
-        for (long long b = 0; b < nb; ++b) {
-            const int par = (int)((start + (launched + b) * p.nchk) & 1);
-            CK(cudaGraphLaunch(c->gblock[par], c->stream));
-            c->launches += c->kernels_per_block;
-        }
-        launched += nb;
+    if (blocks_max > 0) {
+        CK(cudaGraphLaunch(c->gstep[start], c->stream));
         CK(cudaMemcpyAsync(c->h_st, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         done = c->h_st->done;
         iter = c->h_st->iter;
         nchecks = c->h_st->nchecks;
-        if (done != DONE_RUNNING) break;
-        batch = std::min<long long>(batch * 2, 64);
+        // every pass of the loop body launches blocks_per_pass check blocks
+        const long long passes = (nchecks + c->blocks_per_pass - 1) / c->blocks_per_pass;
+        c->launches += passes * c->blocks_per_pass * c->kernels_per_block;
     }
     c->iterations += iter;
     c->cur = (start + iter) & 1;

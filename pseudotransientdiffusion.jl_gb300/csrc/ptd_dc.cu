@@ -178,9 +178,17 @@ __global__ void dc_outer_judge_kernel(DcDev* st, double norm_den, int norm_max, 
     st->best = err;
 }
 
-__global__ void dc_inner_judge_kernel(DcDev* st, int nchk, int itmax, double norm_den, int norm_max, int stall)
+// The inner judge, at the end of the body of the inner solve graph's WHILE
+// node: it ends the loop when the inner solve stops.  Every pass adds nchk
+// iterations until no further block fits in the solve's budget (cap), so the
+// loop ends within cap/nchk passes.
+__global__ void dc_inner_judge_kernel(DcDev* st, int nchk, double norm_den, int norm_max, int stall,
+                                      cudaGraphConditionalHandle loop)
 {
-    if (st->done) return;
+    if (st->done) {
+        cudaGraphSetConditional(loop, 0);
+        return;
+    }
     const double acc = st->acc;
     st->acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
@@ -192,14 +200,24 @@ __global__ void dc_inner_judge_kernel(DcDev* st, int nchk, int itmax, double nor
         st->best_at = st->nchecks;
     }
     if (!(err > st->target)) st->done = (err != err) ? DONE_NAN : DONE_CONVERGED;
-    else if (st->iter + nchk > itmax) st->done = DONE_CAP;
+    else if (st->iter + nchk > st->cap) st->done = DONE_CAP;
     // FP32 attainable accuracy reached (about eps_32 * cond(J)): the inner
     // residual has stopped decreasing (no 5% gain over the last `stall`
     // checks, a window that grows with the grid so that the PT transient of
     // a large grid is not mistaken for stagnation); the FP64 outer
     // correction takes over from here.
     else if (st->nchecks - st->best_at >= stall) st->done = DONE_CONVERGED;
+    if (st->done) cudaGraphSetConditional(loop, 0);
 }
+
+// The iteration budget and the pass counter of the next inner solve.
+__global__ void dc_inner_start_kernel(DcDev* st, int cap)
+{
+    st->cap = cap;
+    st->passes = 0;
+}
+
+__global__ void dc_count_pass_kernel(DcDev* st) { st->passes += 1; }
 
 // ---------------------------------------------------------------------------
 struct DcState {
@@ -302,36 +320,64 @@ static void dc_args(const DcState* dc, int parity, const int* done, DcArgs& a)
         if (_e != cudaSuccess) return cuda_fail(_e, #call);       \
     } while (0)
 
+// One inner solve as one CUDA graph: a WHILE node whose body is one check
+// block (nchk/tb inner launches and the inner judge; two blocks when that
+// launch count is odd, so that every pass starts on the same buffer parity),
+// ended by the judge.
 static int dc_capture(DcState* dc, int parity)
 {
     cudaGraph_t g = nullptr;
-    DCK(cudaStreamBeginCapture(dc->s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t err = cudaSuccess;
+    DCK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle loop;
+    cudaError_t err = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "conditional graph node");
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    err = cudaStreamBeginCaptureToGraph(dc->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "cudaStreamBeginCaptureToGraph");
+    }
     int par = parity, nk = 0;
     const int nl = dc->nchk / dc->tb;   // launches per check block
-    for (int it = 0; it < nl && err == cudaSuccess; ++it) {
-        DcArgs a;
-        dc_args(dc, par, &dc->dev->done, a);
-        err = dc_launch(a, dc->ndim, dc->model, it == nl - 1, dc->cfg, dc->s, dc->tb);
-        ++nk;
-        par ^= 1;
+    const int nblk = (nl & 1) ? 2 : 1;
+    for (int b = 0; b < nblk && err == cudaSuccess; ++b) {
+        for (int it = 0; it < nl && err == cudaSuccess; ++it) {
+            DcArgs a;
+            dc_args(dc, par, &dc->dev->done, a);
+            err = dc_launch(a, dc->ndim, dc->model, it == nl - 1, dc->cfg, dc->s, dc->tb);
+            ++nk;
+            par ^= 1;
+        }
+        if (err == cudaSuccess && b == 0) {
+            dc_count_pass_kernel<<<1, 1, 0, dc->s>>>(dc->dev);
+            err = cudaGetLastError();
+            ++nk;
+        }
+        if (err == cudaSuccess) {
+            dc_inner_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->nchk, dc->dv.norm_den, dc->p.norm == PTD_NORM_MAX,
+                                                       dc->stall, loop);
+            err = cudaGetLastError();
+            ++nk;
+        }
     }
-    if (err == cudaSuccess) {
-        dc_inner_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->nchk, dc->p.itmax, dc->dv.norm_den,
-                                                   dc->p.norm == PTD_NORM_MAX, dc->stall);
-        err = cudaGetLastError();
-        ++nk;
+    cudaError_t e2 = cudaStreamEndCapture(dc->s, &body);
+    if (err != cudaSuccess || e2 != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err != cudaSuccess ? err : e2, "capture inner block");
     }
-    cudaError_t e2 = cudaStreamEndCapture(dc->s, &g);
-    if (err != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
-        return cuda_fail(err, "capture inner block");
-    }
-    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
     cudaError_t e3 = cudaGraphInstantiate(&dc->gblock[parity], g, 0);
     cudaGraphDestroy(g);
     if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
-    dc->kernels_per_block = nk;
+    dc->kernels_per_block = nk;   // per pass
     return PTD_OK;
 }
 
@@ -475,24 +521,15 @@ static int dc_inner(DcState* dc, long long budget, int* iters)
         DCK(cudaMemsetAsync(dc->w[d][1], 0, fb, dc->s));
     }
     dc->cur = 0;
-    const long long blocks_max = std::max<long long>(1, budget / dc->nchk);
-    long long launched = 0, batch = 1;
-    int done = DONE_RUNNING, iter = 0;
-    while (launched < blocks_max) {
-        const long long nb = std::min(batch, blocks_max - launched);
-        for (long long b = 0; b < nb; ++b) {
-            const int par = (int)(((launched + b) * (dc->nchk / dc->tb)) & 1);
-            DCK(cudaGraphLaunch(dc->gblock[par], dc->s));
-            dc->k.launches += dc->kernels_per_block;
-        }
-        launched += nb;
-        DCK(cudaMemcpyAsync(dc->h_dev, dc->dev, sizeof(DcDev), cudaMemcpyDeviceToHost, dc->s));
-        DCK(cudaStreamSynchronize(dc->s));
-        done = dc->h_dev->done;
-        iter = dc->h_dev->iter;
-        if (done != DONE_RUNNING) break;
-        batch = std::min<long long>(batch * 2, 32);
-    }
+    // at least one block even when the step's budget is spent (as before)
+    const long long cap = std::max<long long>(dc->nchk, std::min<long long>(budget, 1LL << 30));
+    dc_inner_start_kernel<<<1, 1, 0, dc->s>>>(dc->dev, (int)cap);
+    DCK(cudaGetLastError());
+    DCK(cudaGraphLaunch(dc->gblock[0], dc->s));
+    DCK(cudaMemcpyAsync(dc->h_dev, dc->dev, sizeof(DcDev), cudaMemcpyDeviceToHost, dc->s));
+    DCK(cudaStreamSynchronize(dc->s));
+    const int iter = dc->h_dev->iter;
+    dc->k.launches += 1 + (long long)dc->h_dev->passes * dc->kernels_per_block;
     dc->cur = (iter / dc->tb) & 1;   // one buffer swap per launch
     dc->k.iterations += iter;
     *iters = iter;

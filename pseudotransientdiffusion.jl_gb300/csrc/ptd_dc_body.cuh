@@ -41,6 +41,8 @@ struct DcDev {
     double outer_acc;  // FP64 residual accumulator
     double outer_err;  // FP64 residual norm
     unsigned long long hmax_bits;  // max |H| over the grid (bit pattern), for the FP32 floor
+    int cap;           // inner iterations allowed to this inner solve (the step's remaining budget)
+    int passes;        // passes of the inner solve graph's loop
 };
 
 // One face of the linearised flux (scaled like ptd_device.cuh):

@@ -8,7 +8,7 @@
 //       fluxes and D double-floats.  Only the operations that need H's full
 //       53 bits run on the FP64 pipe (below).
 //
-// GB300 executes FP64 at ~1/72 of its FP32 rate (measured: 0.50 T DFMA/s
+// GB300 executes FP64 at ~1/58 of its FP32 rate (measured: 0.627 T DFMA/s
 // against 36.5 T FFMA/s), so a PT iteration done in native FP64 is bound by
 // the FP64 pipe long before HBM.  A DF64 value occupies the same 8 bytes as a
 // double, so the DF64 kernels move exactly the bytes of the FP64 kernels while
@@ -202,6 +202,73 @@ struct DFH : DF64 {
         return fma(-ed, f2d_bits(rp.y), fma(-ed, f2d_bits(rp.x), h.d));
     }
 };
+
+// ---------------------------------------------------------------------------
+// Two double-floats at once (the values of two faces): component .x of hi and
+// lo is the first value, .y the second.  Every operation is the DF64 one above
+// done with FP32x2 instructions (__fadd2_rn, __fmul2_rn, __ffma2_rn: one
+// instruction for both components, each rounded exactly like the scalar
+// operation), so each component is bit for bit what the scalar DF64 code
+// gives; the double-float arithmetic of two faces issues as many
+// instructions as that of one.
+struct DF2 {
+    float2 hi, lo;
+};
+
+__device__ __forceinline__ DF2 df2_pack(float2 a, float2 b) { return DF2{make_float2(a.x, b.x), make_float2(a.y, b.y)}; }
+__device__ __forceinline__ float2 df2_first(const DF2& v) { return make_float2(v.hi.x, v.lo.x); }
+__device__ __forceinline__ float2 df2_second(const DF2& v) { return make_float2(v.hi.y, v.lo.y); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ void df2_two_sum(float2 a, float2 b, float2& s, float2& e)
+{
+    s = add2(a, b);
+    const float2 bb = sub2(s, a);
+    e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+__device__ __forceinline__ DF2 df2_fast_two_sum(float2 a, float2 b)
+{
+    const float2 s = add2(a, b);
+    return DF2{s, sub2(b, sub2(s, a))};
+}
+__device__ __forceinline__ DF2 df2_add(const DF2& a, const DF2& b)
+{
+    float2 s, e;
+    df2_two_sum(a.hi, b.hi, s, e);
+    return df2_fast_two_sum(s, add2(e, add2(a.lo, b.lo)));
+}
+__device__ __forceinline__ DF2 df2_sub(const DF2& a, const DF2& b)
+{
+    return df2_add(a, DF2{neg2(b.hi), neg2(b.lo)});
+}
+__device__ __forceinline__ DF2 df2_mul(const DF2& a, const DF2& b)
+{
+    const float2 p = mul2(a.hi, b.hi);
+    float2 e = fma2(a.hi, b.hi, neg2(p));
+    e = fma2(a.hi, b.lo, e);
+    e = fma2(a.lo, b.hi, e);
+    return df2_fast_two_sum(p, e);
+}
+// a*b + c (DF64::mad)
+__device__ __forceinline__ DF2 df2_mad(const DF2& a, const DF2& b, const DF2& c)
+{
+    const float2 p = mul2(a.hi, b.hi);
+    float2 e = fma2(a.hi, b.hi, neg2(p));
+    e = fma2(a.hi, b.lo, e);
+    e = fma2(a.lo, b.hi, e);
+    float2 s, t;
+    df2_two_sum(p, c.hi, s, t);
+    return df2_fast_two_sum(s, add2(t, add2(e, c.lo)));
+}
+// w - c*t with float coefficients c (DF64::nmadf)
+__device__ __forceinline__ DF2 df2_nmadf(const DF2& t, float2 c, const DF2& w)
+{
+    const float2 p = mul2(t.hi, c);
+    const float2 e = fma2(t.lo, c, fma2(t.hi, c, neg2(p)));
+    float2 s, u;
+    df2_two_sum(w.hi, neg2(p), s, u);
+    return df2_fast_two_sum(s, add2(u, sub2(w.lo, e)));
+}
 
 // Split a double into a double-float (host or device).
 __host__ __device__ __forceinline__ float2 split_df(double x)

@@ -112,10 +112,12 @@ __global__ void __launch_bounds__(256) resid_consistent_kernel(PTArgs a, int ndi
     block_reduce_residual(a, part, pmax);
 }
 
-__global__ void judge_kernel(DevState* st, double* errhist, int errcap, int nchk, int itmax,
-                             double tol, double norm_den, int norm_max)
+// The check of one block: err from the accumulated residual, appended to the
+// error history; the step stops at err <= tol, NaN, or when no full check
+// block fits before itmax.  Returns the new done state.
+__device__ __forceinline__ int judge_step(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
+                                          double norm_den, int norm_max)
 {
-    if (st->done) return;
     const double acc = st->acc;
     st->acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
@@ -124,8 +126,30 @@ __global__ void judge_kernel(DevState* st, double* errhist, int errcap, int nchk
     st->nchecks = n + 1;
     st->iter += nchk;
     st->err = err;
-    if (!(err > tol)) st->done = (err != err) ? DONE_NAN : DONE_CONVERGED;
-    else if (st->iter + nchk > itmax) st->done = DONE_CAP;
+    int done = DONE_RUNNING;
+    if (!(err > tol)) done = (err != err) ? DONE_NAN : DONE_CONVERGED;
+    else if (st->iter + nchk > itmax) done = DONE_CAP;
+    st->done = done;
+    return done;
+}
+
+__global__ void judge_kernel(DevState* st, double* errhist, int errcap, int nchk, int itmax,
+                             double tol, double norm_den, int norm_max)
+{
+    if (st->done) return;
+    judge_step(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max);
+}
+
+// The judge at the end of the body of a WHILE graph node: when the step stops
+// it also ends the loop (the node's condition is set to 0), so the graph runs
+// exactly the check blocks of the step, with no host round trip.
+__global__ void judge_cond_kernel(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
+                                  double norm_den, int norm_max, cudaGraphConditionalHandle loop)
+{
+    // a step already stopped (a second block in the body after the stop)
+    // leaves the loop too
+    if (st->done || judge_step(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max) != DONE_RUNNING)
+        cudaGraphSetConditional(loop, 0);
 }
 
 __global__ void reset_state_kernel(DevState* st)
@@ -262,6 +286,13 @@ cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, in
                          double norm_den, int norm_max, cudaStream_t s)
 {
     judge_kernel<<<1, 1, 0, s>>>(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_judge_cond(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
+                              double norm_den, int norm_max, cudaGraphConditionalHandle loop, cudaStream_t s)
+{
+    judge_cond_kernel<<<1, 1, 0, s>>>(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max, loop);
     return cudaGetLastError();
 }
 

@@ -62,6 +62,64 @@ __device__ __forceinline__ typename N::T face_t(const PTArgs& a, const typename 
     return nmadf(N(), c, t, w);
 }
 
+// ---------------------------------------------------------------------------
+// Two faces of one cell at once (the double-float forms): the same arithmetic
+// as two face_t calls, packed into FP32x2 instructions (DF2, ptd_num.cuh), so
+// every component is bit for bit the scalar result.  L is the cell, Ra / Rb
+// its neighbours across the two faces.
+__device__ __forceinline__ DF2 hdiff2(DF64, float2 L, float2 Ra, float2 Rb)
+{
+    return df2_sub(df2_pack(Ra, Rb), df2_pack(L, L));
+}
+__device__ __forceinline__ DF2 hdiff2(DFH, const DFH::HV& L, const DFH::HV& Ra, const DFH::HV& Rb)
+{
+    // FP64 differences, split with integer operations (DFH::hdiff)
+    return df2_pack(split_bits(Ra.d - L.d), split_bits(Rb.d - L.d));
+}
+__device__ __forceinline__ DF2 hsum2(DF64, float2 L, float2 Ra, float2 Rb)
+{
+    return df2_add(df2_pack(L, L), df2_pack(Ra, Rb));
+}
+__device__ __forceinline__ DF2 hsum2(DFH, const DFH::HV& L, const DFH::HV& Ra, const DFH::HV& Rb)
+{
+    return df2_add(df2_pack(L.f, L.f), df2_pack(Ra.f, Rb.f));
+}
+
+template <class N, int MODEL, bool U>
+__device__ __forceinline__ DF2 face2_t(const PTArgs& a, const typename N::HV& HL, const typename N::HV& HRa,
+                                       const typename N::HV& HRb, float hsa, float hsb, float2 DL, float2 DRa,
+                                       float2 DRb, const DF2& w, DF2& u)
+{
+    const DF2 g = hdiff2(N(), HL, HRa, HRb);
+    if (MODEL == LIN) {
+        if (U) u = g;
+        return df2_nmadf(df2_add(g, w), f2(a.fc_lin), w);
+    }
+    float2 c;
+    DF2 K;
+    if (MODEL == LINSTEP) {
+        K = df2_add(df2_pack(DL, DL), df2_pack(DRa, DRb));
+        c = f2(a.fc_lin);
+    } else if (MODEL == NONLIN) {
+        const DF2 s = hsum2(N(), HL, HRa, HRb);
+        K = df2_mul(df2_mul(s, s), s);
+        c = f2(nonlin_face_c(a.f, hsa), nonlin_face_c(a.f, hsb));
+    } else {   // NONLIN_EXPM
+        const DF2 s = hsum2(N(), HL, HRa, HRb);
+        const DF2 e2 = df2_add(df2_pack(DL, DL), df2_pack(DRa, DRb));
+        K = df2_mul(df2_mul(df2_mul(s, s), s), e2);
+        c = f2(nonlin_face_c(a.f, hsa, 0.5f * e2.hi.x), nonlin_face_c(a.f, hsb, 0.5f * e2.hi.y));
+    }
+    DF2 t;
+    if (U) {
+        u = df2_mul(K, g);
+        t = df2_add(u, w);
+    } else {
+        t = df2_mad(K, g, w);
+    }
+    return df2_nmadf(t, c, w);
+}
+
 template <class N>
 __device__ __forceinline__ typename N::T cst(const PTArgs& a, int which);
 // which: 0..2 sigma_d, 3 rdt, 4 rdt/sigma (square cells)
@@ -211,9 +269,23 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
                 if (HASD) Dr = ok ? ld<N>(a.D, idx + 1) : Dc;
             }
             const float hn = N::hf(Hn);
-            T ux = N::zero(), uy = N::zero(), wxn = N::zero(), wyn = N::zero();
-            if (xface) wxn = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + hr, Dc, Dr, wx, ux);
-            if (upd) wyn = face_t<N, MODEL, CHECK>(a, Hc, Hn, hc + hn, Dc, Dn, wy, uy);
+            T ux = N::zero(), uy = N::zero(), wxn = N::zero(), wyn = N::zero(), dx, dy, dux, duy;
+            if constexpr (N::native) {
+                if (xface) wxn = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + hr, Dc, Dr, wx, ux);
+                if (upd) wyn = face_t<N, MODEL, CHECK>(a, Hc, Hn, hc + hn, Dc, Dn, wy, uy);
+            } else {
+                // both faces in one packed evaluation (lanes that need only one
+                // of them discard the other)
+                DF2 u2;
+                const DF2 w2 = face2_t<N, MODEL, CHECK>(a, Hc, Hr, Hn, hc + hr, hc + hn, Dc, Dr, Dn,
+                                                        df2_pack(wx, wy), u2);
+                wxn = df2_first(w2);
+                wyn = df2_second(w2);
+                if (CHECK) {
+                    ux = df2_first(u2);
+                    uy = df2_second(u2);
+                }
+            }
             const T wxl = N::shfl_up(wxn, 1);
             const T uxl = CHECK ? N::shfl_up(ux, 1) : N::zero();
             const float dlf = MODEL == LINSTEP ? __shfl_up_sync(FULL, dcf, 1) : 0.0f;
@@ -224,16 +296,34 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
                 const float dmax = MODEL == LINSTEP ? fmaxf(fmaxf(fmaxf(dcf, dlf), fmaxf(N::lo_f(Dr), dbf)), dnf)
                                                     : (MODEL == NONLIN_EXPM ? N::lo_f(Dc) : 0.0f);
                 const float e = cell_e<MODEL>(a, hc, dmax);
+                // the flux differences (x, y), packed for the double-float forms
+                if constexpr (N::native) {
+                    dx = N::sub(wxn, wxl);
+                    dy = N::sub(wyn, wyb);
+                    if (CHECK) {
+                        dux = N::sub(ux, uxl);
+                        duy = N::sub(uy, uyb);
+                    }
+                } else {
+                    const DF2 d2 = df2_sub(df2_pack(wxn, wyn), df2_pack(wxl, wyb));
+                    dx = df2_first(d2);
+                    dy = df2_second(d2);
+                    if (CHECK) {
+                        const DF2 du2 = df2_sub(df2_pack(ux, uy), df2_pack(uxl, uyb));
+                        dux = df2_first(du2);
+                        duy = df2_second(du2);
+                    }
+                }
                 HS Hnew;
                 if (a.sq) {
-                    Hnew = h_update_sq<N>(a, Hc, Ho, N::add(N::sub(wyn, wyb), N::sub(wxn, wxl)), e);
+                    Hnew = h_update_sq<N>(a, Hc, Ho, N::add(dy, dx), e);
                 } else {
-                    const T div = N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0)));
+                    const T div = N::mad(dy, cst<N>(a, 1), N::mul(dx, cst<N>(a, 0)));
                     Hnew = h_update<N>(a, Hc, Ho, div, e);
                 }
                 N::sth(a.Hout, idx, Hnew);
                 if (CHECK) {
-                    const T divu = N::mad(N::sub(uy, uyb), cst<N>(a, 1), N::mul(N::sub(ux, uxl), cst<N>(a, 0)));
+                    const T divu = N::mad(duy, cst<N>(a, 1), N::mul(dux, cst<N>(a, 0)));
                     const T r = N::sub(divu, N::mul(N::hdn(Hnew, Ho), cst<N>(a, 3)));
                     accumulate_residual(N::to_d(r), part, pmax);
                 }
@@ -348,8 +438,21 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
             const float hn = N::hf(Hn);
             const float dnf = MODEL == LINSTEP ? N::lo_f(Dn) : 0.0f;
             T ux = N::zero(), uy = N::zero(), uz = N::zero(), wxn = N::zero(), wyn = N::zero(), wzn = N::zero();
-            if (xface) wxn = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + hr, Dc, Dr, wx, ux);
-            if (yface) wyn = face_t<N, MODEL, CHECK>(a, Hc, Hu, hc + hu, Dc, Du, wy, uy);
+            if constexpr (N::native) {
+                if (xface) wxn = face_t<N, MODEL, CHECK>(a, Hc, Hr, hc + hr, Dc, Dr, wx, ux);
+                if (yface) wyn = face_t<N, MODEL, CHECK>(a, Hc, Hu, hc + hu, Dc, Du, wy, uy);
+            } else {
+                // the x and y faces in one packed evaluation
+                DF2 u2;
+                const DF2 w2 = face2_t<N, MODEL, CHECK>(a, Hc, Hr, Hu, hc + hr, hc + hu, Dc, Dr, Du,
+                                                        df2_pack(wx, wy), u2);
+                wxn = df2_first(w2);
+                wyn = df2_second(w2);
+                if (CHECK) {
+                    ux = df2_first(u2);
+                    uy = df2_second(u2);
+                }
+            }
             if (upd) wzn = face_t<N, MODEL, CHECK>(a, Hc, Hn, hc + hn, Dc, Dn, wz, uz);
             if (own_x) st<N>(a.wout[0], idx, wxn);
             if (own_y) st<N>(a.wout[1], idx, wyn);
@@ -370,20 +473,38 @@ __device__ __forceinline__ void pt3d_body(const PTArgs& a, int bx, int by, int b
                                                             fmaxf(fmaxf(ddf, dbf), dnf))
                                                     : (MODEL == NONLIN_EXPM ? N::lo_f(Dc) : 0.0f);
                 const float e = cell_e<MODEL>(a, hc, dmax);
+                // the flux differences (x, y packed for the double-float forms; z)
+                T dx, dy, dux, duy;
+                const T dz = N::sub(wzn, wzb);
+                if constexpr (N::native) {
+                    dx = N::sub(wxn, wxl);
+                    dy = N::sub(wyn, wyb);
+                    if (CHECK) {
+                        const T uyb = sU[p][r - 1][lane];
+                        dux = N::sub(ux, uxl);
+                        duy = N::sub(uy, uyb);
+                    }
+                } else {
+                    const DF2 d2 = df2_sub(df2_pack(wxn, wyn), df2_pack(wxl, wyb));
+                    dx = df2_first(d2);
+                    dy = df2_second(d2);
+                    if (CHECK) {
+                        const T uyb = sU[p][r - 1][lane];
+                        const DF2 du2 = df2_sub(df2_pack(ux, uy), df2_pack(uxl, uyb));
+                        dux = df2_first(du2);
+                        duy = df2_second(du2);
+                    }
+                }
                 HS Hnew;
                 if (a.sq) {
-                    const T dsum = N::add(N::add(N::sub(wzn, wzb), N::sub(wyn, wyb)), N::sub(wxn, wxl));
-                    Hnew = h_update_sq<N>(a, Hc, Ho, dsum, e);
+                    Hnew = h_update_sq<N>(a, Hc, Ho, N::add(N::add(dz, dy), dx), e);
                 } else {
-                    const T div = N::mad(N::sub(wzn, wzb), cst<N>(a, 2),
-                                         N::mad(N::sub(wyn, wyb), cst<N>(a, 1), N::mul(N::sub(wxn, wxl), cst<N>(a, 0))));
+                    const T div = N::mad(dz, cst<N>(a, 2), N::mad(dy, cst<N>(a, 1), N::mul(dx, cst<N>(a, 0))));
                     Hnew = h_update<N>(a, Hc, Ho, div, e);
                 }
                 N::sth(a.Hout, idx, Hnew);
                 if (CHECK) {
-                    const T uyb = sU[p][r - 1][lane];
-                    const T divu = N::mad(N::sub(uz, uzb), cst<N>(a, 2),
-                                          N::mad(N::sub(uy, uyb), cst<N>(a, 1), N::mul(N::sub(ux, uxl), cst<N>(a, 0))));
+                    const T divu = N::mad(N::sub(uz, uzb), cst<N>(a, 2), N::mad(duy, cst<N>(a, 1), N::mul(dux, cst<N>(a, 0))));
                     const T r2 = N::sub(divu, N::mul(N::hdn(Hnew, Ho), cst<N>(a, 3)));
                     accumulate_residual(N::to_d(r2), part, pmax);
                 }

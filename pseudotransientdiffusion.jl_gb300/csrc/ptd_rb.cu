@@ -70,7 +70,8 @@ struct RbDev {
     int phase_iter;   // PT iterations of this phase (the buffer parity)
     int nchecks;
     int capped;
-    int pad0, pad1;
+    int phases;       // phases run in this step (passes of the step graph's loop)
+    int pad1;
     double acc;       // FP32 check residual accumulator (sum or max bits)
     double acc64;     // FP64 base residual accumulator
     double err;       // last FP32 check err
@@ -717,6 +718,7 @@ __global__ void rb_reset_kernel(RbDev* st)
     st->phase_iter = 0;
     st->nchecks = 0;
     st->capped = 0;
+    st->phases = 0;
     st->acc = 0.0;
     st->acc64 = 0.0;
     st->err = 0.0;
@@ -752,10 +754,20 @@ __global__ void rb_check_judge_kernel(RbDev* st, double* errhist, int errcap, in
     }
 }
 
-// After each rebase: the FP64 err of the base.
-__global__ void rb_base_judge_kernel(RbDev* st, double tol, double norm_den, int norm_max)
+// After each rebase: the FP64 err of the base.  In the body of the step
+// graph's WHILE node (in_loop) it also counts the phase and ends the loop
+// once the step has stopped.  Every phase adds at least one check block of
+// nchk iterations (its first judge runs with skip clear) and a phase that
+// leaves no room for another block before itmax ends the step (capped), so
+// the loop ends within itmax/nchk passes.
+__global__ void rb_base_judge_kernel(RbDev* st, double tol, double norm_den, int norm_max,
+                                     cudaGraphConditionalHandle loop, int in_loop)
 {
-    if (st->step_done) return;
+    if (in_loop) st->phases += 1;
+    if (st->step_done) {
+        if (in_loop) cudaGraphSetConditional(loop, 0);
+        return;
+    }
     const double acc = st->acc64;
     st->acc64 = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
@@ -771,6 +783,7 @@ __global__ void rb_base_judge_kernel(RbDev* st, double tol, double norm_den, int
     } else {
         st->skip = 0;
     }
+    if (in_loop && st->step_done) cudaGraphSetConditional(loop, 0);
 }
 
 __global__ void rb_tofloat_kernel(const double* src, float* dst, long long n)
@@ -954,14 +967,33 @@ RbBaseArgs base_args(const RbState* rb)
     return b;
 }
 
-// One phase: blocks of nchk iterations each followed by the FP32 judge, then
-// the rebase (fold, base quantities, FP64 judge).  Every phase starts from
+// The rebased PT iteration of one physical step as one CUDA graph: a WHILE
+// node whose body is one phase -- blocks of nchk iterations each followed by
+// the FP32 judge, then the rebase (fold, base quantities, FP64 judge) -- and
+// which the FP64 judge ends when the step stops.  Every phase starts from
 // buffer parity 0.
 int rb_capture(RbState* rb)
 {
     cudaGraph_t g = nullptr;
-    RCK(cudaStreamBeginCapture(rb->s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t err = cudaSuccess;
+    RCK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle loop;
+    cudaError_t err = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "conditional graph node");
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    err = cudaStreamBeginCaptureToGraph(rb->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "cudaStreamBeginCaptureToGraph");
+    }
     int par = 0, nk = 0;
     const int nchk = rb->p.nchk;
     const int nl = nchk / rb->tblk;   // launches per check block (tb divides nchk)
@@ -989,16 +1021,16 @@ int rb_capture(RbState* rb)
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) {
-        rb_base_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX);
+        rb_base_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX,
+                                                 loop, 1);
         err = cudaGetLastError();
     }
     nk += 3;
-    cudaError_t e2 = cudaStreamEndCapture(rb->s, &g);
-    if (err != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
-        return cuda_fail(err, "capture rebased phase");
+    cudaError_t e2 = cudaStreamEndCapture(rb->s, &body);
+    if (err != cudaSuccess || e2 != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err != cudaSuccess ? err : e2, "capture rebased phase");
     }
-    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
     cudaError_t e3 = cudaGraphInstantiate(&rb->gphase, g, 0);
     cudaGraphDestroy(g);
     if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
@@ -1121,27 +1153,19 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
     RCK(cudaGetLastError());
     rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
     RCK(cudaGetLastError());
-    rb_base_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX);
+    rb_base_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX,
+                                             cudaGraphConditionalHandle{}, 0);
     RCK(cudaGetLastError());
     rb->k.launches += 3;
-    const long long per_phase = (long long)rb->blocks_per_phase * rb->p.nchk;
-    const long long phases_max =
-        rb->p.nchk <= rb->p.itmax ? rb->p.itmax / std::max<long long>(per_phase, 1) + rb->p.itmax / rb->p.nchk + 2 : 0;
-    long long launched = 0, batch = 1;
     rb->h_dev->step_done = DONE_RUNNING;
     rb->h_dev->iter = 0;
     rb->h_dev->nchecks = 0;
-    while (launched < phases_max) {
-        const long long nb = std::min(batch, phases_max - launched);
-        for (long long b = 0; b < nb; ++b) {
-            RCK(cudaGraphLaunch(rb->gphase, rb->s));
-            rb->k.launches += rb->kernels_per_phase;
-        }
-        launched += nb;
+    if (rb->p.nchk <= rb->p.itmax) {
+        // the whole step: phases until the FP64 judge stops it
+        RCK(cudaGraphLaunch(rb->gphase, rb->s));
         RCK(cudaMemcpyAsync(rb->h_dev, rb->dev, sizeof(RbDev), cudaMemcpyDeviceToHost, rb->s));
         RCK(cudaStreamSynchronize(rb->s));
-        if (rb->h_dev->step_done != DONE_RUNNING) break;
-        batch = std::min<long long>(batch * 2, 16);
+        rb->k.launches += (long long)rb->h_dev->phases * rb->kernels_per_phase;
     }
     const RbDev& st = *rb->h_dev;
     int32_t iter = st.iter;

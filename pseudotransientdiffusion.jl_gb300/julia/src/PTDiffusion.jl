@@ -16,9 +16,9 @@ is what the tests exercise.
 module PTDiffusion
 
 export PtdParams, diffusion_1D_, diffusion_2D_, diffusion_3D_, diffusion_react_1D_, diffusion_react_2D_,
-       solve!, AdjointSolver, misfit
+       solve!, AdjointSolver, misfit, forward!, gradient!
 
-const libptd = joinpath(@__DIR__, "..", "libptd.so")
+const libptd = joinpath(@__DIR__, "..", "..", "libptd.so")
 
 const PTD_OK = Cint(0)
 const MODEL = Dict(:lin => Int32(0), :linstep => Int32(1), :nonlin => Int32(2))
@@ -229,18 +229,8 @@ L2 misfit of the final state; differentiable through the ChainRulesCore
 """
 misfit(a::AdjointSolver, m, H0, Ht) = forward!(a, H0, m, Ht)
 
-# ChainRulesCore is a weak dependency: the rule is defined when it is loaded.
-if isdefined(Main, :ChainRulesCore)
-    import ChainRulesCore
-    function ChainRulesCore.rrule(::typeof(misfit), a::AdjointSolver, m, H0, Ht)
-        L = forward!(a, H0, m, Ht)
-        function misfit_pullback(dL)
-            gm, gh = gradient!(a)
-            return ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), dL .* gm, dL .* gh,
-                   ChainRulesCore.NoTangent()
-        end
-        return L, misfit_pullback
-    end
-end
+# The ChainRulesCore rrule of `misfit` is the package extension
+# ext/PTDiffusionChainRulesCoreExt.jl (ChainRulesCore is a weak dependency:
+# Julia loads the extension whenever both packages are loaded, in any order).
 
 end # module

@@ -6,7 +6,7 @@ D = H^3): ``forward(H0, m, Ht)`` runs ``params.nt`` implicit steps keeping one
 checkpoint per step and returns L = 1/2 sum_inner (H^nt - Ht)^2;
 ``gradient()`` returns (dL/dm, dL/dH0).  ``DiffusionMisfit`` is the
 torch.autograd.Function over the same calls (the Python counterpart of the
-Julia ChainRulesCore rrule in julia/PTDiffusion.jl).  No reference counterpart.
+Julia ChainRulesCore rrule in the package extension julia/ext/PTDiffusionChainRulesCoreExt.jl).  No reference counterpart.
 """
 from __future__ import annotations
 
@@ -124,24 +124,25 @@ class AdjointSolver:
 def misfit_function():
     """torch.autograd.Function computing L(m, H0) = 1/2 ||H^nt(m, H0) - Ht||^2
     with the library's forward and adjoint (float64 tensors, x fastest,
-    shape (nz, ny, nx) in torch's C order)."""
+    shape (nz, ny, nx) in torch's C order, which is the library's layout).
+    The tensors go to the library as they are -- device tensors as device
+    pointers, so a CUDA tensor is never copied through the host -- and the
+    gradients are written into tensors on the inputs' device."""
     import torch
 
     class DiffusionMisfit(torch.autograd.Function):
         @staticmethod
         def forward(ctx, m, H0, Ht, solver):
-            def host(t):
-                return np.asfortranarray(t.detach().cpu().numpy().transpose(2, 1, 0))
-
-            loss = solver.forward(host(H0), host(m), host(Ht))
+            args = [t.detach().to(torch.float64).contiguous() for t in (H0, m, Ht)]
+            loss = solver.forward(*args)
             ctx.solver = solver
-            ctx.dev = m.device
+            ctx.like = args[1]
             return torch.tensor(loss, dtype=torch.float64, device=m.device)
 
         @staticmethod
         def backward(ctx, gout):
-            gm, gh = ctx.solver.gradient()
-            t = lambda a: torch.from_numpy(np.ascontiguousarray(a.transpose(2, 1, 0))).to(ctx.dev)
-            return gout * t(gm), gout * t(gh), None, None
+            gm, gh = torch.empty_like(ctx.like), torch.empty_like(ctx.like)
+            ctx.solver.gradient(out_m=gm, out_H0=gh)
+            return gout * gm, gout * gh, None, None
 
     return DiffusionMisfit

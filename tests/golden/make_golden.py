@@ -1,9 +1,9 @@
 """Generate the golden fixtures used by the parity tests.
 
-Run once in a checkout that has the reference repository available (the
-default path below, or pass it as the first argument):
+Run once in a checkout that has the reference repository available, with
+the path of the reference checkout as the argument:
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT
 
 It writes three small JSON files next to this script:
 
@@ -144,4 +144,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

@@ -12,7 +12,7 @@ at reduced sizes that the oracle solves in seconds.
 Bar: the FP64-accuracy forms (FP64, DFH, DF64 in 3D) take the oracle's PT
 iteration count in every physical step and return H within 1e-10 relative
 L2; the rebased FP32 form (FP32_RB) likewise within 1e-10, its per-step
-counts within 1 % (plus one check block) of the oracle's; FP32_DC within
+counts within 1 % plus two check blocks of the oracle's; FP32_DC within
 1e-8 of the oracle's H.
 """
 import functools
@@ -69,8 +69,12 @@ def test_benchmark_problem_matches_oracle(name, shape, prec):
     H, it = gpu_solution(name, shape, prec)
     s = S.CONFIGS[name]
     if prec == "fp32_rb":
+        # the rebased form stops at a check block where both its FP32 check
+        # residual and the FP64 residual of its rebased state are <= tol: within
+        # two check blocks of the reference's count (on the 1D problem, whose
+        # steps take ~40 blocks of nchk = 10, that is up to 5 %)
         for a, b in zip(it, it_r):
-            assert abs(a - b) <= 0.01 * b + s.nout, (it, it_r)
+            assert abs(a - b) <= 0.01 * b + 2 * s.nout, (it, it_r)
     else:
         assert it == list(it_r), (it, it_r)
     assert rel_l2(H, Hr) <= RTOL_FP64

@@ -1,4 +1,5 @@
-"""The Julia binding (julia/PTDiffusion.jl) against the C ABI it calls.
+"""The Julia binding (the julia/ package: src/PTDiffusion.jl and its ChainRulesCore
+extension) against the C ABI it calls.
 
 There is no Julia toolchain here, so the binding is checked as text: its
 `PtdParams` mirror must list the members of `ptd_params` (include/ptd.h) in
@@ -11,7 +12,9 @@ import os
 import re
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-JL = os.path.join(ROOT, "pseudotransientdiffusion.jl_gb300", "julia", "PTDiffusion.jl")
+JLPKG = os.path.join(ROOT, "pseudotransientdiffusion.jl_gb300", "julia")
+JL = os.path.join(JLPKG, "src", "PTDiffusion.jl")
+JLEXT = os.path.join(JLPKG, "ext", "PTDiffusionChainRulesCoreExt.jl")
 HEADER = os.path.join(ROOT, "include", "ptd.h")
 
 C_SCALAR = {"int32_t": "Int32", "int": "Int32", "double": "Float64", "float": "Float32", "int64_t": "Int64"}
@@ -166,3 +169,19 @@ def test_enum_tables_match_the_header():
     for k, v in precs.items():
         assert enum["PTD_PREC_" + k.upper()] == v, k
     assert int(re.search(r"const PTD_OK = Cint\((\d+)\)", jl).group(1)) == enum["PTD_OK"]
+
+
+def test_rrule_is_a_package_extension():
+    """The rrule lives in a package extension declared in Project.toml, so it
+    does not depend on the order in which ChainRulesCore and PTDiffusion load."""
+    with open(os.path.join(JLPKG, "Project.toml")) as fh:
+        proj = fh.read()
+    assert re.search(r'^name = "PTDiffusion"$', proj, re.M)
+    assert re.search(r'^\[weakdeps\]\nChainRulesCore = "d360d2e6-b24c-11e9-a2a3-2a2ae2dbcce4"$', proj, re.M)
+    assert re.search(r'^\[extensions\]\nPTDiffusionChainRulesCoreExt = "ChainRulesCore"$', proj, re.M)
+    with open(JLEXT) as fh:
+        ext = fh.read()
+    assert "module PTDiffusionChainRulesCoreExt" in ext
+    assert "function ChainRulesCore.rrule(::typeof(misfit), a::AdjointSolver, m, H0, Ht)" in ext
+    assert "isdefined(Main" not in _julia()
+    assert "forward!" in _julia() and "gradient!" in _julia()
