@@ -268,6 +268,8 @@ struct ptd_ctx : ptd_ctx_base {
     double* W[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     double* D = nullptr;
     DevState* st = nullptr;
+    double* parts = nullptr;      // check-residual partials, one slot per block / warp (fixed-order sum)
+    long long parts_cap = 0;
     int* zero_flag = nullptr;
     double* errhist = nullptr;
     int errcap = 0;
@@ -303,6 +305,28 @@ static void args_for(const ptd_ctx* c, int parity, const int* done, PTArgs& a)
     a.D = c->D;
     a.done = done;
     a.acc = &c->st->acc;
+    a.parts = c->parts;
+}
+
+// The slot array of the check partials, large enough for the launch shape in use.
+static int ensure_parts(ptd_ctx* c)
+{
+    const long long n = pt_check_slots(c->p.ndim, c->nx, c->ny, c->nz, c->cfg, c->p.resid_mode == PTD_RESID_CONSISTENT);
+    if (n <= c->parts_cap) return PTD_OK;
+    if (c->parts) {
+        CK(cudaStreamSynchronize(c->stream));
+        cudaFree(c->parts);
+        c->parts = nullptr;
+        c->parts_cap = 0;
+    }
+    const cudaError_t e = cudaMalloc((void**)&c->parts, (size_t)n * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? PTD_ENOMEM : PTD_ECUDA, "cudaMalloc(check partials): %s",
+                    cudaGetErrorString(e));
+    }
+    c->parts_cap = n;
+    return PTD_OK;
 }
 
 // The PT iteration of one physical step as one CUDA graph: a WHILE node whose
@@ -337,6 +361,8 @@ static int capture_step(ptd_ctx* c, int parity, cudaGraphExec_t* out)
     }
     const int nchk = c->p.nchk;
     const int nblk = (nchk & 1) ? 2 : 1;
+    const long long nparts =
+        pt_check_slots(c->p.ndim, c->nx, c->ny, c->nz, c->cfg, c->p.resid_mode == PTD_RESID_CONSISTENT);
     int par = parity;
     int nk = 0;
     for (int b = 0; b < nblk && err == cudaSuccess; ++b) {
@@ -355,8 +381,8 @@ static int capture_step(ptd_ctx* c, int parity, cudaGraphExec_t* out)
             par ^= 1;
         }
         if (err == cudaSuccess)
-            err = launch_judge_cond(c->st, c->errhist, c->errcap, nchk, c->p.itmax, c->p.tol, c->dv.norm_den,
-                                    c->p.norm == PTD_NORM_MAX, loop, c->stream);
+            err = launch_judge_parts(c->st, c->parts, nparts, c->errhist, c->errcap, nchk, c->p.itmax, c->p.tol,
+                                     c->dv.norm_den, c->p.norm == PTD_NORM_MAX, loop, c->stream);
         nk += 1;
     }
     cudaError_t e2 = cudaStreamEndCapture(c->stream, &body);
@@ -487,6 +513,7 @@ static void free_ctx(ptd_ctx* c)
         for (int q = 0; q < 2; ++q) cudaFree(c->W[d][q]);
     cudaFree(c->D);
     cudaFree(c->st);
+    cudaFree(c->parts);
     cudaFree(c->zero_flag);
     cudaFree(c->errhist);
     cudaFree(c->stage);
@@ -570,6 +597,7 @@ extern "C" int ptd_create(ptd_ctx** out, const ptd_params* p)
         }
     } else {
         if ((p->flags & PTD_FLAG_AUTOTUNE) && p->ndim > 1) rc = autotune(c);
+        if (!rc) rc = ensure_parts(c);
         for (int q = 0; q < 2 && !rc; ++q) {
             if (p->nchk <= p->itmax) rc = capture_step(c, q, &c->gstep[q]);
             if (!rc) rc = capture_plain(c, q, &c->gplain[q]);
@@ -618,6 +646,7 @@ extern "C" int ptd_set_launch_config(ptd_ctx* c, const int32_t cfg[4])
     } else if (c->rb) {
         rc = rb_set_config(c->rb, k);
     } else {
+        rc = ensure_parts(c);
         for (int q = 0; q < 2 && !rc; ++q) {
             if (c->gstep[q]) cudaGraphExecDestroy(c->gstep[q]);
             if (c->gplain[q]) cudaGraphExecDestroy(c->gplain[q]);

@@ -62,6 +62,10 @@ struct PTArgs {
     const void* D;      // LINSTEP cell diffusivity
     const int* done;    // nonzero: the step has stopped, skip the iteration
     double* acc;        // residual accumulator: sum R^2 (RMS) or max |R| bits (MAX)
+    // Per-block (1D, 3D) / per-warp (2D) partials of the check residual, one
+    // slot each, that the judge sums in a fixed order: the same residual norm
+    // on every run.  NULL: the partials go into acc by atomics instead.
+    double* parts;
     int norm_max;
     // equal sigma_d in every dimension (square cells): the update is formed
     // as (H - Hold) rdt/sigma + sum_d (w_R - w_L) with e*sigma, one
@@ -192,9 +196,12 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 }
 
 // Block-wide residual reduction into acc (sum of squares, or max |R| as the
-// ordered bit pattern of a non-negative double; NaN orders above +inf).
+// ordered bit pattern of a non-negative double; NaN orders above +inf), or,
+// with parts, into the block's own slot parts[slot] (same encoding).  The
+// reduction inside the block has a fixed order either way.
 __device__ __forceinline__ void block_reduce_residual(double* acc, int norm_max, double part_sum,
-                                                      unsigned long long part_max)
+                                                      unsigned long long part_max, double* parts = nullptr,
+                                                      long long slot = 0)
 {
     __shared__ double s_sum[32];
     __shared__ unsigned long long s_max[32];
@@ -214,19 +221,21 @@ __device__ __forceinline__ void block_reduce_residual(double* acc, int norm_max,
         if (norm_max) {
             unsigned long long v = ln < nw ? s_max[ln] : 0ull;
             v = warp_max_u64(v);
-            if (ln == 0 && v) atomicMax(reinterpret_cast<unsigned long long*>(acc), v);
+            if (ln == 0 && parts) parts[slot] = __longlong_as_double((long long)v);
+            else if (ln == 0 && v) atomicMax(reinterpret_cast<unsigned long long*>(acc), v);
         } else {
             double v = ln < nw ? s_sum[ln] : 0.0;
             v = warp_sum(v);
-            if (ln == 0) atomicAdd(acc, v);
+            if (ln == 0 && parts) parts[slot] = v;
+            else if (ln == 0) atomicAdd(acc, v);
         }
     }
 }
 
 __device__ __forceinline__ void block_reduce_residual(const PTArgs& a, double part_sum,
-                                                      unsigned long long part_max)
+                                                      unsigned long long part_max, long long slot)
 {
-    block_reduce_residual(a.acc, a.norm_max, part_sum, part_max);
+    block_reduce_residual(a.acc, a.norm_max, part_sum, part_max, a.parts, slot);
 }
 
 __device__ __forceinline__ void accumulate_residual(double r, double& sum, unsigned long long& mx)
@@ -285,15 +294,19 @@ __device__ __forceinline__ void warp_flush_residual32(double* acc, int norm_max,
 // residual carries the FP64 base residual): same encoding, one atomic per
 // warp, called from inside the last step of the y march with all 32 lanes
 // converged (after the march, the check variants held 61-97 registers).
+// With parts, the warp's result goes into its own slot parts[slot] instead.
 __device__ __forceinline__ void warp_flush_residual(double* acc, int norm_max, double part_sum,
-                                                    unsigned long long part_max, int lane)
+                                                    unsigned long long part_max, int lane, double* parts = nullptr,
+                                                    long long slot = 0)
 {
     if (norm_max) {
         part_max = warp_max_u64(part_max);
-        if (lane == 0 && part_max) atomicMax(reinterpret_cast<unsigned long long*>(acc), part_max);
+        if (lane == 0 && parts) parts[slot] = __longlong_as_double((long long)part_max);
+        else if (lane == 0 && part_max) atomicMax(reinterpret_cast<unsigned long long*>(acc), part_max);
     } else {
         part_sum = warp_sum(part_sum);
-        if (lane == 0) atomicAdd(acc, part_sum);
+        if (lane == 0 && parts) parts[slot] = part_sum;
+        else if (lane == 0) atomicAdd(acc, part_sum);
     }
 }
 

@@ -48,8 +48,10 @@ cudaError_t launch_expm(const double* m, void* E, long long n, bool df64, cudaSt
 cudaError_t launch_from_df64(const void* src, double* dst, long long n, cudaStream_t s);
 cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
                          double norm_den, int norm_max, cudaStream_t s);
-cudaError_t launch_judge_cond(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
-                              double norm_den, int norm_max, cudaGraphConditionalHandle loop, cudaStream_t s);
+cudaError_t launch_judge_parts(DevState* st, const double* parts, long long nparts, double* errhist, int errcap,
+                               int nchk, int itmax, double tol, double norm_den, int norm_max,
+                               cudaGraphConditionalHandle loop, cudaStream_t s);
+long long pt_check_slots(int ndim, int nx, int ny, int nz, const LaunchCfg& cfg, bool consistent);
 cudaError_t launch_reset_state(DevState* st, cudaStream_t s);
 cudaError_t preload_pt2d_f64();
 

@@ -36,27 +36,35 @@ __global__ void __launch_bounds__(256) pt1d_kernel(PTArgs a)
     double part = 0.0;
     unsigned long long pmax = 0ull;
     pt1d_body<N, MODEL, CHECK>(a, blockIdx.x, part, pmax);
-    if (CHECK) block_reduce_residual(a, part, pmax);
+    if (CHECK) block_reduce_residual(a, part, pmax, blockIdx.x);
 }
 
 template <class N, int MODEL, bool CHECK>
-__global__ void __launch_bounds__(256) pt2d_kernel(PTArgs a, int chunk)
+__global__ void __launch_bounds__(256, CHECK ? 5 : 6) pt2d_kernel(PTArgs a, int chunk)
 {
     if (step_done(a.done)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    // the body flushes its check partials into a.acc (last step of its march)
-    pt2d_body<N, MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+    // the body flushes its check partials (last step of its march) into the
+    // warp's slot, warps numbered x fastest
+    const long long slot = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.y + threadIdx.y;
+    pt2d_body<N, MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax, slot);
 }
 
+// Resident CTAs per SM the register allocation must allow: 48 warps (3 CTAs
+// of 16 warps) for the plain iterations of the LIN and NONLIN models, which
+// fit in 40 registers (DFH NONLIN with a 24-byte spill), 32 warps for the
+// check iterations and the models with a per-cell field (more live values).
 template <class N, int MODEL, bool CHECK, int R>
-__global__ void __launch_bounds__(32 * R) pt3d_kernel(PTArgs a, int chunk)
+__global__ void __launch_bounds__(32 * R, (CHECK || MODEL == LINSTEP || MODEL == NONLIN_EXPM) ? 32 / R : 48 / R)
+    pt3d_kernel(PTArgs a, int chunk)
 {
     if (step_done(a.done)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
     pt3d_body<N, MODEL, CHECK, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a, part, pmax);
+    if (CHECK)
+        block_reduce_residual(a, part, pmax, ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -109,7 +117,7 @@ __global__ void __launch_bounds__(256) resid_consistent_kernel(PTArgs a, int ndi
         const T r = N::sub(div, N::mul(N::hdo(H, N::ldo(a.Hold, c)), cst<N>(a, 3)));
         accumulate_residual(N::to_d(r), part, pmax);
     }
-    block_reduce_residual(a, part, pmax);
+    block_reduce_residual(a, part, pmax, blockIdx.x);
 }
 
 // The check of one block: err from the accumulated residual, appended to the
@@ -140,16 +148,49 @@ __global__ void judge_kernel(DevState* st, double* errhist, int errcap, int nchk
     judge_step(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max);
 }
 
-// The judge at the end of the body of a WHILE graph node: when the step stops
-// it also ends the loop (the node's condition is set to 0), so the graph runs
-// exactly the check blocks of the step, with no host round trip.
-__global__ void judge_cond_kernel(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
-                                  double norm_den, int norm_max, cudaGraphConditionalHandle loop)
+// The judge of the one-grid solver, at the end of the body of the WHILE
+// graph node of a physical step: it sums (or maxes) the check partials of the
+// block's PT kernels from their slots in a fixed order -- thread t takes the
+// slots t, t + 256, ... in order, then a fixed tree over the threads -- so the
+// residual norm, and with it the stopping iteration, is the same on every run;
+// when the step stops it also ends the loop (the node's condition set to 0),
+// so the graph runs exactly the check blocks of the step.
+__global__ void __launch_bounds__(256) judge_parts_kernel(DevState* st, const double* parts, long long nparts,
+                                                          double* errhist, int errcap, int nchk, int itmax, double tol,
+                                                          double norm_den, int norm_max, cudaGraphConditionalHandle loop)
 {
+    __shared__ double s_sum[256];
+    __shared__ unsigned long long s_max[256];
+    const int t = threadIdx.x;
     // a step already stopped (a second block in the body after the stop)
-    // leaves the loop too
-    if (st->done || judge_step(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max) != DONE_RUNNING)
-        cudaGraphSetConditional(loop, 0);
+    // leaves the loop too; every thread reads done before thread 0 writes it
+    if (st->done) {
+        if (t == 0) cudaGraphSetConditional(loop, 0);
+        return;
+    }
+    double sum = 0.0;
+    unsigned long long mx = 0ull;
+    for (long long i = t; i < nparts; i += 256) {
+        const double v = parts[i];
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        mx = bits > mx ? bits : mx;
+        sum += v;
+    }
+    s_sum[t] = sum;
+    s_max[t] = mx;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) {
+            s_sum[t] += s_sum[t + o];
+            s_max[t] = s_max[t + o] > s_max[t] ? s_max[t + o] : s_max[t];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        st->acc = norm_max ? __longlong_as_double((long long)s_max[0]) : s_sum[0];
+        if (judge_step(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max) != DONE_RUNNING)
+            cudaGraphSetConditional(loop, 0);
+    }
 }
 
 __global__ void reset_state_kernel(DevState* st)
@@ -289,11 +330,31 @@ cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, in
     return cudaGetLastError();
 }
 
-cudaError_t launch_judge_cond(DevState* st, double* errhist, int errcap, int nchk, int itmax, double tol,
-                              double norm_den, int norm_max, cudaGraphConditionalHandle loop, cudaStream_t s)
+cudaError_t launch_judge_parts(DevState* st, const double* parts, long long nparts, double* errhist, int errcap,
+                               int nchk, int itmax, double tol, double norm_den, int norm_max,
+                               cudaGraphConditionalHandle loop, cudaStream_t s)
 {
-    judge_cond_kernel<<<1, 1, 0, s>>>(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max, loop);
+    judge_parts_kernel<<<1, 256, 0, s>>>(st, parts, nparts, errhist, errcap, nchk, itmax, tol, norm_den, norm_max,
+                                         loop);
     return cudaGetLastError();
+}
+
+// The number of check-residual slots the fused kernel of a check iteration
+// writes with this launch shape (the grids of launch_model below: blocks in
+// 1D and 3D, warps in 2D), or the consistent-residual kernel's blocks.
+long long pt_check_slots(int ndim, int nx, int ny, int nz, const LaunchCfg& cfg, bool consistent)
+{
+    if (consistent) return fill_blocks();
+    if (ndim == 1) return (nx + 255) / 256;
+    if (ndim == 2) {
+        const int W = cfg.warps2d;
+        const long long tiles = (nx - 2 + 30) / 31;
+        return ((tiles + W - 1) / W) * W * (long long)((ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);
+    }
+    const long long tx = (nx - 2 + 30) / 31;
+    const long long nzc = (nz - 2 + cfg.chunk3d - 1) / cfg.chunk3d;
+    const long long ty = cfg.rows3d == 8 ? (ny - 2 + 6) / 7 : (ny - 2 + 14) / 15;
+    return tx * ty * nzc;
 }
 
 cudaError_t launch_reset_state(DevState* st, cudaStream_t s)

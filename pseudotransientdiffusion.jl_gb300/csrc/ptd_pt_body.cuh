@@ -216,9 +216,10 @@ __device__ __forceinline__ void pt1d_body(const PTArgs& a, int bx, double& part,
 // 2D: blockDim = (32, W); warp w of block b owns the x strip of tile
 // t = b*W + w: cells i = 31t + lane (lane 0 = left neighbour), and marches
 // rows j0 .. j1-1 of y chunk cy.
+// slot: the warp's slot in a.parts (when a.parts is set).
 template <class N, int MODEL, bool CHECK>
 __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int chunk, double& part,
-                                          unsigned long long& pmax)
+                                          unsigned long long& pmax, long long slot = 0)
 {
     using T = typename N::T;
     using HV = typename N::HV;
@@ -337,8 +338,10 @@ __device__ __forceinline__ void pt2d_body(const PTArgs& a, int tile, int cy, int
                 Dc = Dn;
                 dcf = dnf;
             }
-            if (CHECK && j == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane);
+            if (CHECK && j == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
         }
+    } else if (CHECK && a.parts && lane == 0) {
+        a.parts[slot] = 0.0;   // a warp with no cells: its slot still holds this check's (empty) part
     }
 }
 

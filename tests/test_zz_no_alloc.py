@@ -93,6 +93,7 @@ def test_noalloc_rejects_host_memory():
                                      None, None)
     assert st == _abi.PTD_EINVAL and "D must be device memory" in _abi.last_error()
     Hh = np.ones(64 * 64)
+    p = ptdiff.make_params(S.SCRIPTS["diff_2D_nonlin"], shape)
     st = _lib().ptd_solve_2d_noalloc(C.byref(p), Hh.ctypes.data_as(C.c_void_p), None, None, None)
     assert st == _abi.PTD_EINVAL and "H must be device memory" in _abi.last_error()
 
