@@ -362,10 +362,15 @@ class GridBench:
         if precision == "fp32_rb":
             # one FP32 iteration reads delta, H_b (FP32), the fluxes omega_d, the
             # base flux defects t_b,d and R_b, writes delta and omega_d: (2+3nd+2)*4 B
-            # per cell; in 2D a launch runs two iterations (temporal blocking, even nchk)
-            ipl = 2 if nd == 2 and self.s.nout % 2 == 0 else 1
+            # per cell; a launch runs two iterations (temporal blocking) with an even
+            # check cadence in 2D, and in 3D for the LIN and NONLIN models
+            tb_ok = nd == 2 or (nd == 3 and self.s.model in (0, 2))
+            ipl = 2 if tb_ok and self.s.nout % 2 == 0 else 1
             nbytes = (2 + 3 * nd + 2) * 4 * self.cells
-            name = f"rb{nd}d{'_tb2' if ipl == 2 else ''}_kernel ({ipl} FP32 iteration{'s' if ipl > 1 else ''} per launch)"
+            kname = {1: "rb1d_kernel", 2: "rb2d_kernel", 3: "rb3d_kernel"}[nd]
+            if ipl == 2:
+                kname = "rb2d_tb2_pair_kernel" if nd == 2 and self.s.model in (0, 2) else f"rb{nd}d_tb2_kernel"
+            name = f"{kname} ({ipl} FP32 iteration{'s' if ipl > 1 else ''} per launch)"
         else:
             ipl, nbytes = 1, self.A
             name = f"pt{nd}d_kernel<{precision.upper()}> (fused PT iteration)"
@@ -512,11 +517,10 @@ def run_c1(pg):
             "rel_l2_vs_oracle": rel_l2(H, Hr)}
 
 
-def run_batch_record(args, world, rank, pg, K=3, W=1):
-    """The batched 2D step-diffusion workload: 256 instances, sides log-uniform
-    in [128, 1024] (seeded), FP32 + FP64 defect correction, tol 1e-8; the
-    instances are sharded over the ranks by cell count (no collective on the
-    data path).  Metric: instances solved per second (one physical step)."""
+def _batch_run(prec, world, rank, pg, K, W):
+    """K timed batch solves (one physical step each) of the 256-instance batch
+    in one precision; the instances are sharded over the ranks by cell count
+    (no collective on the data path)."""
     import torch
 
     import ptdiff
@@ -526,7 +530,6 @@ def run_batch_record(args, world, rank, pg, K=3, W=1):
     sizes, Hs, Ds = ptdiff.batch_instances(n, seed=0)
     mine = PD.shard_by_cells([int(s) ** 2 for s in sizes], world)[rank]
     sz = [int(sizes[i]) for i in mine]
-    prec = args.precision if args.precision in ("fp64", "df64", "fp32_dc") and args.workload != "suite" else "fp32_dc"
     p = ptdiff.batch_params(len(mine), model=1, precision=prec, nt=1)
     b = ptdiff.BatchSolver(p, sz, sz)
     w, c, us = b.tune()
@@ -539,6 +542,7 @@ def run_batch_record(args, world, rank, pg, K=3, W=1):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     err = [0.0]
+    iters = None
     for _ in range(K):
         iters, err = b.solve([Hs[i].copy(order="F") for i in mine], [Ds[i] for i in mine])
     torch.cuda.synchronize()
@@ -548,16 +552,36 @@ def run_batch_record(args, world, rank, pg, K=3, W=1):
     b.close()
     t_max = reduce_max(pg, dt)
     total = reduce_sum(pg, len(mine) * K)
-    return {"metric": "batch instances per second (one implicit step to tol)",
-            "value": round(total / t_max, 3), "unit": "instances/s", "steps": K, "warmup": W,
-            "ms_per_step": round(t_max / K * 1e3, 3), "dtype": DTYPES[prec],
-            "config": {"workload": "batch_linstep_256", "instances": n, "sides": "log-uniform 128..1024, seed 0",
-                       "tol": 1e-8, "precision": prec,
-                       "tuned": {"warps": w, "chunk": c, "inner_iterations_per_launch": depth,
-                                 "us_per_iter": round(float(us), 2)}},
-            "e2e_note": "H0 and D of every instance copied from host memory and H back inside every timed step",
-            "gpu_launches": int(l1 - l0), "inner_iterations": int(i1 - i0), "max_err_last": float(max(err)),
-            "clocks": clk}
+    return {"value": round(total / t_max, 3), "ms_per_step": round(t_max / K * 1e3, 3), "steps": K, "warmup": W,
+            "tuned": {"warps": w, "chunk": c, "iterations_per_launch": depth, "us_per_iter": round(float(us), 2)},
+            "gpu_launches": int(l1 - l0), "iterations": int(i1 - i0),
+            "max_iterations_of_an_instance": int(np.max(iters)) if iters is not None else 0,
+            "max_err_last": float(max(err)), "clocks": clk}
+
+
+def run_batch_record(args, world, rank, pg, K=3, W=1):
+    """The batched 2D step-diffusion workload: 256 instances, sides log-uniform
+    in [128, 1024] (seeded), step-function D, tol 1e-8, one implicit step per
+    solve.  Metric: instances solved per second.  The suite runs the rebased
+    FP32 form (FP32_RB) and, for comparison, the FP32 + FP64 defect correction
+    (FP32_DC)."""
+    suite = args.workload == "suite"
+    prec = args.precision if args.precision in ("fp64", "df64", "fp32_dc", "fp32_rb") and not suite else "fp32_rb"
+    r = _batch_run(prec, world, rank, pg, K, W)
+    rec = {"metric": "batch instances per second (one implicit step to tol)",
+           "value": r["value"], "unit": "instances/s", "steps": K, "warmup": W,
+           "ms_per_step": r["ms_per_step"], "dtype": DTYPES[prec],
+           "config": {"workload": "batch_linstep_256", "instances": 256, "sides": "log-uniform 128..1024, seed 0",
+                      "tol": 1e-8, "precision": prec, "tuned": r["tuned"]},
+           "e2e_note": "H0 and D of every instance copied from host memory and H back inside every timed step",
+           "gpu_launches": r["gpu_launches"], "iterations": r["iterations"],
+           "max_iterations_of_an_instance": r["max_iterations_of_an_instance"], "max_err_last": r["max_err_last"],
+           "clocks": r["clocks"]}
+    if suite and prec != "fp32_dc":
+        d = _batch_run("fp32_dc", world, rank, pg, 2, 1)
+        d["speedup_of_" + prec] = round(r["value"] / d["value"], 3) if d["value"] else None
+        rec["fp32_dc"] = d
+    return rec
 
 
 def run_adjoint_record(args, world, rank, pg, K=2, W=1):

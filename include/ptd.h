@@ -90,7 +90,7 @@ enum { PTD_MODEL_LIN = 0, PTD_MODEL_LINSTEP = 1, PTD_MODEL_NONLIN = 2, PTD_MODEL
  *           reference's check residual (every nchk, formed in FP32 from the
  *           FP64 base residual) and the FP64 residual of the rebased state
  *           are both <= tol; H is the FP64 base.  Every model, mixed
- *           residual; single grids only. */
+ *           residual; single grids and the batch (ptd_batch_*). */
 enum { PTD_PREC_FP64 = 0, PTD_PREC_FP32_DC = 1, PTD_PREC_DF64 = 2, PTD_PREC_DFH = 3, PTD_PREC_FP32_RB = 4 };
 
 /* Residual used for the stopping test.  MIXED is the reference's: the
@@ -195,7 +195,10 @@ PTD_API void ptd_destroy(ptd_ctx* ctx);
  * H0 (and D for the step model), advanced together by one kernel launch per
  * PT iteration with per-instance convergence flags.  No reference
  * counterpart (the reference solves one grid per run); the per-instance
- * algorithm is that of ptd_solve (FP64, DF64) or its FP32_DC form.
+ * algorithm is that of ptd_solve (FP64, DF64) or its FP32_DC or FP32_RB form.
+ * FP32_RB: one physical step of the whole batch is one CUDA graph launch
+ * (phases of every instance until all have stopped); an instance that
+ * reaches itmax stops at its last full check block.
  * Constraint: itmax is a multiple of nchk. */
 typedef struct ptd_batch_params {
     int32_t ninst;       /* number of instances */
@@ -219,16 +222,17 @@ PTD_API int ptd_batch_create(ptd_batch** b, const ptd_batch_params* p, const int
 /* H[i] in: H0 of instance i, out: H after nt steps (nx[i]*ny[i], x fastest; host
  * or device).  D[i]: step-model diffusivity or NULL.  iters: ninst*nt PT
  * iterations (FP32_DC: inner FP32 iterations), instance-major.  err_last
- * (nullable, ninst): last residual norm of each instance.  n_done: ninst. */
+ * (nullable, ninst): last residual norm of each instance (FP32_RB: the FP64
+ * residual of its returned H).  n_done: ninst. */
 PTD_API int ptd_batch_solve(ptd_batch* b, double* const* H, const double* const* D, int32_t* iters,
                             double* err_last, int32_t* n_done);
 /* Autotuner: times every (warps per CTA, rows per y chunk) launch shape of the
- * batched kernel on the batch's own instances -- for FP32_DC also one or two
- * (temporally blocked) inner iterations per launch -- and keeps the fastest
- * per iteration. */
+ * batched kernel on the batch's own instances -- for FP32_DC and FP32_RB also
+ * one or two (temporally blocked) FP32 iterations per launch -- and keeps the
+ * fastest per iteration. */
 PTD_API int ptd_batch_tune(ptd_batch* b, int32_t* warps, int32_t* chunk, float* us_per_iteration);
-/* The launch shape in use: warps per CTA, rows per y chunk, inner iterations
- * per launch (2 = temporally blocked FP32_DC kernel). */
+/* The launch shape in use: warps per CTA, rows per y chunk, FP32 iterations
+ * per launch (2 = the temporally blocked FP32_DC or FP32_RB kernel). */
 PTD_API int ptd_batch_config(ptd_batch* b, int32_t* warps, int32_t* chunk, int32_t* iters_per_launch);
 PTD_API int ptd_batch_counters(ptd_batch* b, int64_t* kernel_launches, int64_t* pt_iterations);
 PTD_API void ptd_batch_destroy(ptd_batch* b);

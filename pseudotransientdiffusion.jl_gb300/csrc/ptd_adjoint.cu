@@ -906,7 +906,11 @@ extern "C" int ptd_adj_create(ptd_adj** out, const ptd_params* p)
     A->expm = p->model == PTD_MODEL_NONLIN_EXPM;
     A->blocks_per_phase = std::max(1, (200 + A->nchk - 1) / A->nchk);
     derive(A->p, A->dv);
-    A->cfg = tuned_config(A->p);
+    {   // the adjoint kernels tile like the one-cell-per-lane FP64 kernels
+        ptd_params pt = A->p;
+        pt.precision = PTD_PREC_FP64;
+        A->cfg = tuned_config(pt);
+    }
     {   // stagnation window: ~2 n_max iterations, the PT iteration's own time scale
         const int nmax = std::max(p->nx, std::max(p->ny, p->nz));
         A->stall = std::max(10, (2 * nmax + A->nchk - 1) / A->nchk);

@@ -311,7 +311,7 @@ static void args_for(const ptd_ctx* c, int parity, const int* done, PTArgs& a)
 // The slot array of the check partials, large enough for the launch shape in use.
 static int ensure_parts(ptd_ctx* c)
 {
-    const long long n = pt_check_slots(c->p.ndim, c->nx, c->ny, c->nz, c->cfg, c->p.resid_mode == PTD_RESID_CONSISTENT);
+    const long long n = pt_check_slots(c->p.ndim, c->nx, c->ny, c->nz, c->cfg, c->p.resid_mode == PTD_RESID_CONSISTENT, c->num);
     if (n <= c->parts_cap) return PTD_OK;
     if (c->parts) {
         CK(cudaStreamSynchronize(c->stream));
@@ -362,7 +362,7 @@ static int capture_step(ptd_ctx* c, int parity, cudaGraphExec_t* out)
     const int nchk = c->p.nchk;
     const int nblk = (nchk & 1) ? 2 : 1;
     const long long nparts =
-        pt_check_slots(c->p.ndim, c->nx, c->ny, c->nz, c->cfg, c->p.resid_mode == PTD_RESID_CONSISTENT);
+        pt_check_slots(c->p.ndim, c->nx, c->ny, c->nz, c->cfg, c->p.resid_mode == PTD_RESID_CONSISTENT, c->num);
     int par = parity;
     int nk = 0;
     for (int b = 0; b < nblk && err == cudaSuccess; ++b) {

@@ -20,6 +20,16 @@
 // the device (forcing term, FP32-floor-aware inner target, backtracking), so
 // instances that need different numbers of outer corrections also proceed
 // independently; the host only replays graphs until all have finished.
+//
+// FP32_RB: the rebased FP32 form of ptd_rb.cu (ptd_rb_body.cuh) per instance.
+// A physical step of the whole batch is one CUDA graph launch: a WHILE node
+// whose body is one phase of every instance -- check blocks of two-iteration
+// launches over all instances, each followed by the per-instance FP32 judge,
+// then the FP64 rebase of every running instance (fold, base quantities,
+// per-instance FP64 judge) -- and which the FP64 judge ends once every
+// instance has stopped.  An instance whose phase or step is over skips the
+// iteration launches (its CTAs return at entry) and waits for the next
+// rebase; no host round trip per check or per phase.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -29,6 +39,7 @@
 #include "ptd_dc_body.cuh"
 #include "ptd_internal.h"
 #include "ptd_pt_body.cuh"
+#include "ptd_rb_body.cuh"
 
 namespace ptd {
 
@@ -340,6 +351,86 @@ __global__ void tofloat_batch_kernel(const double* src, float* dst, long long n)
 }
 
 // ---------------------------------------------------------------------------
+// FP32_RB: one (TB = 1) or two (TB = 2) rebased FP32 iterations over every
+// instance whose phase is running.
+template <int MODEL, bool CHECK, int TB>
+__global__ void __launch_bounds__(256) rb2d_batch_kernel(const RbArgs* __restrict__ tab,
+                                                         const int4* __restrict__ work, int chunk)
+{
+    const int4 w = work[blockIdx.x];
+    const RbArgs a = tab[w.x];
+    if (rb_skip(a.skip)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    // the bodies flush their check partials into a.acc (last step of their march)
+    if (TB == 2) rb2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    else rb2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+}
+
+__global__ void rb_reset_batch_kernel(RbDev* st, int ninst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ninst) rb_reset(&st[i]);
+}
+
+__global__ void rb_check_judge_batch_kernel(RbDev* st, int ninst, int nchk, int itmax, double tol,
+                                            const double* norm_den, int norm_max)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ninst) rb_check_judge(&st[i], nullptr, 0, nchk, itmax, tol, norm_den[i], norm_max);
+}
+
+// The FP64 judge of every instance (one block); in the step graph's WHILE
+// node (in_loop) it ends the loop once no instance is running.  Every pass of
+// the body adds at least one check block to each running instance, and an
+// instance with no room for another block before itmax stops (capped), so the
+// loop ends within itmax/nchk passes.
+__global__ void __launch_bounds__(256) rb_base_judge_batch_kernel(RbDev* st, int ninst, double tol,
+                                                                  const double* norm_den, int norm_max,
+                                                                  cudaGraphConditionalHandle loop, int in_loop,
+                                                                  int* passes)
+{
+    int running = 0;
+    for (int i = threadIdx.x; i < ninst; i += blockDim.x)
+        if (!rb_base_judge(&st[i], tol, norm_den[i], norm_max)) running = 1;
+    const int any = __syncthreads_or(running);
+    if (in_loop && threadIdx.x == 0) {
+        *passes += 1;
+        if (!any) cudaGraphSetConditional(loop, 0);
+    }
+}
+
+// Fold the changes of every running instance into its base (one chunk of an
+// instance's padded fields per CTA, fwork: {instance, first element, count}).
+__global__ void __launch_bounds__(256) rb_fold_batch_kernel(const RbFoldArgs* __restrict__ ftab, const RbDev* st,
+                                                            const int4* __restrict__ fwork, int tb)
+{
+    const int4 w = fwork[blockIdx.x];
+    if (st[w.x].step_done) return;
+    const int parity = (st[w.x].phase_iter / tb) & 1;   // one buffer swap per launch of tb iterations
+    const RbFoldArgs f = ftab[w.x];
+    for (int k = threadIdx.x; k < w.z; k += blockDim.x) rb_fold_elem(f, parity, (long long)w.y + k);
+}
+
+// Base quantities of every running instance (of all instances at a step
+// start: use_st = 0), one chunk of an instance's padded field per CTA.
+__global__ void __launch_bounds__(256) rb_base_batch_kernel(const RbBaseArgs* __restrict__ btab, const RbDev* st,
+                                                            const int4* __restrict__ fwork, int use_st)
+{
+    const int4 w = fwork[blockIdx.x];
+    if (use_st && st[w.x].step_done) return;   // uniform over the block
+    const RbBaseArgs b = btab[w.x];
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    for (int k = threadIdx.x; k < w.z; k += blockDim.x) {
+        const long long e = (long long)w.y + k;
+        const int ix = (int)(e % b.sy), iy = (int)(e / b.sy);
+        if (ix < b.nx) rb_base_cell(b, ix, iy, 0, part, pmax);   // padding columns hold no cell
+    }
+    block_reduce_residual(b.acc64, b.norm_max, part, pmax);
+}
+
+// ---------------------------------------------------------------------------
 #define BCK(call)                                                 \
     do {                                                          \
         cudaError_t _e = (call);                                  \
@@ -396,11 +487,27 @@ struct ptd_batch {
     int ncwork = 0;
     int4* fwork = nullptr;
     int nfwork = 0;
+    // FP32_RB (H64, Hold64, D64, Hf, Df, d, w32 as above): FP64 base fluxes,
+    // FP32 base defects, FP64 check residual, per-instance control blocks
+    bool rb = false;
+    double* wb64[2] = {nullptr, nullptr};
+    float* tb32[2] = {nullptr, nullptr};
+    float* Rb32 = nullptr;
+    double* Cb64 = nullptr;
+    RbDev* rdev = nullptr;
+    RbDev* h_rdev = nullptr;
+    RbArgs* rbtab[2] = {nullptr, nullptr};
+    RbFoldArgs* ftab = nullptr;
+    RbBaseArgs* btab = nullptr;
+    int* passes = nullptr;
+    int* h_passes = nullptr;
+    cudaGraphExec_t gstep = nullptr;
+    int blocks_per_phase = 1;
     // common
     int4* work = nullptr;
     int nwork = 0;
     int nchk = 10;
-    int tb = 1;        // FP32_DC: inner iterations per launch (2: temporal blocking)
+    int tb = 1;        // FP32_DC, FP32_RB: FP32 iterations per launch (2: temporal blocking)
     int stall = 10;
     cudaGraphExec_t g[2] = {nullptr, nullptr};
     int kernels_per_graph = 0;
@@ -459,13 +566,30 @@ cudaError_t launch_dc_batch(ptd_batch* b, int par, bool check)
     return cudaGetLastError();
 }
 
+cudaError_t launch_rb_batch(ptd_batch* b, int par, bool check)
+{
+    const dim3 blk(32, b->cfg.warps2d);
+    const RbArgs* t = b->rbtab[par];
+#define RBB(M)                                                                                                 \
+    (b->tb == 2 ? (check ? rb2d_batch_kernel<M, true, 2><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)  \
+                         : rb2d_batch_kernel<M, false, 2><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)) \
+                : (check ? rb2d_batch_kernel<M, true, 1><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)  \
+                         : rb2d_batch_kernel<M, false, 1><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)))
+    if (b->model == LIN) RBB(LIN);
+    else if (b->model == LINSTEP) RBB(LINSTEP);
+    else RBB(NONLIN);
+#undef RBB
+    return cudaGetLastError();
+}
+
 void build_work(ptd_batch* b, std::vector<int4>& work)
 {
     work.clear();
     const int W = b->cfg.warps2d, ch = b->cfg.chunk2d;
     for (int i = 0; i < b->ninst; ++i) {
         // x tiles of 31 updated columns, or 28 for the temporally blocked kernel
-        const int tiles = (b->dc && b->tb == 2) ? (b->inst[i].nx - 2 + 27) / 28 : (b->inst[i].nx - 2 + 30) / 31;
+        const int tiles = ((b->dc || b->rb) && b->tb == 2) ? (b->inst[i].nx - 2 + 27) / 28
+                                                            : (b->inst[i].nx - 2 + 30) / 31;
         const int bx = (tiles + W - 1) / W;
         const int by = (b->inst[i].ny - 2 + ch - 1) / ch;
         for (int y = 0; y < by; ++y)
@@ -486,8 +610,76 @@ int upload_work(ptd_batch* b)
     return PTD_OK;
 }
 
+// FP32_RB: one physical step of the batch as one graph (the header comment).
+int capture_rb(ptd_batch* b)
+{
+    if (b->gstep) cudaGraphExecDestroy(b->gstep);
+    b->gstep = nullptr;
+    cudaGraph_t g = nullptr;
+    BCK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle loop;
+    cudaError_t err = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "batch: conditional graph node");
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    err = cudaStreamBeginCaptureToGraph(b->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "cudaStreamBeginCaptureToGraph");
+    }
+    const int n = b->ninst, nb = (n + 127) / 128;
+    const int nl = b->nchk / b->tb;   // launches per check block (tb divides nchk)
+    int par = 0, nk = 0;
+    for (int blk = 0; blk < b->blocks_per_phase && err == cudaSuccess; ++blk) {
+        for (int it = 0; it < nl && err == cudaSuccess; ++it) {
+            err = launch_rb_batch(b, par, it == nl - 1);
+            par ^= 1;
+            ++nk;
+        }
+        if (err == cudaSuccess) {
+            rb_check_judge_batch_kernel<<<nb, 128, 0, b->s>>>(b->rdev, n, b->nchk, b->bp.itmax, b->bp.tol,
+                                                              b->norm_den, b->bp.norm == PTD_NORM_MAX);
+            err = cudaGetLastError();
+            ++nk;
+        }
+    }
+    if (err == cudaSuccess) {
+        rb_fold_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->ftab, b->rdev, b->fwork, b->tb);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) {
+        rb_base_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->btab, b->rdev, b->fwork, 1);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) {
+        rb_base_judge_batch_kernel<<<1, 256, 0, b->s>>>(b->rdev, n, b->bp.tol, b->norm_den,
+                                                        b->bp.norm == PTD_NORM_MAX, loop, 1, b->passes);
+        err = cudaGetLastError();
+    }
+    nk += 3;
+    cudaError_t e2 = cudaStreamEndCapture(b->s, &body);
+    if (err != cudaSuccess || e2 != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err != cudaSuccess ? err : e2, "batch: capture the rebased phase");
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&b->gstep, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+    b->kernels_per_graph = nk;
+    return PTD_OK;
+}
+
 int capture(ptd_batch* b)
 {
+    if (b->rb) return capture_rb(b);
     for (int q = 0; q < 2; ++q) {
         if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
         b->g[q] = nullptr;
@@ -550,8 +742,119 @@ void one_grid_params(const ptd_batch_params& bp, int nx, int ny, ptd_params& p)
     p.norm = bp.norm;
 }
 
+// Field work: chunks of every instance's padded fields ({instance, first
+// element, count}), and (with cells) of its inner cells.
+int build_chunks(ptd_batch* b, bool cells)
+{
+    std::vector<int4> cw, fw;
+    const int CH = 2048;
+    for (int i = 0; i < b->ninst; ++i) {
+        const Inst& I = b->inst[i];
+        const long long nc = (long long)(I.nx - 2) * (I.ny - 2);
+        for (long long s0 = 0; cells && s0 < nc; s0 += CH)
+            cw.push_back(make_int4(i, (int)s0, (int)std::min<long long>(CH, nc - s0), 0));
+        for (long long s0 = 0; s0 < I.nfield; s0 += CH)
+            fw.push_back(make_int4(i, (int)s0, (int)std::min<long long>(CH, I.nfield - s0), 0));
+    }
+    int rc = cells ? balloc(&b->cwork, cw.size() * sizeof(int4)) : PTD_OK;
+    if (!rc) rc = balloc(&b->fwork, fw.size() * sizeof(int4));
+    if (rc) return rc;
+    if (cells) BCK(cudaMemcpy(b->cwork, cw.data(), cw.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->fwork, fw.data(), fw.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b->ncwork = (int)cw.size();
+    b->nfwork = (int)fw.size();
+    return PTD_OK;
+}
+
+// FP32_RB: the per-instance argument blocks of the iteration (per buffer
+// parity), the fold and the base kernels.
+int fill_tables_rb(ptd_batch* b)
+{
+    const int n = b->ninst;
+    std::vector<RbArgs> t[2] = {std::vector<RbArgs>(n), std::vector<RbArgs>(n)};
+    std::vector<RbFoldArgs> ft(n);
+    std::vector<RbBaseArgs> bt(n);
+    std::vector<double> nd(n);
+    for (int i = 0; i < n; ++i) {
+        const Inst& I = b->inst[i];
+        const long long o = I.off;
+        nd[i] = I.dv.norm_den;
+        for (int q = 0; q < 2; ++q) {
+            RbArgs& a = t[q][i];
+            std::memset(&a, 0, sizeof(a));
+            a.nx = I.nx;
+            a.ny = I.ny;
+            a.nz = 1;
+            a.sy = I.sy;
+            a.sz = I.nfield;
+            a.rdt = (float)I.dv.rdt;
+            for (int d = 0; d < 3; ++d) a.sig[d] = (float)I.dv.sig[d];
+            a.c_lin = (float)I.dv.c_lin;
+            a.e_lin = (float)I.dv.e_lin;
+            a.f = fparams(I.dv);
+            a.din = b->d[q] + o;
+            a.dout = b->d[q ^ 1] + o;
+            for (int d = 0; d < 3; ++d) {
+                const int dd = d < 2 ? d : 0;
+                a.win[d] = b->w32[dd][q] + o;
+                a.wout[d] = b->w32[dd][q ^ 1] + o;
+                a.tb[d] = b->tb32[dd] + o;
+            }
+            a.Rb = b->Rb32 + o;
+            a.Cb = b->Cb64 + o;
+            a.Hf = b->Hf + o;
+            a.Df = b->Df ? b->Df + o : nullptr;
+            a.skip = &b->rdev[i].skip;
+            a.acc = &b->rdev[i].acc;
+            a.norm_max = b->bp.norm == PTD_NORM_MAX;
+        }
+        RbFoldArgs& f = ft[i];
+        std::memset(&f, 0, sizeof(f));
+        f.n = I.nfield;
+        f.H = b->H64 + o;
+        f.ndim = 2;
+        f.d[0] = b->d[0] + o;
+        f.d[1] = b->d[1] + o;
+        for (int d = 0; d < 2; ++d) {
+            f.wb[d] = b->wb64[d] + o;
+            f.w[d][0] = b->w32[d][0] + o;
+            f.w[d][1] = b->w32[d][1] + o;
+        }
+        RbBaseArgs& g = bt[i];
+        std::memset(&g, 0, sizeof(g));
+        g.nx = I.nx;
+        g.ny = I.ny;
+        g.nz = 1;
+        g.ndim = 2;
+        g.model = b->model;
+        g.sy = I.sy;
+        g.sz = I.nfield;
+        g.rdt = I.dv.rdt;
+        for (int d = 0; d < 3; ++d) g.sig[d] = I.dv.sig[d];
+        g.H = b->H64 + o;
+        g.Hold = b->Hold64 + o;
+        for (int d = 0; d < 2; ++d) {
+            g.wb[d] = b->wb64[d] + o;
+            g.tb[d] = b->tb32[d] + o;
+        }
+        g.D = b->D64 ? b->D64 + o : nullptr;
+        g.Rb = b->Rb32 + o;
+        g.Cb = b->Cb64 + o;
+        g.Hf = b->Hf + o;
+        g.acc64 = &b->rdev[i].acc64;
+        g.norm_max = b->bp.norm == PTD_NORM_MAX;
+    }
+    for (int q = 0; q < 2; ++q)
+        BCK(cudaMemcpy(b->rbtab[q], t[q].data(), n * sizeof(RbArgs), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->ftab, ft.data(), n * sizeof(RbFoldArgs), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->btab, bt.data(), n * sizeof(RbBaseArgs), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->norm_den, nd.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    return build_chunks(b, false);
+}
+
 int fill_tables(ptd_batch* b)
 {
+    if (b->rb) return fill_tables_rb(b);
     const int n = b->ninst;
     if (!b->dc) {
         std::vector<PTArgs> t[2] = {std::vector<PTArgs>(n), std::vector<PTArgs>(n)};
@@ -641,24 +944,7 @@ int fill_tables(ptd_batch* b)
     BCK(cudaMemcpy(b->H_ptrs, hp.data(), n * sizeof(double*), cudaMemcpyHostToDevice));
     BCK(cudaMemcpy(b->bst, bd.data(), n * sizeof(BDev), cudaMemcpyHostToDevice));
     // cell work (inner cells, residual) and field work (whole fields, apply)
-    std::vector<int4> cw, fw;
-    const int CH = 2048;
-    for (int i = 0; i < n; ++i) {
-        const Inst& I = b->inst[i];
-        const long long cells = (long long)(I.nx - 2) * (I.ny - 2);
-        for (long long s0 = 0; s0 < cells; s0 += CH)
-            cw.push_back(make_int4(i, (int)s0, (int)std::min<long long>(CH, cells - s0), 0));
-        for (long long s0 = 0; s0 < I.nfield; s0 += CH)
-            fw.push_back(make_int4(i, (int)s0, (int)std::min<long long>(CH, I.nfield - s0), 0));
-    }
-    int rc = balloc(&b->cwork, cw.size() * sizeof(int4));
-    if (!rc) rc = balloc(&b->fwork, fw.size() * sizeof(int4));
-    if (rc) return rc;
-    BCK(cudaMemcpy(b->cwork, cw.data(), cw.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    BCK(cudaMemcpy(b->fwork, fw.data(), fw.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    b->ncwork = (int)cw.size();
-    b->nfwork = (int)fw.size();
-    return PTD_OK;
+    return build_chunks(b, true);
 }
 
 void free_batch(ptd_batch* b)
@@ -667,6 +953,12 @@ void free_batch(ptd_batch* b)
     if (b->s) cudaStreamSynchronize(b->s);
     for (int q = 0; q < 2; ++q)
         if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
+    if (b->gstep) cudaGraphExecDestroy(b->gstep);
+    void* rbp[] = {b->wb64[0], b->wb64[1], b->tb32[0], b->tb32[1], b->Rb32, b->Cb64, b->rdev,
+                   b->rbtab[0], b->rbtab[1], b->ftab, b->btab, b->passes};
+    for (void* p : rbp) cudaFree(p);
+    if (b->h_rdev) cudaFreeHost(b->h_rdev);
+    if (b->h_passes) cudaFreeHost(b->h_passes);
     void* ptrs[] = {b->H[0], b->H[1], b->Hold, b->W[0][0], b->W[0][1], b->W[1][0], b->W[1][1], b->D,
                     b->stage, b->st, b->norm_den, b->tab[0], b->tab[1], b->H64, b->Hold64, b->D64, b->Hf,
                     b->Df, b->rf, b->d[0], b->d[1], b->w32[0][0], b->w32[0][1], b->w32[1][0], b->w32[1][1],
@@ -740,7 +1032,7 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
         return bfail(PTD_EINVAL, "batch: itmax must be a positive multiple of nchk");
     for (int k = 0; k < 8; ++k)
         if (p->reserved[k]) return bfail(PTD_EINVAL, "reserved fields must be zero");
-    if (p->precision == PTD_PREC_DFH || p->precision == PTD_PREC_FP32_RB) return bfail(PTD_EINVAL, "batch: precision FP64, DF64 or FP32_DC");
+    if (p->precision == PTD_PREC_DFH) return bfail(PTD_EINVAL, "batch: precision FP64, DF64, FP32_DC or FP32_RB");
     ptd_batch* b = new (std::nothrow) ptd_batch();
     if (!b) return bfail(PTD_ENOMEM, "batch: host allocation failed");
     b->bp = *p;
@@ -748,6 +1040,7 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
     b->model = p->model;
     b->df64 = p->precision == PTD_PREC_DF64;
     b->dc = p->precision == PTD_PREC_FP32_DC;
+    b->rb = p->precision == PTD_PREC_FP32_RB;
     b->inst.resize(b->ninst);
     long long off = 0;
     int rc = PTD_OK;
@@ -781,7 +1074,9 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
     }
     b->nchk = b->dc ? std::max(1, std::min(p->nchk, 50)) : p->nchk;
     if (b->dc && p->itmax % b->nchk) b->nchk = p->nchk;
-    b->tb = (b->dc && b->nchk % 2 == 0 && !(p->flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
+    b->tb = ((b->dc || b->rb) && b->nchk % 2 == 0 && !(p->flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
+    // FP32_RB: a phase is the check blocks of ~200 iterations between two rebases
+    b->blocks_per_phase = std::max(1, (200 + b->nchk - 1) / b->nchk);
     cudaError_t e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         free_batch(b);
@@ -789,7 +1084,42 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
     }
     const size_t db = (size_t)b->total * sizeof(double), fb = (size_t)b->total * sizeof(float);
     const int n = b->ninst;
-    if (!b->dc) {
+    if (b->rb) {
+        const bool ls = p->model == PTD_MODEL_LINSTEP;
+        rc = balloc(&b->H64, db);
+        if (!rc) rc = balloc(&b->Hold64, db);
+        if (!rc && ls) rc = balloc(&b->D64, db);
+        if (!rc) rc = balloc(&b->Hf, fb);
+        if (!rc && ls) rc = balloc(&b->Df, fb);
+        for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->d[q], fb);
+        for (int d = 0; d < 2 && !rc; ++d) {
+            for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->w32[d][q], fb);
+            if (!rc) rc = balloc(&b->wb64[d], db);
+            if (!rc) rc = balloc(&b->tb32[d], fb);
+        }
+        if (!rc) rc = balloc(&b->Rb32, fb);
+        if (!rc) rc = balloc(&b->Cb64, db);
+        if (!rc) rc = balloc(&b->rdev, n * sizeof(RbDev));
+        for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->rbtab[q], n * sizeof(RbArgs));
+        if (!rc) rc = balloc(&b->ftab, n * sizeof(RbFoldArgs));
+        if (!rc) rc = balloc(&b->btab, n * sizeof(RbBaseArgs));
+        if (!rc) rc = balloc(&b->norm_den, n * sizeof(double));
+        if (!rc) rc = balloc(&b->passes, sizeof(int));
+        if (!rc && (cudaMallocHost((void**)&b->h_rdev, n * sizeof(RbDev)) != cudaSuccess ||
+                    cudaMallocHost((void**)&b->h_passes, sizeof(int)) != cudaSuccess))
+            rc = bfail(PTD_ENOMEM, "batch: cudaMallocHost failed");
+        if (!rc) {
+            double* zd[] = {b->wb64[0], b->wb64[1], b->Cb64};
+            for (double* z : zd)
+                if (cudaMemset(z, 0, db) != cudaSuccess) rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
+            // faces past the last one of each direction are read (never used) by the halo lanes
+            float* zf[] = {b->tb32[0], b->tb32[1], b->Rb32};
+            for (float* z : zf)
+                if (cudaMemset(z, 0, fb) != cudaSuccess) rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
+            if (cudaMemset(b->rdev, 0, n * sizeof(RbDev)) != cudaSuccess)
+                rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
+        }
+    } else if (!b->dc) {
         for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->H[q], db);
         if (!rc) rc = balloc(&b->Hold, db);
         for (int d = 0; d < 2 && !rc; ++d)
@@ -857,7 +1187,8 @@ extern "C" int ptd_batch_counters(ptd_batch* b, int64_t* launches, int64_t* iter
 
 static int batch_read_states(ptd_batch* b)
 {
-    if (b->dc) BCK(cudaMemcpyAsync(b->h_bst, b->bst, b->ninst * sizeof(BDev), cudaMemcpyDeviceToHost, b->s));
+    if (b->rb) BCK(cudaMemcpyAsync(b->h_rdev, b->rdev, b->ninst * sizeof(RbDev), cudaMemcpyDeviceToHost, b->s));
+    else if (b->dc) BCK(cudaMemcpyAsync(b->h_bst, b->bst, b->ninst * sizeof(BDev), cudaMemcpyDeviceToHost, b->s));
     else BCK(cudaMemcpyAsync(b->h_st, b->st, b->ninst * sizeof(DevState), cudaMemcpyDeviceToHost, b->s));
     BCK(cudaStreamSynchronize(b->s));
     return PTD_OK;
@@ -983,6 +1314,39 @@ static int batch_dc_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
     return PTD_OK;
 }
 
+// FP32_RB: one physical step of every instance -- the base quantities of the
+// step's start state, then the step graph (phases until every instance has
+// stopped).  An instance that reaches itmax stops at its last full check
+// block.
+static int batch_rb_step(ptd_batch* b, int32_t* iters, double* err_last, int* nan_any, int* capped_any)
+{
+    const int n = b->ninst, nb = (n + 127) / 128;
+    rb_reset_batch_kernel<<<nb, 128, 0, b->s>>>(b->rdev, n);
+    BCK(cudaGetLastError());
+    rb_base_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->btab, b->rdev, b->fwork, 0);
+    BCK(cudaGetLastError());
+    rb_base_judge_batch_kernel<<<1, 256, 0, b->s>>>(b->rdev, n, b->bp.tol, b->norm_den, b->bp.norm == PTD_NORM_MAX,
+                                                    cudaGraphConditionalHandle{}, 0, b->passes);
+    BCK(cudaGetLastError());
+    BCK(cudaMemsetAsync(b->passes, 0, sizeof(int), b->s));
+    b->launches += 3;
+    if (b->nchk <= b->bp.itmax) BCK(cudaGraphLaunch(b->gstep, b->s));
+    BCK(cudaMemcpyAsync(b->h_passes, b->passes, sizeof(int), cudaMemcpyDeviceToHost, b->s));
+    int rc = batch_read_states(b);
+    if (rc) return rc;
+    b->launches += (long long)(*b->h_passes) * b->kernels_per_graph;
+    for (int i = 0; i < n; ++i) {
+        const RbDev& st = b->h_rdev[i];
+        iters[i] = st.iter;
+        b->iterations += st.iter;
+        if (err_last) err_last[i] = st.err64;
+        if (st.step_done == DONE_NAN) *nan_any = 1;
+        if (st.step_done == DONE_CAP || st.step_done == DONE_RUNNING) *capped_any = 1;
+    }
+    BCK(cudaMemcpyAsync(b->Hold64, b->H64, (size_t)b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->s));
+    return PTD_OK;
+}
+
 extern "C" int ptd_batch_solve(ptd_batch* b, double* const* H, const double* const* D, int32_t* iters,
                                double* err_last, int32_t* n_done)
 {
@@ -994,7 +1358,23 @@ extern "C" int ptd_batch_solve(ptd_batch* b, double* const* H, const double* con
     const size_t db = (size_t)b->total * sizeof(double);
     int rc;
     const int n = b->ninst;
-    if (!b->dc) {
+    if (b->rb) {
+        const size_t fb = (size_t)b->total * sizeof(float);
+        BCK(cudaMemsetAsync(b->H64, 0, db, b->s));
+        if ((rc = upload(b, b->H64, H))) return rc;
+        BCK(cudaMemcpyAsync(b->Hold64, b->H64, db, cudaMemcpyDeviceToDevice, b->s));
+        for (int d = 0; d < 2; ++d) {
+            BCK(cudaMemsetAsync(b->wb64[d], 0, db, b->s));
+            for (int q = 0; q < 2; ++q) BCK(cudaMemsetAsync(b->w32[d][q], 0, fb, b->s));
+        }
+        for (int q = 0; q < 2; ++q) BCK(cudaMemsetAsync(b->d[q], 0, fb, b->s));
+        if (b->D64) {
+            BCK(cudaMemsetAsync(b->D64, 0, db, b->s));
+            if ((rc = upload(b, b->D64, D))) return rc;
+            tofloat_batch_kernel<<<fill_blocks(), 256, 0, b->s>>>(b->D64, b->Df, b->total);
+            BCK(cudaGetLastError());
+        }
+    } else if (!b->dc) {
         double* h0 = b->df64 ? b->stage : (double*)b->H[0];
         BCK(cudaMemsetAsync(h0, 0, db, b->s));
         if ((rc = upload(b, h0, H))) return rc;
@@ -1027,8 +1407,9 @@ extern "C" int ptd_batch_solve(ptd_batch* b, double* const* H, const double* con
     std::vector<int32_t> it(n);
     int nan_any = 0, capped_any = 0;
     for (int step = 0; step < b->bp.nt; ++step) {
-        rc = b->dc ? batch_dc_step(b, it.data(), err_last, &nan_any, &capped_any)
-                   : batch_pt_step(b, it.data(), err_last, &nan_any);
+        rc = b->rb   ? batch_rb_step(b, it.data(), err_last, &nan_any, &capped_any)
+             : b->dc ? batch_dc_step(b, it.data(), err_last, &nan_any, &capped_any)
+                     : batch_pt_step(b, it.data(), err_last, &nan_any);
         if (rc) return rc;
         for (int i = 0; i < n; ++i) iters[(size_t)i * b->bp.nt + step] = it[i];
         if (nan_any) break;
@@ -1037,7 +1418,7 @@ extern "C" int ptd_batch_solve(ptd_batch* b, double* const* H, const double* con
         BCK(launch_from_df64(b->H[0], b->stage, b->total, b->s));
         rc = download(b, H, b->stage);
     } else {
-        rc = download(b, H, b->dc ? b->H64 : (double*)b->H[0]);
+        rc = download(b, H, (b->dc || b->rb) ? b->H64 : (double*)b->H[0]);
     }
     if (rc) return rc;
     BCK(cudaStreamSynchronize(b->s));
@@ -1056,7 +1437,8 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
     if (!b) return bfail(PTD_EINVAL, "batch is NULL");
     const int Ws[] = {2, 4, 8};
     const int Cs[] = {16, 32, 64, 128};
-    const bool try_tb = b->dc && b->nchk % 2 == 0 && !(b->bp.flags & PTD_FLAG_DC_NO_TBLOCK);
+    const bool fp32 = b->dc || b->rb;
+    const bool try_tb = fp32 && b->nchk % 2 == 0 && !(b->bp.flags & PTD_FLAG_DC_NO_TBLOCK);
     float best = 1e30f;   // ms per inner iteration
     LaunchCfg bestc = b->cfg;
     int best_tb = b->tb;
@@ -1066,7 +1448,9 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
     // plain iterations on the current fields with every instance's flag cleared
     // (the fields are zero after ptd_batch_create; ptd_batch_solve uploads its
     // own state afterwards)
-    if (b->dc) {
+    if (b->rb) {
+        BCK(cudaMemsetAsync(b->rdev, 0, b->ninst * sizeof(RbDev), b->s));
+    } else if (b->dc) {
         set_done_batch_kernel<<<(b->ninst + 127) / 128, 128, 0, b->s>>>(b->bst, b->ninst, 0);
         BCK(cudaGetLastError());
     } else {
@@ -1075,7 +1459,7 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
     for (int tbc = 1; tbc <= (try_tb ? 2 : 1); ++tbc)
         for (int W : Ws)
             for (int C : Cs) {
-                b->tb = b->dc ? tbc : 1;
+                b->tb = fp32 ? tbc : 1;
                 b->cfg.warps2d = W;
                 b->cfg.chunk2d = C;
                 int rc = upload_work(b);
@@ -1084,7 +1468,9 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
                 for (int rep = 0; rep < 2; ++rep) {
                     BCK(cudaEventRecord(e0, b->s));
                     for (int it = 0; it < nl; ++it)
-                        BCK(b->dc ? launch_dc_batch(b, it & 1, false) : launch_pt_batch(b, it & 1, false));
+                        BCK(b->rb   ? launch_rb_batch(b, it & 1, false)
+                            : b->dc ? launch_dc_batch(b, it & 1, false)
+                                    : launch_pt_batch(b, it & 1, false));
                     BCK(cudaEventRecord(e1, b->s));
                     BCK(cudaEventSynchronize(e1));
                 }
@@ -1120,6 +1506,6 @@ extern "C" int ptd_batch_config(ptd_batch* b, int32_t* warps, int32_t* chunk, in
     if (!b) return bfail(PTD_EINVAL, "batch is NULL");
     if (warps) *warps = b->cfg.warps2d;
     if (chunk) *chunk = b->cfg.chunk2d;
-    if (iters_per_launch) *iters_per_launch = b->dc ? b->tb : 1;
+    if (iters_per_launch) *iters_per_launch = (b->dc || b->rb) ? b->tb : 1;
     return PTD_OK;
 }

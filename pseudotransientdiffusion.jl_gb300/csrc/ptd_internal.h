@@ -40,6 +40,7 @@ void derive(const ptd_params& p, Derived& dv);
 void fill_args(const ptd_params& p, const Derived& dv, PTArgs& a);
 FParams fparams(const Derived& dv);
 LaunchCfg tuned_config(const ptd_params& p);
+int z_chunk(long long bxy, int nz, long long slots);
 int copy_field_in(const ptd_ctx_base& g, double* dst, const double* src, cudaStream_t s);
 int copy_field_out(const ptd_ctx_base& g, double* dst, const double* src, cudaStream_t s);
 

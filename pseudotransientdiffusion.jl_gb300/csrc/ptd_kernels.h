@@ -51,7 +51,8 @@ cudaError_t launch_judge(DevState* st, double* errhist, int errcap, int nchk, in
 cudaError_t launch_judge_parts(DevState* st, const double* parts, long long nparts, double* errhist, int errcap,
                                int nchk, int itmax, double tol, double norm_den, int norm_max,
                                cudaGraphConditionalHandle loop, cudaStream_t s);
-long long pt_check_slots(int ndim, int nx, int ny, int nz, const LaunchCfg& cfg, bool consistent);
+// num: NUM_* of the kernels (the double-float forms tile differently)
+long long pt_check_slots(int ndim, int nx, int ny, int nz, const LaunchCfg& cfg, bool consistent, int num);
 cudaError_t launch_reset_state(DevState* st, cudaStream_t s);
 cudaError_t preload_pt2d_f64();
 

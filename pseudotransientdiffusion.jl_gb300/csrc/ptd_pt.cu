@@ -23,7 +23,7 @@
 // as y rows of an x-y tile (rows 1..R-1 updated, row 0 the neighbour, y faces
 // exchanged through shared memory, one barrier per plane) and marches the
 // tile along z carrying the z face below in a register.
-#include "ptd_pt_body.cuh"
+#include "ptd_pair_body.cuh"
 
 namespace ptd {
 
@@ -65,6 +65,21 @@ __global__ void __launch_bounds__(32 * R, (CHECK || MODEL == LINSTEP || MODEL ==
     pt3d_body<N, MODEL, CHECK, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, chunk, part, pmax);
     if (CHECK)
         block_reduce_residual(a, part, pmax, ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+}
+
+// 2D, the double-float forms (DF64, DFH): two x-adjacent cells per lane
+// (ptd_pair_body.cuh), 62-cell tiles.  (The same pairing in 3D was slower than
+// the one-cell kernel at 512^3 -- DF64 2244 against 2045 us: its 60-96
+// registers leave 16-32 resident warps per SM for a march with a barrier per
+// plane.)
+template <class N, int MODEL, bool CHECK>
+__global__ void __launch_bounds__(256) pt2d_pair_kernel(PTArgs a, int chunk)
+{
+    if (step_done(a.done)) return;
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    const long long slot = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.y + threadIdx.y;
+    pt2d_pair_body<N, MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -241,7 +256,18 @@ static cudaError_t launch_model(const PTArgs& a, int ndim, const LaunchCfg& cfg,
     if (ndim == 1) {
         const int bs = 256;
         pt1d_kernel<N, MODEL, CHECK><<<(a.nx + bs - 1) / bs, bs, 0, s>>>(a);
-    } else if (ndim == 2) {
+        return cudaGetLastError();
+    }
+    if constexpr (!N::native) {
+        if (ndim == 2) {
+            const int W = cfg.warps2d;
+            const int tiles = (a.nx - 2 + 61) / 62;
+            dim3 grid((tiles + W - 1) / W, (a.ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);
+            pt2d_pair_kernel<N, MODEL, CHECK><<<grid, dim3(32, W), 0, s>>>(a, cfg.chunk2d);
+            return cudaGetLastError();
+        }
+    }
+    if (ndim == 2) {
         const int W = cfg.warps2d;
         const int tiles = (a.nx - 2 + 30) / 31;
         dim3 grid((tiles + W - 1) / W, (a.ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);
@@ -342,18 +368,20 @@ cudaError_t launch_judge_parts(DevState* st, const double* parts, long long npar
 // The number of check-residual slots the fused kernel of a check iteration
 // writes with this launch shape (the grids of launch_model below: blocks in
 // 1D and 3D, warps in 2D), or the consistent-residual kernel's blocks.
-long long pt_check_slots(int ndim, int nx, int ny, int nz, const LaunchCfg& cfg, bool consistent)
+long long pt_check_slots(int ndim, int nx, int ny, int nz, const LaunchCfg& cfg, bool consistent, int num)
 {
     if (consistent) return fill_blocks();
     if (ndim == 1) return (nx + 255) / 256;
     if (ndim == 2) {
+        const int tw = num != NUM_F64 ? 62 : 31;   // the double-float forms: two cells per lane
         const int W = cfg.warps2d;
-        const long long tiles = (nx - 2 + 30) / 31;
+        const long long tiles = (nx - 2 + tw - 1) / tw;
         return ((tiles + W - 1) / W) * W * (long long)((ny - 2 + cfg.chunk2d - 1) / cfg.chunk2d);
     }
     const long long tx = (nx - 2 + 30) / 31;
     const long long nzc = (nz - 2 + cfg.chunk3d - 1) / cfg.chunk3d;
-    const long long ty = cfg.rows3d == 8 ? (ny - 2 + 6) / 7 : (ny - 2 + 14) / 15;
+    const int rows = cfg.rows3d;
+    const long long ty = (ny - 2 + rows - 2) / (rows - 1);
     return tx * ty * nzc;
 }
 

@@ -26,6 +26,27 @@ int sm_count()
     return cache[dev];
 }
 
+// The z march length of a 3D launch of bxy CTAs per z chunk on `slots`
+// resident CTA slots: the longest march (512..16) whose CTA count fills the
+// slots in whole waves to >= 90 % (wave quantization), else the best filling
+// one.
+int z_chunk(long long bxy, int nz, long long slots)
+{
+    int best = 16;
+    double best_eff = -1.0;
+    for (int chunk = 512; chunk >= 16; chunk /= 2) {
+        const long long nb = bxy * ((nz - 2 + chunk - 1) / chunk);
+        const long long waves = (nb + slots - 1) / slots;
+        const double eff = (double)nb / (double)(waves * slots);
+        if (nb >= slots && eff >= 0.9) return chunk;
+        if (eff > best_eff) {
+            best_eff = eff;
+            best = chunk;
+        }
+    }
+    return best;
+}
+
 LaunchCfg tuned_config(const ptd_params& p)
 {
     LaunchCfg c;
@@ -39,29 +60,12 @@ LaunchCfg tuned_config(const ptd_params& p)
         c.warps2d = 2;
         c.chunk2d = 16;
     } else if (p.ndim == 3) {
-        // 512-thread CTAs, 3 resident per SM at <= 40 registers (456 slots on
-        // the 152 SMs of a GB300).
-        // Take the longest z march whose CTA count fills the slots in whole
-        // waves to >= 90 % (wave quantization), else the best filling one.
-        const int rows = 16;
+        // 512-thread CTAs of 31 x 15 updated cells, 3 resident per SM at <= 40
+        // registers (456 slots on the 152 SMs of a GB300).
+        const int rows = 16, tw = 31;
         const long long slots = 3LL * sm_count();
-        const long long bxy = (long long)((p.nx - 2 + 30) / 31) * ((p.ny - 2 + rows - 2) / (rows - 1));
-        int best = 16;
-        double best_eff = -1.0;
-        for (int chunk = 512; chunk >= 16; chunk /= 2) {
-            const long long nb = bxy * ((p.nz - 2 + chunk - 1) / chunk);
-            const long long waves = (nb + slots - 1) / slots;
-            const double eff = (double)nb / (double)(waves * slots);
-            if (nb >= slots && eff >= 0.9) {
-                best = chunk;
-                best_eff = 2.0;
-                break;
-            }
-            if (eff > best_eff) {
-                best_eff = eff;
-                best = chunk;
-            }
-        }
+        const long long bxy = (long long)((p.nx - 2 + tw - 1) / tw) * ((p.ny - 2 + rows - 2) / (rows - 1));
+        const int best = z_chunk(bxy, p.nz, slots);
         c.chunk3d = best;
         c.rows3d = rows;
     }

@@ -63,7 +63,8 @@ def _lib():
 def batch_params(ninst, model=LINSTEP, precision="fp32_dc", **kw) -> PtdBatchParams:
     p = PtdBatchParams()
     _abi.check(_lib().ptd_batch_params_init(C.byref(p), ninst, model), "ptd_batch_params_init")
-    p.precision = {"fp64": 0, "fp32_dc": 1, "df64": 2}[precision] if isinstance(precision, str) else precision
+    p.precision = ({"fp64": 0, "fp32_dc": 1, "df64": 2, "fp32_rb": 4}[precision] if isinstance(precision, str)
+                   else precision)
     for k, v in kw.items():
         setattr(p, k, v)
     return p

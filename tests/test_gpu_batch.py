@@ -1,6 +1,8 @@
 """Batched solves (ptd_batch_*): every instance must match the one-grid
 oracle run of its own problem -- equal PT iteration counts and relative L2
-error <= 1e-10 for FP64/DF64; the converged-to-tol bound for FP32_DC."""
+error <= 1e-10 for FP64/DF64; the converged-to-tol bound for FP32_DC and
+FP32_RB (whose counts also stay within 1 % plus two check blocks of the
+oracle's, and equal those of the one-grid FP32_RB solver)."""
 import numpy as np
 import pytest
 
@@ -22,7 +24,7 @@ def oracle_instance(model, H0, D, **kw):
     return O.solve(s, H0, D)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "df64", "fp32_dc"])
+@pytest.mark.parametrize("prec", ["fp64", "df64", "fp32_dc", "fp32_rb"])
 @pytest.mark.parametrize("model", [S.LINSTEP, S.NONLIN])
 def test_batch_matches_oracle(prec, model):
     sizes, Hs, Ds = ptdiff.batch_instances(7, seed=3, nmin=12, nmax=90)
@@ -40,7 +42,10 @@ def test_batch_matches_oracle(prec, model):
         Hr, it_r, _, st = oracle_instance(model, Hs0[k], None if Ds is None else Ds[k], ttot=0.2 * nt,
                                           resc=p.resc)
         assert st == 0
-        if prec == "fp32_dc":
+        if prec == "fp32_rb":
+            for a, b_ in zip(iters[k], it_r):
+                assert abs(int(a) - int(b_)) <= 0.01 * b_ + 2 * p.nchk, (iters[k], it_r)
+        if prec in ("fp32_dc", "fp32_rb"):
             rms = float(np.sqrt(np.mean(np.square(Hr))))
             Ht, _, _, _ = oracle_instance(model, Hs0[k], None if Ds is None else Ds[k], ttot=0.2 * nt,
                                           resc=p.resc, tol=1e-11)
@@ -92,3 +97,36 @@ def test_batch_temporal_blocking_matches_one_iteration_per_launch(model):
     assert np.array_equal(it1, it2)
     for k in range(len(sizes)):
         assert rel_l2(H2[k], H1[k]) <= 1e-12
+
+
+@pytest.mark.parametrize("model", [S.LIN, S.LINSTEP, S.NONLIN])
+@pytest.mark.parametrize("flags", [0, "no_tblock"])
+def test_batch_rebased_matches_one_grid_solver(model, flags):
+    """FP32_RB: each instance of the batch takes the PT iterations of the
+    one-grid FP32_RB solver on its own problem (the same FP32 iterations,
+    rebases and stopping rule) and returns its H; one- and two-iteration
+    launches alike, on uneven instances down to 3 x 3."""
+    from ptdiff import _abi
+
+    fl = 0 if flags == 0 else _abi.FLAG_DC_NO_TBLOCK
+    sizes, Hs, Ds = ptdiff.batch_instances(6, seed=6, nmin=3, nmax=130)
+    if model != S.LINSTEP:
+        Ds = None
+    resc = 1 / 1.2 if model == S.NONLIN else 1.0
+    H = [h.copy(order="F") for h in Hs]
+    p = ptdiff.batch_params(len(sizes), model=model, precision="fp32_rb", nt=2, flags=fl, resc=resc)
+    with ptdiff.BatchSolver(p, sizes, sizes) as b:
+        assert b.config()[2] == (1 if fl else 2)
+        iters, err = b.solve(H, Ds)
+    base = S.SCRIPTS["diff_2D_linstep" if model == S.LINSTEP else "diff_2D_nonlin"
+                     if model == S.NONLIN else "diff_2D_lin"]
+    for k in range(len(sizes)):
+        s = base.with_(ttot=0.4, resc=resc)
+        shape = (int(sizes[k]), int(sizes[k]))
+        H1 = Hs[k].copy(order="F")
+        with ptdiff.Solver(ptdiff.make_params(s, shape, precision="fp32_rb", dc_tblock=not fl)) as sol:
+            it1, _, st = sol.solve(H1, None if Ds is None else Ds[k])
+        assert st == 0
+        assert list(iters[k]) == list(it1), (k, list(iters[k]), list(it1))
+        assert rel_l2(H[k], H1) <= 1e-12
+        assert err[k] <= 1e-8

@@ -154,7 +154,11 @@ def test_rebased_fp32_expm_model_matches_fp64(shape):
     ("diff_2D_lin", (64, 64), {}), ("diff_2D_linstep", (66, 33), {}), ("diff_2D_nonlin", (97, 130), {}),
     ("diff_2D_nonlin", (3, 3), {}), ("diff_2D_linstep", (200, 7), {}), ("diff_2D_lin", (31, 250), {}),
     ("diff_2D_react", (64, 64), {}), ("diff_2D_nonlin", (58, 60), {"nchk": 2}),
-    ("diff_2D_nonlin", (64, 64), {"nchk": 10, "itmax": 95}), ("diff_2D_nonlin_perf", (64, 64), {"itmax": 33})])
+    ("diff_2D_nonlin", (64, 64), {"nchk": 10, "itmax": 95}), ("diff_2D_nonlin_perf", (64, 64), {"itmax": 33}),
+    # LIN and NONLIN run two columns per lane (60 per warp): several tiles, a last
+    # face at the 62nd column of a tile (nx = 60 t + 62), widths around the pitch
+    ("diff_2D_nonlin", (122, 40), {}), ("diff_2D_lin", (182, 61), {}), ("diff_2D_nonlin", (256, 96), {}),
+    ("diff_2D_nonlin", (121, 33), {}), ("diff_2D_lin", (63, 70), {})])
 def test_rebased_fp32_temporal_blocking_matches_one_iteration_per_launch(name, shape, kw):
     s = S.SCRIPTS[name]
     H2, _, it2, _, st2 = run(s, shape, **kw)
@@ -162,6 +166,40 @@ def test_rebased_fp32_temporal_blocking_matches_one_iteration_per_launch(name, s
     assert st1 == 0 and st2 == 0
     assert list(it1) == list(it2)
     assert rel_l2(H2, H1) <= 1e-12
+
+
+# 3D LIN and NONLIN likewise (z temporal blocking, rb3d_tb2_kernel): grids
+# of one z chunk and of several (the march of each chunk starts two planes
+# below it), ragged x/y tiles, odd check cadences (one iteration per
+# launch), itmax not a multiple of nchk, the fixed-iteration protocol.
+@pytest.mark.parametrize("name,shape,kw", [
+    ("diff_3D_lin_multixpu", (34, 30, 28), {}), ("diff_3D_nonlin_multixpu", (40, 33, 45), {}),
+    ("diff_3D_nonlin_multixpu", (3, 3, 3), {}), ("diff_3D_nonlin_multixpu", (70, 17, 21), {"nchk": 2}),
+    ("diff_3D_nonlin_multixpu", (30, 31, 64), {"nchk": 10, "itmax": 95}),
+    ("diff_3D_nonlin_multixpu", (29, 45, 36), {"nchk": 5}),
+    ("diff_3D_nonlin_perf", (32, 32, 32), {"itmax": 33}), ("diff_3D_lin_multixpu", (60, 4, 100), {})])
+def test_rebased_fp32_3d_temporal_blocking_matches_one_iteration_per_launch(name, shape, kw):
+    s = S.SCRIPTS[name]
+    H2, _, it2, _, st2 = run(s, shape, **kw)
+    H1, _, it1, _, st1 = run(s, shape, dc_tblock=False, **kw)
+    assert st1 == 0 and st2 == 0
+    assert list(it1) == list(it2)
+    assert rel_l2(H2, H1) <= 1e-12
+
+
+def test_rebased_fp32_3d_temporal_blocking_fixed_iterations():
+    """Fixed iterations (the perf protocol): the two-iteration launches give
+    the iterates of one-iteration launches, odd counts included."""
+    s = S.SCRIPTS["diff_3D_nonlin_multixpu"]
+    shape = (48, 40, 52)
+    out = []
+    for tblock in (True, False):
+        with ptdiff.Solver(ptdiff.make_params(s, shape, precision="fp32_rb", dc_tblock=tblock)) as sol:
+            H = S.initial_condition(s, *shape)
+            sol.set_state(H)
+            sol.iterate(37)
+            out.append(sol.get_state())
+    assert rel_l2(out[0], out[1]) <= 1e-13
 
 
 def test_rebased_fp32_temporal_blocking_expm_and_iterate():
