@@ -352,19 +352,59 @@ __global__ void tofloat_batch_kernel(const double* src, float* dst, long long n)
 
 // ---------------------------------------------------------------------------
 // FP32_RB: one (TB = 1) or two (TB = 2) rebased FP32 iterations over every
-// instance whose phase is running.
+// instance whose phase is running.  CTA b takes the b-th work item of the
+// running instances (`active`, rebuilt after every judge by
+// compact_active_kernel, in instance order); CTAs past their number return at
+// entry after one load, so once most instances have stopped a launch costs
+// their remaining work rather than a table walk per work item of the whole
+// batch.  (A persistent grid walking the list held 74-98 registers against
+// the march's 40-64.)
 template <int MODEL, bool CHECK, int TB>
 __global__ void __launch_bounds__(256) rb2d_batch_kernel(const RbArgs* __restrict__ tab,
-                                                         const int4* __restrict__ work, int chunk)
+                                                         const int4* __restrict__ work,
+                                                         const int* __restrict__ active, const int* nactive,
+                                                         int chunk)
 {
-    const int4 w = work[blockIdx.x];
+    if ((int)blockIdx.x >= __ldcg(nactive)) return;
+    const int4 w = work[active[blockIdx.x]];
     const RbArgs a = tab[w.x];
-    if (rb_skip(a.skip)) return;
+    if (rb_skip(a.skip)) return;   // its phase ended since the list was built
     double part = 0.0;
     unsigned long long pmax = 0ull;
     // the bodies flush their check partials into a.acc (last step of their march)
     if (TB == 2) rb2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
     else rb2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+}
+
+// The work items of the running instances, in instance order (one block):
+// instance i owns items wfirst[i] .. wfirst[i] + wcount[i] - 1.
+__global__ void __launch_bounds__(256) compact_active_kernel(const RbDev* st, const int* wfirst, const int* wcount,
+                                                             int ninst, int* active, int* nactive)
+{
+    __shared__ int s_off[256];
+    __shared__ int s_base;
+    const int t = threadIdx.x;
+    if (t == 0) s_base = 0;
+    __syncthreads();
+    for (int i0 = 0; i0 < ninst; i0 += 256) {
+        const int i = i0 + t;
+        const int c = (i < ninst && !st[i].skip && !st[i].step_done) ? wcount[i] : 0;
+        // inclusive scan of the counts over the block
+        s_off[t] = c;
+        __syncthreads();
+        for (int o = 1; o < 256; o <<= 1) {
+            const int v = t >= o ? s_off[t - o] : 0;
+            __syncthreads();
+            s_off[t] += v;
+            __syncthreads();
+        }
+        const int start = s_base + s_off[t] - c;
+        for (int q = 0; q < c; ++q) active[start + q] = wfirst[i] + q;
+        __syncthreads();
+        if (t == 255) s_base += s_off[255];
+        __syncthreads();
+    }
+    if (t == 0) *nactive = s_base;
 }
 
 __global__ void rb_reset_batch_kernel(RbDev* st, int ninst)
@@ -501,6 +541,10 @@ struct ptd_batch {
     RbBaseArgs* btab = nullptr;
     int* passes = nullptr;
     int* h_passes = nullptr;
+    int* wfirst = nullptr;     // per instance: its first work item and its count
+    int* wcount = nullptr;
+    int* active = nullptr;     // work items of the running instances, and their count
+    int* nactive = nullptr;
     cudaGraphExec_t gstep = nullptr;
     int blocks_per_phase = 1;
     // common
@@ -570,15 +614,20 @@ cudaError_t launch_rb_batch(ptd_batch* b, int par, bool check)
 {
     const dim3 blk(32, b->cfg.warps2d);
     const RbArgs* t = b->rbtab[par];
-#define RBB(M)                                                                                                 \
-    (b->tb == 2 ? (check ? rb2d_batch_kernel<M, true, 2><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)  \
-                         : rb2d_batch_kernel<M, false, 2><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)) \
-                : (check ? rb2d_batch_kernel<M, true, 1><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)  \
-                         : rb2d_batch_kernel<M, false, 1><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->cfg.chunk2d)))
+#define RBK(M, C, T) rb2d_batch_kernel<M, C, T><<<b->nwork, blk, 0, b->s>>>(t, b->work, b->active, b->nactive, b->cfg.chunk2d)
+#define RBB(M) (b->tb == 2 ? (check ? RBK(M, true, 2) : RBK(M, false, 2)) : (check ? RBK(M, true, 1) : RBK(M, false, 1)))
     if (b->model == LIN) RBB(LIN);
     else if (b->model == LINSTEP) RBB(LINSTEP);
     else RBB(NONLIN);
 #undef RBB
+#undef RBK
+    return cudaGetLastError();
+}
+
+// The list of the running instances' work items (after every judge).
+cudaError_t compact_rb(ptd_batch* b)
+{
+    compact_active_kernel<<<1, 256, 0, b->s>>>(b->rdev, b->wfirst, b->wcount, b->ninst, b->active, b->nactive);
     return cudaGetLastError();
 }
 
@@ -607,6 +656,23 @@ int upload_work(ptd_batch* b)
     if (rc) return rc;
     BCK(cudaMemcpy(b->work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice));
     b->nwork = (int)work.size();
+    if (b->rb) {
+        std::vector<int> first(b->ninst, 0), count(b->ninst, 0);
+        for (int k = (int)work.size() - 1; k >= 0; --k) {
+            first[work[k].x] = k;
+            count[work[k].x] += 1;
+        }
+        if (b->active) cudaFree(b->active);
+        b->active = nullptr;
+        rc = balloc(&b->active, work.size() * sizeof(int));
+        if (!rc && !b->wfirst) rc = balloc(&b->wfirst, b->ninst * sizeof(int));
+        if (!rc && !b->wcount) rc = balloc(&b->wcount, b->ninst * sizeof(int));
+        if (!rc && !b->nactive) rc = balloc(&b->nactive, sizeof(int));
+        if (rc) return rc;
+        BCK(cudaMemcpy(b->wfirst, first.data(), b->ninst * sizeof(int), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(b->wcount, count.data(), b->ninst * sizeof(int), cudaMemcpyHostToDevice));
+        BCK(cudaMemset(b->nactive, 0, sizeof(int)));
+    }
     return PTD_OK;
 }
 
@@ -650,6 +716,10 @@ int capture_rb(ptd_batch* b)
             err = cudaGetLastError();
             ++nk;
         }
+        if (err == cudaSuccess) {
+            err = compact_rb(b);
+            ++nk;
+        }
     }
     if (err == cudaSuccess) {
         rb_fold_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->ftab, b->rdev, b->fwork, b->tb);
@@ -664,7 +734,8 @@ int capture_rb(ptd_batch* b)
                                                         b->bp.norm == PTD_NORM_MAX, loop, 1, b->passes);
         err = cudaGetLastError();
     }
-    nk += 3;
+    if (err == cudaSuccess) err = compact_rb(b);
+    nk += 4;
     cudaError_t e2 = cudaStreamEndCapture(b->s, &body);
     if (err != cudaSuccess || e2 != cudaSuccess) {
         cudaGraphDestroy(g);
@@ -955,7 +1026,8 @@ void free_batch(ptd_batch* b)
         if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
     if (b->gstep) cudaGraphExecDestroy(b->gstep);
     void* rbp[] = {b->wb64[0], b->wb64[1], b->tb32[0], b->tb32[1], b->Rb32, b->Cb64, b->rdev,
-                   b->rbtab[0], b->rbtab[1], b->ftab, b->btab, b->passes};
+                   b->rbtab[0], b->rbtab[1], b->ftab, b->btab, b->passes, b->wfirst, b->wcount,
+                   b->active, b->nactive};
     for (void* p : rbp) cudaFree(p);
     if (b->h_rdev) cudaFreeHost(b->h_rdev);
     if (b->h_passes) cudaFreeHost(b->h_passes);
@@ -1328,8 +1400,9 @@ static int batch_rb_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
     rb_base_judge_batch_kernel<<<1, 256, 0, b->s>>>(b->rdev, n, b->bp.tol, b->norm_den, b->bp.norm == PTD_NORM_MAX,
                                                     cudaGraphConditionalHandle{}, 0, b->passes);
     BCK(cudaGetLastError());
+    BCK(compact_rb(b));
     BCK(cudaMemsetAsync(b->passes, 0, sizeof(int), b->s));
-    b->launches += 3;
+    b->launches += 4;
     if (b->nchk <= b->bp.itmax) BCK(cudaGraphLaunch(b->gstep, b->s));
     BCK(cudaMemcpyAsync(b->h_passes, b->passes, sizeof(int), cudaMemcpyDeviceToHost, b->s));
     int rc = batch_read_states(b);
@@ -1464,6 +1537,7 @@ extern "C" int ptd_batch_tune(ptd_batch* b, int32_t* warps_out, int32_t* chunk_o
                 b->cfg.chunk2d = C;
                 int rc = upload_work(b);
                 if (rc) return rc;
+                if (b->rb) BCK(compact_rb(b));   // every instance running
                 const int nl = 12 / tbc;   // 12 inner iterations either way
                 for (int rep = 0; rep < 2; ++rep) {
                     BCK(cudaEventRecord(e0, b->s));

@@ -701,14 +701,15 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
 // faces; after the level-2 faces); the march starts two planes below the
 // chunk (one at the bottom boundary) so that level 1 is in place where level
 // 2 needs it.  Each iteration's arithmetic is rb3d_body's, operation for
-// operation (the x and y faces of a level as one FP32x2 evaluation, which
-// rounds every component like the scalar face), so a launch gives the
-// iterates of two one-iteration launches.  Rows only do the work whose
-// results are used (row = warp, so the tests are uniform): level-1 updates
-// and x/z faces on rows 1..R-2, level-1 y faces on rows 0..R-2, level-2
-// updates and x/z faces on rows 2..R-3, level-2 y faces on rows 1..R-3.
-// A launch reads and writes each field once for two iterations: 26 bytes
-// per cell-iteration instead of 52.
+// operation, so a launch gives the iterates of two one-iteration launches.
+// A launch reads and writes each field once for two iterations: 26 bytes per
+// cell-iteration instead of 52.  Every row and lane evaluates both levels
+// (the halo rows' results are discarded): measured at 512^3, 1225 us per
+// iteration against 1244 us one iteration per launch -- the 28 x 12 of 32 x 16
+// cells that a tile updates at level 2 make the launch issue-bound, which
+// takes back almost all of the halved bytes.  (Skipping the halo rows' unused
+// work per warp, with the x and y faces of a level as one FP32x2 evaluation,
+// was slower: 1365 us.)
 template <int MODEL, bool CHECK, int R>
 __device__ __forceinline__ void rb3d_tb2_body(const RbArgs& a, int bx, int by, int bz, int chunk, double& part,
                                               unsigned long long& pmax)
@@ -728,27 +729,21 @@ __device__ __forceinline__ void rb3d_tb2_body(const RbArgs& a, int bx, int by, i
     if (k0 >= k1) return;   // uniform over the block
     const int ic = min(max(i, 0), nx - 1), jc = min(max(j, 0), ny - 1);
     const bool colin = i >= 1 && i <= nx - 2, rowin = j >= 1 && j <= ny - 2;
-    // the rows' work (uniform over each warp)
-    const bool r1u = r >= 1 && r <= R - 2;    // level-1 update, x and z faces
-    const bool r1y = r <= R - 2;              // level-1 y face
-    const bool r2u = r >= 2 && r <= R - 3;    // level-2 update, x and z faces
-    const bool r2y = r >= 1 && r <= R - 3;    // level-2 y face
-    const bool upd1 = colin && rowin && lane >= 1 && lane <= 30 && r1u;
-    const bool upd2 = colin && rowin && lane >= 2 && lane <= 29 && r2u;
+    const bool upd1 = colin && rowin && lane >= 1 && lane <= 30 && r >= 1 && r <= R - 2;
+    const bool lv2 = lane >= 2 && lane <= 29 && r >= 2 && r <= R - 3;   // level-2 cell of the tile
+    const bool upd2 = lv2 && colin && rowin;
     // level-2 faces stored: x faces of lanes 1..28 (lane 29's face is the next
     // tile's lane-1 face) and the grid's last face; y faces of rows 1..R-4
     // likewise; z faces of the level-2 cells
-    const bool xf2 = i >= 0 && i <= nx - 2 && lane >= 1 && lane <= 29 && r2u && rowin;
+    const bool xf2 = i >= 0 && i <= nx - 2 && lane >= 1 && lane <= 29 && r >= 2 && r <= R - 3 && rowin;
     const bool own_x = xf2 && (lane <= 28 || i == nx - 2);
-    const bool yf2 = j >= 0 && j <= ny - 2 && r2y && lane >= 2 && lane <= 29 && colin;
+    const bool yf2 = j >= 0 && j <= ny - 2 && r >= 1 && r <= R - 3 && lane >= 2 && lane <= 29 && colin;
     const bool own_y = yf2 && (r <= R - 4 || j == ny - 2);
-    constexpr bool PACKF = true;   // LIN, NONLIN: x and y faces as one FP32x2 evaluation
     const long long sz = a.sz;
     const long long col = (long long)jc * a.sy + ic;
     const float s0 = a.sig[0], s1 = a.sig[1], s2 = a.sig[2], rdt = a.rdt;
     const bool up = r < R - 1;
     float u;
-    float2 u2;
 
     // ---- start state: planes ks and ks+1 (ks = k0-2, or 0 at the bottom)
     const int ks = k0 >= 2 ? k0 - 2 : 0;
@@ -757,8 +752,7 @@ __device__ __forceinline__ void rb3d_tb2_body(const RbArgs& a, int bx, int by, i
     float h0 = a.Hf[o0];
     float d1 = a.din[o0 + sz], h1 = a.Hf[o0 + sz];
     float tbz0 = a.tb[2][o0];
-    float wz1b = 0.0f;                    // level-1 z face below the level-1 plane
-    if (r1u) wz1b = rb_face<MODEL, false>(a, p0, d1, h0, h1, 0.0f, 0.0f, a.win[2][o0], tbz0, u);   // ks+1/2
+    float wz1b = rb_face<MODEL, false>(a, p0, d1, h0, h1, 0.0f, 0.0f, a.win[2][o0], tbz0, u);   // level 1, ks+1/2
     float wx1p = 0.0f, wy1p = 0.0f, tbx0 = 0.0f, tby0 = 0.0f, rb0 = 0.0f, hu0 = h0;
     float wz2b = 0.0f, uz2b = 0.0f;
     sdi[(ks + 1) & 1][r][lane] = d1;
@@ -770,8 +764,6 @@ __device__ __forceinline__ void rb3d_tb2_body(const RbArgs& a, int bx, int by, i
         const bool l1 = kn <= nz - 2;         // interior: updated at level 1, plane kn+1 exists
         const long long on = o0 + sz;
         // ---- A: inputs of plane kn, level-1 faces there
-        // every row issues the plane's loads first (the halo rows' extra reads
-        // hit L2), so that they are in flight together
         float d2 = d1, h2 = h1;
         if (l1) {
             d2 = a.din[on + sz];
@@ -779,93 +771,59 @@ __device__ __forceinline__ void rb3d_tb2_body(const RbArgs& a, int bx, int by, i
         }
         const float wx = a.win[0][on], wy = a.win[1][on], wz = a.win[2][on];
         const float tbx1 = a.tb[0][on], tby1 = a.tb[1][on], tbz1 = a.tb[2][on], rb1 = a.Rb[on];
-        float wx1 = 0.0f, wy1 = 0.0f, wz1 = 0.0f, hu = h1;
-        if (r1y) {
-            const float du = sdi[kn & 1][r + 1][lane];
-            hu = shi[kn & 1][r + 1][lane];
-            const float d1r = __shfl_down_sync(FULL, d1, 1);
-            const float h1r = __shfl_down_sync(FULL, h1, 1);
-            if (r1u) {
-                if (PACKF) {
-                    const float2 w1 = rb_face2<MODEL, false>(a, f2(d1), f2(d1r, du), f2(h1), f2(h1r, hu), f2(0.0f),
-                                                             f2(0.0f), f2(wx, wy), f2(tbx1, tby1), u2);
-                    wx1 = w1.x;
-                    wy1 = w1.y;
-                } else {
-                    wx1 = rb_face<MODEL, false>(a, d1, d1r, h1, h1r, 0.0f, 0.0f, wx, tbx1, u);
-                    wy1 = rb_face<MODEL, false>(a, d1, du, h1, hu, 0.0f, 0.0f, wy, tby1, u);
-                }
-                wz1 = rb_face<MODEL, false>(a, d1, d2, h1, h2, 0.0f, 0.0f, wz, tbz1, u);   // kn+1/2
-            } else {
-                wy1 = rb_face<MODEL, false>(a, d1, du, h1, hu, 0.0f, 0.0f, wy, tby1, u);
-            }
-            sy1[r][lane] = wy1;
-        }
+        const float du = up ? sdi[kn & 1][r + 1][lane] : d1;
+        const float hu = up ? shi[kn & 1][r + 1][lane] : h1;
+        const float d1r = __shfl_down_sync(FULL, d1, 1);
+        const float h1r = __shfl_down_sync(FULL, h1, 1);
+        const float wx1 = rb_face<MODEL, false>(a, d1, d1r, h1, h1r, 0.0f, 0.0f, wx, tbx1, u);
+        const float wy1 = rb_face<MODEL, false>(a, d1, du, h1, hu, 0.0f, 0.0f, wy, tby1, u);
+        const float wz1 = rb_face<MODEL, false>(a, d1, d2, h1, h2, 0.0f, 0.0f, wz, tbz1, u);   // kn+1/2
+        sy1[r][lane] = wy1;
         sdi[(kn + 1) & 1][r][lane] = d2;
         shi[(kn + 1) & 1][r][lane] = h2;
         __syncthreads();
         // ---- B: level-1 update of plane kn; level-2 faces of plane k
+        const float wy1b = r >= 1 ? sy1[r - 1][lane] : 0.0f;
+        const float wx1l = __shfl_up_sync(FULL, wx1, 1);
         float p1 = d1;
-        if (r1u) {
-            const float wy1b = sy1[r - 1][lane];
-            const float wx1l = __shfl_up_sync(FULL, wx1, 1);
-            if (l1 && upd1) {
-                const float e = rb_cell_e<MODEL>(a, h1 + d1, 0.0f);
-                const float div = fmaf(wz1 - wz1b, s2, fmaf(wy1 - wy1b, s1, (wx1 - wx1l) * s0));
-                p1 = fmaf(-e, fmaf(d1, rdt, rb1 + div), d1);
-            }
-            sd1[kn & 1][r][lane] = p1;
+        if (l1 && upd1) {
+            const float e = rb_cell_e<MODEL>(a, h1 + d1, 0.0f);
+            const float div = fmaf(wz1 - wz1b, s2, fmaf(wy1 - wy1b, s1, (wx1 - wx1l) * s0));
+            p1 = fmaf(-e, fmaf(d1, rdt, rb1 + div), d1);
         }
-        float wx2 = 0.0f, wy2 = 0.0f, wz2 = 0.0f, ux2 = 0.0f, uy2 = 0.0f, uz2 = 0.0f;
-        if (r2y) {
-            const float p0u = sd1[k & 1][r + 1][lane];
-            const float p0r = __shfl_down_sync(FULL, p0, 1);
-            const float h0r = __shfl_down_sync(FULL, h0, 1);
-            if (r2u) {
-                if (PACKF) {
-                    float2 uu = f2(0.0f);
-                    const float2 w2 = rb_face2<MODEL, CHECK>(a, f2(p0), f2(p0r, p0u), f2(h0), f2(h0r, hu0), f2(0.0f),
-                                                             f2(0.0f), f2(wx1p, wy1p), f2(tbx0, tby0), uu);
-                    wx2 = w2.x;
-                    wy2 = w2.y;
-                    ux2 = uu.x;
-                    uy2 = uu.y;
-                } else {
-                    wx2 = rb_face<MODEL, CHECK>(a, p0, p0r, h0, h0r, 0.0f, 0.0f, wx1p, tbx0, ux2);
-                    wy2 = rb_face<MODEL, CHECK>(a, p0, p0u, h0, hu0, 0.0f, 0.0f, wy1p, tby0, uy2);
-                }
-                wz2 = rb_face<MODEL, CHECK>(a, p0, p1, h0, h1, 0.0f, 0.0f, wz1b, tbz0, uz2);   // k+1/2
-            } else {
-                wy2 = rb_face<MODEL, CHECK>(a, p0, p0u, h0, hu0, 0.0f, 0.0f, wy1p, tby0, uy2);
-            }
-            sy2[r][lane] = wy2;
-            if (CHECK) su2[r][lane] = uy2;
-        }
+        sd1[kn & 1][r][lane] = p1;
+        const float p0r = __shfl_down_sync(FULL, p0, 1);
+        const float h0r = __shfl_down_sync(FULL, h0, 1);
+        const float p0u = up ? sd1[k & 1][r + 1][lane] : p0;
+        float ux2 = 0.0f, uy2 = 0.0f, uz2 = 0.0f;
+        const float wx2 = rb_face<MODEL, CHECK>(a, p0, p0r, h0, h0r, 0.0f, 0.0f, wx1p, tbx0, ux2);
+        const float wy2 = rb_face<MODEL, CHECK>(a, p0, p0u, h0, hu0, 0.0f, 0.0f, wy1p, tby0, uy2);
+        const float wz2 = rb_face<MODEL, CHECK>(a, p0, p1, h0, h1, 0.0f, 0.0f, wz1b, tbz0, uz2);   // k+1/2
+        sy2[r][lane] = wy2;
+        if (CHECK) su2[r][lane] = uy2;
         __syncthreads();
         // ---- C: level-2 update of plane k
-        if (r2u) {
-            const float wx2l = __shfl_up_sync(FULL, wx2, 1);
-            const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
-            if (k >= k0) {   // uniform over the block
-                const float wy2b = sy2[r - 1][lane];
-                if (upd2) {
-                    const float e = rb_cell_e<MODEL>(a, h0 + p0, 0.0f);
-                    const float div = fmaf(wz2 - wz2b, s2, fmaf(wy2 - wy2b, s1, (wx2 - wx2l) * s0));
-                    const float q = fmaf(-e, fmaf(p0, rdt, rb0 + div), p0);
-                    a.dout[o0] = q;
-                    a.wout[2][o0] = wz2;
-                    if (CHECK) {
-                        const float uy2b = su2[r - 1][lane];
-                        const float divu = fmaf(uz2 - uz2b, s2, fmaf(uy2 - uy2b, s1, (ux2 - ux2l) * s0));
-                        accumulate_residual(a.Cb[o0] + (double)divu - (double)q * (double)rdt, part, pmax);
-                    }
+        const float wx2l = __shfl_up_sync(FULL, wx2, 1);
+        const float ux2l = CHECK ? __shfl_up_sync(FULL, ux2, 1) : 0.0f;
+        if (k >= k0) {   // uniform over the block
+            const float wy2b = r >= 1 ? sy2[r - 1][lane] : 0.0f;
+            if (upd2) {
+                const float e = rb_cell_e<MODEL>(a, h0 + p0, 0.0f);
+                const float div = fmaf(wz2 - wz2b, s2, fmaf(wy2 - wy2b, s1, (wx2 - wx2l) * s0));
+                const float q = fmaf(-e, fmaf(p0, rdt, rb0 + div), p0);
+                a.dout[o0] = q;
+                a.wout[2][o0] = wz2;
+                if (CHECK) {
+                    const float uy2b = su2[r - 1][lane];
+                    const float divu = fmaf(uz2 - uz2b, s2, fmaf(uy2 - uy2b, s1, (ux2 - ux2l) * s0));
+                    accumulate_residual(a.Cb[o0] + (double)divu - (double)q * (double)rdt, part, pmax);
                 }
-                if (own_x) a.wout[0][o0] = wx2;
-            } else if (k == 0 && upd2) {
-                a.wout[2][o0] = wz2;   // the bottom boundary's face 1/2, owned by the first chunk
             }
+            if (own_x) a.wout[0][o0] = wx2;
+            if (own_y) a.wout[1][o0] = wy2;
+        } else if (k == 0 && upd2) {
+            a.wout[2][o0] = wz2;   // the bottom boundary's face 1/2, owned by the first chunk
         }
-        if (k >= k0 && own_y) a.wout[1][o0] = wy2;
         // ---- shift the planes
         p0 = p1;
         h0 = h1;

@@ -111,20 +111,23 @@ class BatchSolver:
         return w.value, c.value, t.value
 
     def solve(self, Hs, Ds=None):
-        """Solve in place on the list of Fortran-ordered arrays Hs.  Returns
-        (iters[ninst, nt], err_last[ninst])."""
+        """Solve in place on the list of fields Hs: Fortran-ordered host arrays,
+        or contiguous float64 tensors (host or device; x fastest, i.e. the
+        transpose of a C-ordered (ny, nx) tensor).  Returns (iters[ninst, nt],
+        err_last[ninst])."""
         n = self.params.ninst
         cells = [int(a) * int(b) for a, b in zip(self.nx, self.ny)]
         if len(Hs) != n or (Ds is not None and len(Ds) != n):
             raise ValueError(f"expected {n} H arrays{' and D arrays' if Ds is not None else ''}")
         for i, H in enumerate(Hs):
             _abi.check_field(H, cells[i], f"H[{i}]", out=True)
-        hp = (C.c_void_p * n)(*[H.ctypes.data for H in Hs])
+        addr = lambda a: a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        hp = (C.c_void_p * n)(*[addr(H) for H in Hs])
         dp = None
         if Ds is not None:
-            Ds = [_abi.check_field(np.asfortranarray(D, dtype=np.float64), cells[i], f"D[{i}]")
-                  for i, D in enumerate(Ds)]
-            dp = (C.c_void_p * n)(*[D.ctypes.data for D in Ds])
+            Ds = [_abi.check_field(D if hasattr(D, "data_ptr") else np.asfortranarray(D, dtype=np.float64),
+                                   cells[i], f"D[{i}]") for i, D in enumerate(Ds)]
+            dp = (C.c_void_p * n)(*[addr(D) for D in Ds])
         iters = np.zeros(n * max(self.params.nt, 1), dtype=np.int32)
         err = np.zeros(n, dtype=np.float64)
         nd = C.c_int32(0)

@@ -130,3 +130,21 @@ def test_batch_rebased_matches_one_grid_solver(model, flags):
         assert list(iters[k]) == list(it1), (k, list(iters[k]), list(it1))
         assert rel_l2(H[k], H1) <= 1e-12
         assert err[k] <= 1e-8
+
+
+def test_batch_device_tensors_match_host_arrays():
+    """H and D handed over as device tensors (the fields stay on the GPU) give
+    the host arrays' result."""
+    import torch
+
+    sizes, Hs, Ds = ptdiff.batch_instances(4, seed=8, nmin=20, nmax=70)
+    p = ptdiff.batch_params(len(sizes), model=S.LINSTEP, precision="fp32_rb", nt=1)
+    Hh = [h.copy(order="F") for h in Hs]
+    Hd = [torch.from_numpy(np.ravel(h, order="F").copy()).cuda() for h in Hs]
+    Dd = [torch.from_numpy(np.ravel(d, order="F").copy()).cuda() for d in Ds]
+    with ptdiff.BatchSolver(p, sizes, sizes) as b:
+        it_h, _ = b.solve(Hh, Ds)
+        it_d, _ = b.solve(Hd, Dd)
+    assert np.array_equal(it_h, it_d)
+    for k in range(len(sizes)):
+        assert np.array_equal(np.ravel(Hh[k], order="F"), Hd[k].cpu().numpy())
