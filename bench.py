@@ -68,7 +68,7 @@ DTYPES = {"fp64": "f64", "df64": "df64 (f32x2)", "dfh": "f64 state, df64 (f32x2)
 # ncu summaries holding the DRAM traffic per launch of a form's dominant kernel
 TRAFFIC = {("3d_nonlin_512", "fp64"): "pt_kernel_3d_nonlin_512.md",
            ("2d_nonlin_4096", "fp64"): "pt_kernel_2d_nonlin_4096.md",
-           ("2d_nonlin_4096", "fp32_rb"): "rb2d_fp32rb_nonlin_4096.md"}
+           ("2d_nonlin_4096", "fp32_rb"): "rb2d_tb2_pair_nonlin_4096.md"}
 
 
 def log(*a):
@@ -363,8 +363,8 @@ class GridBench:
             # one FP32 iteration reads delta, H_b (FP32), the fluxes omega_d, the
             # base flux defects t_b,d and R_b, writes delta and omega_d: (2+3nd+2)*4 B
             # per cell; a launch runs two iterations (temporal blocking) with an even
-            # check cadence in 2D, and in 3D for the LIN and NONLIN models
-            tb_ok = nd == 2 or (nd == 3 and self.s.model in (0, 2))
+            # check cadence in 2D
+            tb_ok = nd == 2   # 3D: one iteration per launch unless PTD_FLAG_RB_TBLOCK_3D
             ipl = 2 if tb_ok and self.s.nout % 2 == 0 else 1
             nbytes = (2 + 3 * nd + 2) * 4 * self.cells
             kname = {1: "rb1d_kernel", 2: "rb2d_kernel", 3: "rb3d_kernel"}[nd]

@@ -108,6 +108,10 @@ enum { PTD_NORM_RMS = 0, PTD_NORM_MAX = 1 };
                                  x rows per y march; 3D: z-march length x warps per CTA) and keeps the fastest */
 #define PTD_FLAG_DC_NO_TBLOCK 0x4 /* FP32_DC and FP32_RB in 2D: one FP32 iteration per launch (default: two
                                      per launch, temporally blocked, when the check cadence is even) */
+#define PTD_FLAG_RB_TBLOCK_3D 0x8 /* FP32_RB in 3D (LIN, NONLIN): two FP32 iterations per launch (z temporal
+                                     blocking, even check cadence; same iterates).  Off by default: at 512^3 it
+                                     moves half the bytes of the one-iteration kernel but is issue-bound at
+                                     about the same time per iteration */
 
 typedef struct ptd_params {
     int32_t ndim;        /* 1, 2, 3 */

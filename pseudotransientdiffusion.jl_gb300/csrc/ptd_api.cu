@@ -153,7 +153,7 @@ int ptd::validate(const ptd_params* p)
     if (p->resid_mode != PTD_RESID_MIXED && p->resid_mode != PTD_RESID_CONSISTENT)
         return fail(PTD_EINVAL, "unknown resid_mode %d", p->resid_mode);
     if (p->norm != PTD_NORM_RMS && p->norm != PTD_NORM_MAX) return fail(PTD_EINVAL, "unknown norm %d", p->norm);
-    if (p->flags & ~(PTD_FLAG_STRICT | PTD_FLAG_AUTOTUNE | PTD_FLAG_DC_NO_TBLOCK))
+    if (p->flags & ~(PTD_FLAG_STRICT | PTD_FLAG_AUTOTUNE | PTD_FLAG_DC_NO_TBLOCK | PTD_FLAG_RB_TBLOCK_3D))
         return fail(PTD_EINVAL, "unknown flags 0x%x", p->flags);
     for (int k = 0; k < 8; ++k)
         if (p->reserved[k]) return fail(PTD_EINVAL, "reserved fields must be zero");

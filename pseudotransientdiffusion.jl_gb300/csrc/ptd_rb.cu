@@ -406,9 +406,11 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     rb->cfg = tuned_config(p);
     // a phase: the check blocks of ~200 PT iterations between two FP64 rebases
     rb->blocks_per_phase = std::max(1, (200 + p.nchk - 1) / p.nchk);
-    // two iterations per launch: 2D (every model) and 3D (LIN, NONLIN), with
-    // an even check cadence
-    const bool tb3 = p.ndim == 3 && (p.model == PTD_MODEL_LIN || p.model == PTD_MODEL_NONLIN);
+    // two iterations per launch with an even check cadence: 2D (every model),
+    // and 3D (LIN, NONLIN) when asked for (PTD_FLAG_RB_TBLOCK_3D: at 512^3
+    // 1233 against 1243 us per iteration, issue-bound at half the bytes)
+    const bool tb3 = p.ndim == 3 && (p.model == PTD_MODEL_LIN || p.model == PTD_MODEL_NONLIN) &&
+                     (p.flags & PTD_FLAG_RB_TBLOCK_3D);
     rb->tblk = ((p.ndim == 2 || tb3) && p.nchk % 2 == 0 && !(p.flags & PTD_FLAG_DC_NO_TBLOCK)) ? 2 : 1;
     if (rb->tblk == 2 && p.ndim == 3)   // 28 x 12 level-2 cells per CTA, 2 CTAs per SM
         rb->cfg.chunk3d = z_chunk((long long)((p.nx - 2 + 27) / 28) * ((p.ny - 2 + 11) / 12), p.nz, 2LL * sm_count());

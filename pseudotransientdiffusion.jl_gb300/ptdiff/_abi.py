@@ -23,6 +23,7 @@ NORM_RMS, NORM_MAX = 0, 1
 FLAG_STRICT = 0x1
 FLAG_AUTOTUNE = 0x2
 FLAG_DC_NO_TBLOCK = 0x4
+FLAG_RB_TBLOCK_3D = 0x8
 
 
 class PtdParams(C.Structure):

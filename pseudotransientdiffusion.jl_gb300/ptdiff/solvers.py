@@ -28,9 +28,11 @@ PRECISIONS = {"fp64": _abi.PREC_FP64, "fp32_dc": _abi.PREC_FP32_DC, "df64": _abi
 
 def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=None,
                 precision="fp64", resid="mixed", norm="rms", norm_len=0.0, strict=False,
-                autotune=False, dc_max_outer=0, dc_inner_rtol=0.0, dc_tblock=True) -> _abi.PtdParams:
+                autotune=False, dc_max_outer=0, dc_inner_rtol=0.0, dc_tblock=True,
+                rb_tblock_3d=False) -> _abi.PtdParams:
     """ptd_params for a script at a grid shape (x fastest).  dc_tblock=False:
-    one FP32 iteration per launch in 2D (FP32_DC, FP32_RB) instead of two."""
+    one FP32 iteration per launch in 2D (FP32_DC, FP32_RB) instead of two;
+    rb_tblock_3d=True: two FP32_RB iterations per launch in 3D."""
     p = _abi.PtdParams()
     _abi.check(_abi.lib().ptd_params_init(C.byref(p), script.ndim, script.model), "ptd_params_init")
     p.nx = shape[0]
@@ -50,7 +52,7 @@ def make_params(script: Script, shape, *, nt=None, itmax=None, nchk=None, tol=No
     p.norm = {"rms": _abi.NORM_RMS, "max": _abi.NORM_MAX}[norm]
     p.norm_len = norm_len
     p.flags = ((_abi.FLAG_STRICT if strict else 0) | (_abi.FLAG_AUTOTUNE if autotune else 0)
-               | (0 if dc_tblock else _abi.FLAG_DC_NO_TBLOCK))
+               | (0 if dc_tblock else _abi.FLAG_DC_NO_TBLOCK) | (_abi.FLAG_RB_TBLOCK_3D if rb_tblock_3d else 0))
     p.dc_max_outer = dc_max_outer
     p.dc_inner_rtol = dc_inner_rtol
     return p

@@ -168,7 +168,7 @@ def test_rebased_fp32_temporal_blocking_matches_one_iteration_per_launch(name, s
     assert rel_l2(H2, H1) <= 1e-12
 
 
-# 3D LIN and NONLIN likewise (z temporal blocking, rb3d_tb2_kernel): grids
+# 3D LIN and NONLIN likewise with PTD_FLAG_RB_TBLOCK_3D (z temporal blocking, rb3d_tb2_kernel): grids
 # of one z chunk and of several (the march of each chunk starts two planes
 # below it), ragged x/y tiles, odd check cadences (one iteration per
 # launch), itmax not a multiple of nchk, the fixed-iteration protocol.
@@ -180,8 +180,8 @@ def test_rebased_fp32_temporal_blocking_matches_one_iteration_per_launch(name, s
     ("diff_3D_nonlin_perf", (32, 32, 32), {"itmax": 33}), ("diff_3D_lin_multixpu", (60, 4, 100), {})])
 def test_rebased_fp32_3d_temporal_blocking_matches_one_iteration_per_launch(name, shape, kw):
     s = S.SCRIPTS[name]
-    H2, _, it2, _, st2 = run(s, shape, **kw)
-    H1, _, it1, _, st1 = run(s, shape, dc_tblock=False, **kw)
+    H2, _, it2, _, st2 = run(s, shape, rb_tblock_3d=True, **kw)
+    H1, _, it1, _, st1 = run(s, shape, **kw)
     assert st1 == 0 and st2 == 0
     assert list(it1) == list(it2)
     assert rel_l2(H2, H1) <= 1e-12
@@ -194,7 +194,7 @@ def test_rebased_fp32_3d_temporal_blocking_fixed_iterations():
     shape = (48, 40, 52)
     out = []
     for tblock in (True, False):
-        with ptdiff.Solver(ptdiff.make_params(s, shape, precision="fp32_rb", dc_tblock=tblock)) as sol:
+        with ptdiff.Solver(ptdiff.make_params(s, shape, precision="fp32_rb", rb_tblock_3d=tblock)) as sol:
             H = S.initial_condition(s, *shape)
             sol.set_state(H)
             sol.iterate(37)
