@@ -471,6 +471,45 @@ __global__ void __launch_bounds__(256) rb_base_batch_kernel(const RbBaseArgs* __
 }
 
 // ---------------------------------------------------------------------------
+// Host <-> device transfers go through a contiguous packed copy of all
+// instances' fields (one plain copy per instance at the link's rate instead
+// of a pitched copy of nx-element rows); these kernels convert between the
+// packed layout and the padded one.  pwork: {instance, first packed element,
+// count}.
+struct PackInst {
+    long long poff;   // offset of the instance in the packed buffer
+    long long off;    // offset of the instance in the padded fields
+    long long sy;     // its row pitch
+    int nx, pad;
+};
+
+__global__ void __launch_bounds__(256) unpack_batch_kernel(const double* __restrict__ packed, double* __restrict__ dst,
+                                                           const PackInst* __restrict__ pi,
+                                                           const int4* __restrict__ pwork)
+{
+    const int4 w = pwork[blockIdx.x];
+    const PackInst I = pi[w.x];
+    for (int k = threadIdx.x; k < w.z; k += blockDim.x) {
+        const long long e = (long long)w.y + k;
+        const long long r = e / I.nx;
+        dst[I.off + r * I.sy + (e - r * I.nx)] = packed[I.poff + e];
+    }
+}
+
+__global__ void __launch_bounds__(256) pack_batch_kernel(const double* __restrict__ src, double* __restrict__ packed,
+                                                         const PackInst* __restrict__ pi,
+                                                         const int4* __restrict__ pwork)
+{
+    const int4 w = pwork[blockIdx.x];
+    const PackInst I = pi[w.x];
+    for (int k = threadIdx.x; k < w.z; k += blockDim.x) {
+        const long long e = (long long)w.y + k;
+        const long long r = e / I.nx;
+        packed[I.poff + e] = src[I.off + r * I.sy + (e - r * I.nx)];
+    }
+}
+
+// ---------------------------------------------------------------------------
 #define BCK(call)                                                 \
     do {                                                          \
         cudaError_t _e = (call);                                  \
@@ -545,6 +584,11 @@ struct ptd_batch {
     int* wcount = nullptr;
     int* active = nullptr;     // work items of the running instances, and their count
     int* nactive = nullptr;
+    // packed host <-> device transfers
+    double* packed = nullptr;
+    PackInst* pinst = nullptr;
+    int4* pwork = nullptr;
+    int npwork = 0;
     cudaGraphExec_t gstep = nullptr;
     int blocks_per_phase = 1;
     // common
@@ -1027,7 +1071,7 @@ void free_batch(ptd_batch* b)
     if (b->gstep) cudaGraphExecDestroy(b->gstep);
     void* rbp[] = {b->wb64[0], b->wb64[1], b->tb32[0], b->tb32[1], b->Rb32, b->Cb64, b->rdev,
                    b->rbtab[0], b->rbtab[1], b->ftab, b->btab, b->passes, b->wfirst, b->wcount,
-                   b->active, b->nactive};
+                   b->active, b->nactive, b->packed, b->pinst, b->pwork};
     for (void* p : rbp) cudaFree(p);
     if (b->h_rdev) cudaFreeHost(b->h_rdev);
     if (b->h_passes) cudaFreeHost(b->h_passes);
@@ -1043,26 +1087,59 @@ void free_batch(ptd_batch* b)
     delete b;
 }
 
-// Upload instance fields: src[i] (nx_i*ny_i doubles, host or device) into
-// the concatenated padded field dst (FP64).
-int upload(ptd_batch* b, double* dst, const double* const* src)
+// The packed layout: instance i's nx*ny values at poff_i (x fastest, no
+// padding), and its conversion table.
+int setup_packing(ptd_batch* b)
 {
+    std::vector<PackInst> pi(b->ninst);
+    std::vector<int4> pw;
+    long long poff = 0;
+    const int CH = 4096;
     for (int i = 0; i < b->ninst; ++i) {
         const Inst& I = b->inst[i];
-        const size_t w = (size_t)I.nx * sizeof(double);
-        BCK(cudaMemcpy2DAsync(dst + I.off, (size_t)I.sy * sizeof(double), src[i], w, w, I.ny, cudaMemcpyDefault,
-                              b->s));
+        pi[i] = PackInst{poff, I.off, I.sy, I.nx, 0};
+        const long long n = (long long)I.nx * I.ny;
+        for (long long s0 = 0; s0 < n; s0 += CH)
+            pw.push_back(make_int4(i, (int)s0, (int)std::min<long long>(CH, n - s0), 0));
+        poff += n;
     }
+    int rc = balloc(&b->packed, (size_t)poff * sizeof(double));
+    if (!rc) rc = balloc(&b->pinst, pi.size() * sizeof(PackInst));
+    if (!rc) rc = balloc(&b->pwork, pw.size() * sizeof(int4));
+    if (rc) return rc;
+    BCK(cudaMemcpy(b->pinst, pi.data(), pi.size() * sizeof(PackInst), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->pwork, pw.data(), pw.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b->npwork = (int)pw.size();
+    return PTD_OK;
+}
+
+// Upload instance fields: src[i] (nx_i*ny_i doubles, host or device) into
+// the concatenated padded field dst (FP64): one contiguous copy per instance
+// into the packed buffer, then one conversion kernel.
+int upload(ptd_batch* b, double* dst, const double* const* src)
+{
+    long long poff = 0;
+    for (int i = 0; i < b->ninst; ++i) {
+        const Inst& I = b->inst[i];
+        const size_t n = (size_t)I.nx * I.ny;
+        BCK(cudaMemcpyAsync(b->packed + poff, src[i], n * sizeof(double), cudaMemcpyDefault, b->s));
+        poff += (long long)n;
+    }
+    unpack_batch_kernel<<<b->npwork, 256, 0, b->s>>>(b->packed, dst, b->pinst, b->pwork);
+    BCK(cudaGetLastError());
     return PTD_OK;
 }
 
 int download(ptd_batch* b, double* const* dst, const double* src)
 {
+    pack_batch_kernel<<<b->npwork, 256, 0, b->s>>>(src, b->packed, b->pinst, b->pwork);
+    BCK(cudaGetLastError());
+    long long poff = 0;
     for (int i = 0; i < b->ninst; ++i) {
         const Inst& I = b->inst[i];
-        const size_t w = (size_t)I.nx * sizeof(double);
-        BCK(cudaMemcpy2DAsync(dst[i], w, src + I.off, (size_t)I.sy * sizeof(double), w, I.ny, cudaMemcpyDefault,
-                              b->s));
+        const size_t n = (size_t)I.nx * I.ny;
+        BCK(cudaMemcpyAsync(dst[i], b->packed + poff, n * sizeof(double), cudaMemcpyDefault, b->s));
+        poff += (long long)n;
     }
     return PTD_OK;
 }
@@ -1237,6 +1314,7 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
             if (z && cudaMemset(z, 0, fb) != cudaSuccess) rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
     }
     if (!rc) rc = fill_tables(b);
+    if (!rc) rc = setup_packing(b);
     if (!rc) rc = upload_work(b);
     if (!rc) rc = capture(b);
     if (rc) {

@@ -11,6 +11,17 @@
 
 namespace ptd {
 
+// Slot of this warp (2D: warps numbered x fastest) / block (1D, 3D) in
+// RbArgs::parts.
+__device__ __forceinline__ long long warp_slot()
+{
+    return ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.y + threadIdx.y;
+}
+__device__ __forceinline__ long long block_slot()
+{
+    return ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+
 template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) rb1d_kernel(RbArgs a)
 {
@@ -18,7 +29,7 @@ __global__ void __launch_bounds__(256) rb1d_kernel(RbArgs a)
     double part = 0.0;
     unsigned long long pmax = 0ull;
     rb1d_body<MODEL, CHECK>(a, blockIdx.x, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax, a.parts, blockIdx.x);
 }
 
 template <int MODEL, bool CHECK>
@@ -27,8 +38,8 @@ __global__ void __launch_bounds__(256) rb2d_kernel(RbArgs a, int chunk)
     if (rb_skip(a.skip)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    // the body flushes its check partials into a.acc (last step of its march)
-    rb2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+    // the body flushes its check partials into its warp's slot (last step of its march)
+    rb2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax, warp_slot());
 }
 
 // Two iterations per launch, two columns per lane (LIN, NONLIN).
@@ -39,7 +50,8 @@ __global__ void __launch_bounds__(256) rb2d_tb2_pair_kernel(RbArgs a, int chunk)
     double part = 0.0;
     unsigned long long pmax = 0ull;
     if constexpr (MODEL == LIN || MODEL == NONLIN)
-        rb2d_tb2_pair_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+        rb2d_tb2_pair_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax,
+                                         warp_slot());
 }
 
 // The plain NONLIN variant is capped at 32 registers (8 CTAs of 256 threads
@@ -53,8 +65,8 @@ __global__ void __launch_bounds__(256, (MODEL == NONLIN && !CHECK) ? 8 : 0) rb2d
     if (rb_skip(a.skip)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    // the body flushes its check partials into a.acc (last step of its march)
-    rb2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+    // the body flushes its check partials into its warp's slot (last step of its march)
+    rb2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax, warp_slot());
 }
 
 // Two iterations per launch in 3D (LIN, NONLIN): 16-warp CTAs, 2 resident per SM.
@@ -66,7 +78,7 @@ __global__ void __launch_bounds__(512, 2) rb3d_tb2_kernel(RbArgs a, int chunk)
     unsigned long long pmax = 0ull;
     if constexpr (MODEL == LIN || MODEL == NONLIN)
         rb3d_tb2_body<MODEL, CHECK, 16>(a, blockIdx.x, blockIdx.y, blockIdx.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax, a.parts, block_slot());
 }
 
 template <int MODEL, bool CHECK>
@@ -76,7 +88,7 @@ __global__ void __launch_bounds__(512) rb3d_kernel(RbArgs a, int chunk)
     double part = 0.0;
     unsigned long long pmax = 0ull;
     rb3d_body<MODEL, CHECK, 16>(a, blockIdx.x, blockIdx.y, blockIdx.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax, a.parts, block_slot());
 }
 
 __global__ void rb_fold_kernel(RbFoldArgs f, const RbDev* st, int parity, int tb)
@@ -102,16 +114,22 @@ __global__ void __launch_bounds__(256) rb_base_kernel(RbBaseArgs b, const RbDev*
         const long long rest = t / b.nx;
         rb_base_cell(b, ix, (int)(rest % b.ny), (int)(rest / b.ny), part, pmax);
     }
-    block_reduce_residual(b.acc64, b.norm_max, part, pmax);
+    block_reduce_residual(b.acc64, b.norm_max, part, pmax, b.parts, blockIdx.x);
 }
 
 __global__ void rb_reset_kernel(RbDev* st) { rb_reset(st); }
 
 // After each block of nchk iterations: the FP32 check err (rb_check_judge).
-__global__ void rb_check_judge_kernel(RbDev* st, double* errhist, int errcap, int nchk, int itmax, double tol,
-                                      double norm_den, int norm_max)
+__global__ void __launch_bounds__(256) rb_check_judge_kernel(RbDev* st, const double* parts, long long nparts,
+                                                             double* errhist, int errcap, int nchk, int itmax,
+                                                             double tol, double norm_den, int norm_max)
 {
-    rb_check_judge(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max);
+    if (st->skip || st->step_done) return;   // no PT kernel ran: the slots are stale
+    const double acc = sum_slots(parts, nparts, norm_max);
+    if (threadIdx.x == 0) {
+        st->acc = acc;
+        rb_check_judge(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max);
+    }
 }
 
 // After each rebase: the FP64 err of the base (rb_base_judge).  In the body of
@@ -120,12 +138,27 @@ __global__ void rb_check_judge_kernel(RbDev* st, double* errhist, int errcap, in
 // of nchk iterations (its first judge runs with skip clear) and a phase that
 // leaves no room for another block before itmax ends the step (capped), so
 // the loop ends within itmax/nchk passes.
-__global__ void rb_base_judge_kernel(RbDev* st, double tol, double norm_den, int norm_max,
-                                     cudaGraphConditionalHandle loop, int in_loop)
+__global__ void __launch_bounds__(256) rb_base_judge_kernel(RbDev* st, const double* parts, long long nparts,
+                                                            double tol, double norm_den, int norm_max,
+                                                            cudaGraphConditionalHandle loop, int in_loop)
 {
-    if (in_loop) st->phases += 1;
-    const int done = rb_base_judge(st, tol, norm_den, norm_max);
-    if (in_loop && done) cudaGraphSetConditional(loop, 0);
+    // every thread reads step_done before thread 0 can change it
+    const bool stopped = st->step_done != 0;
+    __syncthreads();
+    if (stopped) {   // the base kernel did not run: the slots are stale
+        if (threadIdx.x == 0 && in_loop) {
+            st->phases += 1;
+            cudaGraphSetConditional(loop, 0);
+        }
+        return;
+    }
+    const double acc = sum_slots(parts, nparts, norm_max);
+    if (threadIdx.x == 0) {
+        if (in_loop) st->phases += 1;
+        st->acc64 = acc;
+        const int done = rb_base_judge(st, tol, norm_den, norm_max);
+        if (in_loop && done) cudaGraphSetConditional(loop, 0);
+    }
 }
 
 __global__ void rb_tofloat_kernel(const double* src, float* dst, long long n)
@@ -158,6 +191,10 @@ struct RbState {
     int* zero_flag = nullptr;
     double* errhist = nullptr;
     int errcap = 0;
+    double* parts = nullptr;                      // check-residual slots of the check launches
+    long long nparts = 0;
+    double* parts64 = nullptr;                    // FP64 residual slots of the base kernel
+    long long nparts64 = 0;
     int blocks_per_phase = 1;
     int tblk = 1;                                 // iterations per launch (2: temporal blocking, 2D)
     cudaGraphExec_t gphase = nullptr;
@@ -200,6 +237,7 @@ void rb_args(const RbState* rb, int parity, const int* skip, RbArgs& a)
     a.Df = rb->Df;
     a.skip = skip;
     a.acc = &rb->dev->acc;
+    a.parts = rb->parts;
     a.norm_max = rb->p.norm == PTD_NORM_MAX;
 }
 
@@ -276,6 +314,49 @@ cudaError_t rb_run_plain(const RbState* rb, int32_t niter, const int* skip, int&
     return cudaSuccess;
 }
 
+// The check-residual slots of the check launch (the grids of
+// rb_launch_model): warps in 2D, blocks in 1D and 3D.
+long long rb_check_slots(const RbState* rb)
+{
+    const ptd_params& p = rb->p;
+    const LaunchCfg& c = rb->cfg;
+    if (p.ndim == 1) return (p.nx + 255) / 256;
+    if (p.ndim == 2) {
+        const bool pair = rb->tblk == 2 && (p.model == PTD_MODEL_LIN || p.model == PTD_MODEL_NONLIN);
+        const long long tiles = pair ? (p.nx - 1 + 59) / 60 : (rb->tblk == 2 ? (p.nx - 2 + 27) / 28 : (p.nx - 2 + 30) / 31);
+        const int chunk = rb->tblk == 2 ? 2 * c.chunk2d : c.chunk2d;
+        const int W = c.warps2d;
+        return (tiles + W - 1) / W * W * (long long)((p.ny - 2 + chunk - 1) / chunk);
+    }
+    const long long nzc = (p.nz - 2 + c.chunk3d - 1) / c.chunk3d;
+    if (rb->tblk == 2) return (long long)((p.nx - 2 + 27) / 28) * ((p.ny - 2 + 11) / 12) * nzc;
+    return (long long)((p.nx - 2 + 30) / 31) * ((p.ny - 2 + 14) / 15) * nzc;
+}
+
+// (Re)allocate the residual slots for the current launch configuration.
+int rb_alloc_parts(RbState* rb)
+{
+    const long long n = rb_check_slots(rb);
+    if (n > rb->nparts) {
+        cudaFree(rb->parts);
+        rb->parts = nullptr;
+        rb->nparts = 0;
+        if (cudaMalloc((void**)&rb->parts, (size_t)n * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(PTD_ENOMEM, "rb: cudaMalloc failed");
+        }
+    }
+    rb->nparts = n;
+    if (!rb->parts64) {
+        rb->nparts64 = fill_blocks();
+        if (cudaMalloc((void**)&rb->parts64, (size_t)rb->nparts64 * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(PTD_ENOMEM, "rb: cudaMalloc failed");
+        }
+    }
+    return PTD_OK;
+}
+
 RbFoldArgs fold_args(const RbState* rb)
 {
     RbFoldArgs f;
@@ -317,6 +398,7 @@ RbBaseArgs base_args(const RbState* rb)
     b.Cb = rb->Cb;
     b.Hf = rb->Hf;
     b.acc64 = &rb->dev->acc64;
+    b.parts = rb->parts64;
     b.norm_max = rb->p.norm == PTD_NORM_MAX;
     return b;
 }
@@ -360,8 +442,9 @@ int rb_capture(RbState* rb)
             ++nk;
         }
         if (err == cudaSuccess) {
-            rb_check_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->errhist, rb->errcap, nchk, rb->p.itmax,
-                                                      rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX);
+            rb_check_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts, rb->nparts, rb->errhist, rb->errcap, nchk,
+                                                        rb->p.itmax, rb->p.tol, rb->dv.norm_den,
+                                                        rb->p.norm == PTD_NORM_MAX);
             err = cudaGetLastError();
             ++nk;
         }
@@ -375,8 +458,8 @@ int rb_capture(RbState* rb)
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) {
-        rb_base_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX,
-                                                 loop, 1);
+        rb_base_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts64, rb->nparts64, rb->p.tol, rb->dv.norm_den,
+                                                   rb->p.norm == PTD_NORM_MAX, loop, 1);
         err = cudaGetLastError();
     }
     nk += 3;
@@ -437,6 +520,7 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     if (!rc) rc = alloc((void**)&rb->dev, sizeof(RbDev));
     if (!rc) rc = alloc((void**)&rb->zero_flag, sizeof(int));
     if (!rc) rc = alloc((void**)&rb->errhist, (size_t)rb->errcap * sizeof(double));
+    if (!rc) rc = rb_alloc_parts(rb);
     if (!rc && cudaMallocHost((void**)&rb->h_dev, sizeof(RbDev)) != cudaSuccess) {
         cudaGetLastError();
         rc = set_error(PTD_ENOMEM, "rb: cudaMallocHost failed");
@@ -480,6 +564,8 @@ void rb_destroy(RbState* rb)
     cudaFree(rb->dev);
     cudaFree(rb->zero_flag);
     cudaFree(rb->errhist);
+    cudaFree(rb->parts);
+    cudaFree(rb->parts64);
     if (rb->h_dev) cudaFreeHost(rb->h_dev);
     delete rb;
 }
@@ -514,8 +600,8 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
     RCK(cudaGetLastError());
     rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
     RCK(cudaGetLastError());
-    rb_base_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.tol, rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX,
-                                             cudaGraphConditionalHandle{}, 0);
+    rb_base_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts64, rb->nparts64, rb->p.tol, rb->dv.norm_den,
+                                               rb->p.norm == PTD_NORM_MAX, cudaGraphConditionalHandle{}, 0);
     RCK(cudaGetLastError());
     rb->k.launches += 3;
     rb->h_dev->step_done = DONE_RUNNING;
@@ -579,6 +665,8 @@ int rb_iterate(RbState* rb, int32_t niter)
 int rb_set_config(RbState* rb, const LaunchCfg& cfg)
 {
     rb->cfg = cfg;
+    const int rc = rb_alloc_parts(rb);
+    if (rc) return rc;
     if (rb->gphase) {   // captured once the base fields are known (rb_set_state)
         cudaGraphExecDestroy(rb->gphase);
         rb->gphase = nullptr;

@@ -60,6 +60,10 @@ struct RbArgs {
     const float* Df;      // LINSTEP: D, NONLIN_EXPM: exp(m), as FP32
     const int* skip;
     double* acc;
+    // Per-warp (2D) / per-block (1D, 3D) slots of the check residual that the
+    // judge sums in a fixed order (the same residual norm on every run); NULL:
+    // the partials go into acc by atomics instead (the batched solver).
+    double* parts;
     int norm_max;
 };
 
@@ -195,7 +199,7 @@ __device__ __forceinline__ void rb1d_body(const RbArgs& a, int bx, double& part,
 // 2D: the tiling of ptd_pt_body.cuh (31 updated columns per warp, y march).
 template <int MODEL, bool CHECK>
 __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
-                                          unsigned long long& pmax)
+                                          unsigned long long& pmax, long long slot = 0)
 {
     constexpr bool LS = MODEL == LINSTEP;
     constexpr bool HASD = LS || MODEL == NONLIN_EXPM;   // a per-cell field in Df
@@ -260,8 +264,10 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
                 Db = Dc;
                 Dc = Dn;
             }
-            if (CHECK && j == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane);
+            if (CHECK && j == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
         }
+    } else if (CHECK && a.parts && lane == 0) {
+        a.parts[slot] = 0.0;   // a warp with no cells: its slot still holds this check's (empty) part
     }
 }
 
@@ -286,14 +292,17 @@ __device__ __forceinline__ float rb_star(float Dc, float Db, float Dn)
 
 template <int MODEL, bool CHECK>
 __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
-                                              unsigned long long& pmax)
+                                              unsigned long long& pmax, long long slot = 0)
 {
     constexpr bool HASD = MODEL == LINSTEP || MODEL == NONLIN_EXPM;
     const int lane = threadIdx.x;
     const int nx = a.nx, ny = a.ny;
     const int j0 = 1 + cy * chunk;
     const int j1 = min(j0 + chunk, ny - 1);
-    if (28 * tile >= nx - 2 || j0 >= j1) return;   // uniform over the warp
+    if (28 * tile >= nx - 2 || j0 >= j1) {   // uniform over the warp
+        if (CHECK && a.parts && lane == 0) a.parts[slot] = 0.0;
+        return;
+    }
     const int i = 28 * tile + lane - 1;
     const int ic = min(max(i, 0), nx - 1);          // clamped column of this lane's loads
     const bool colin = i >= 1 && i <= nx - 2;
@@ -437,7 +446,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         D0 = D1;
         D0r = D1r;
         D1 = D2;
-        if (CHECK && s == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane);
+        if (CHECK && s == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
     }
 }
 
@@ -455,14 +464,17 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
 // q = 2..61 (60 columns per warp).
 template <int MODEL, bool CHECK>
 __device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
-                                                   unsigned long long& pmax)
+                                                   unsigned long long& pmax, long long slot = 0)
 {
     static_assert(MODEL == LIN || MODEL == NONLIN, "the pair kernel serves LIN and NONLIN");
     const int lane = threadIdx.x;
     const int nx = a.nx, ny = a.ny;
     const int j0 = 1 + cy * chunk;
     const int j1 = min(j0 + chunk, ny - 1);
-    if (60 * tile > nx - 2 || j0 >= j1) return;   // uniform over the warp
+    if (60 * tile > nx - 2 || j0 >= j1) {   // uniform over the warp
+        if (CHECK && a.parts && lane == 0) a.parts[slot] = 0.0;
+        return;
+    }
     const int c0 = 60 * tile - 2 + 2 * lane;      // column of the lane's first cell
     // pairs left of the grid or past the row pitch are read at the nearest
     // pair: their values feed only faces and cells that are discarded
@@ -530,7 +542,9 @@ __device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, in
     if (j0 == 1) st2(a.wout[1], oA, wy2b, u2a, u2b);
     float2 h0 = hB;
 
-    // ---- march: level 1 of row s+1, level 2 of row s
+    // ---- march: level 1 of row s+1, level 2 of row s.  (Issuing a step's
+    // loads one step ahead, in registers, was no faster: 66.6 against 66.4 us
+    // per iteration at 4096^2, its 78 registers halving the resident warps.)
     long long o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float2 p1 = d1, wx1 = f2(0.0f), wy1 = f2(0.0f), r1 = f2(0.0f), h2 = h1, tbx1 = f2(0.0f), tby1 = f2(0.0f);
@@ -574,7 +588,7 @@ __device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, in
         h0 = h1;
         h0r = h1r;
         h1 = h2;
-        if (CHECK && s == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane);
+        if (CHECK && s == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
     }
 }
 
@@ -889,6 +903,7 @@ struct RbBaseArgs {
     double* Cb;
     float* Hf;
     double* acc64;
+    double* parts;      // per-block slots of the FP64 residual (NULL: atomics into acc64)
     int norm_max;
 };
 
@@ -992,6 +1007,37 @@ __device__ __forceinline__ int rb_base_judge(RbDev* st, double tol, double norm_
         st->skip = 0;
     }
     return st->step_done;
+}
+
+// The sum (or max) of nparts check-residual slots in a fixed order, by one
+// block of 256 threads: thread t takes slots t, t + 256, ... in order, then a
+// fixed tree over the threads.  Every thread returns the result.
+__device__ __forceinline__ double sum_slots(const double* parts, long long nparts, int norm_max)
+{
+    __shared__ double s_sum[256];
+    __shared__ unsigned long long s_max[256];
+    const int t = threadIdx.x;
+    double sum = 0.0;
+    unsigned long long mx = 0ull;
+    for (long long i = t; i < nparts; i += 256) {
+        const double v = parts[i];
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        mx = bits > mx ? bits : mx;
+        sum += v;
+    }
+    s_sum[t] = sum;
+    s_max[t] = mx;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) {
+            s_sum[t] += s_sum[t + o];
+            s_max[t] = s_max[t + o] > s_max[t] ? s_max[t + o] : s_max[t];
+        }
+        __syncthreads();
+    }
+    const double r = norm_max ? __longlong_as_double((long long)s_max[0]) : s_sum[0];
+    __syncthreads();
+    return r;
 }
 
 __device__ __forceinline__ void rb_reset(RbDev* st)

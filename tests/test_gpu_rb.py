@@ -224,3 +224,26 @@ def test_rebased_fp32_temporal_blocking_expm_and_iterate():
     assert list(ia) == list(ib)
     assert rel_l2(Ha, Hb) <= 1e-12
     assert rel_l2(Hia, Hib) <= 1e-12
+
+
+@pytest.mark.parametrize("prec,name,shape", [
+    ("fp64", "2d_nonlin_4096", (384, 384)), ("dfh", "2d_nonlin_4096", (384, 384)),
+    ("fp64", "3d_nonlin_512", (64, 64, 64)), ("df64", "3d_nonlin_512", (64, 64, 64)),
+    ("fp32_rb", "2d_nonlin_4096", (384, 384)), ("fp32_rb", "3d_nonlin_512", (64, 64, 64)),
+    ("fp32_rb", "1d_lin_512", (512,))])
+def test_check_residual_is_deterministic(prec, name, shape):
+    """The check residual is summed from per-warp / per-block slots in a fixed
+    order: two solves of the same problem give the same error history bit for
+    bit (and so the same stopping iterations)."""
+    s = S.CONFIGS[name]
+    out = []
+    for _ in range(2):
+        H = S.initial_condition(s, *shape)
+        with ptdiff.Solver(ptdiff.make_params(s, shape, nt=2, precision=prec)) as sol:
+            iters, eh, st = sol.solve(H)
+        assert st == 0
+        out.append((list(iters), np.asarray(eh).copy(), H))
+    (i1, e1, h1), (i2, e2, h2) = out
+    assert i1 == i2
+    assert np.array_equal(e1, e2)
+    assert np.array_equal(np.ravel(h1), np.ravel(h2))
