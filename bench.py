@@ -68,7 +68,8 @@ DTYPES = {"fp64": "f64", "df64": "df64 (f32x2)", "dfh": "f64 state, df64 (f32x2)
 # ncu summaries holding the DRAM traffic per launch of a form's dominant kernel
 TRAFFIC = {("3d_nonlin_512", "fp64"): "pt_kernel_3d_nonlin_512.md",
            ("2d_nonlin_4096", "fp64"): "pt_kernel_2d_nonlin_4096.md",
-           ("2d_nonlin_4096", "fp32_rb"): "rb2d_tb2_pair_nonlin_4096.md"}
+           ("2d_nonlin_4096", "fp32_rb"): "rb2d_tb2_pair_nonlin_4096.md",
+           ("3d_nonlin_512", "fp32_rb"): "rb3d_nonlin_256.md"}
 
 
 def log(*a):

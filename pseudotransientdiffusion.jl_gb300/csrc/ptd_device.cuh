@@ -153,13 +153,16 @@ __device__ __forceinline__ float nonlin_cell_e(const FParams& a, float h, float 
 
 // The face parameter c with every operation explicit (no contraction left to
 // the compiler), for the FP32 kernels whose scalar and packed two-lane forms
-// must round identically (ptd_rb.cu, ptd_dc_body.cuh): c = 1/(1 + fk2/Re_f),
-// Re_f = pi + sqrt(pi^2 + fA/D_f).
+// must round identically (ptd_rb_body.cuh, ptd_dc_body.cuh):
+// c = 1/(1 + fk2/Re_f) = Re_f/(Re_f + fk2), Re_f = pi + sqrt(pi^2 + fA/D_f),
+// in three MUFU operations (the reciprocal of Re_f saved).  D_f -> 0 gives
+// Re_f -> inf and c -> 1, taken explicitly where Re_f + fk2 overflows.
 __device__ __forceinline__ float face_c_rn(const FParams& f, float df)
 {
     const float q = __fmaf_rn(f.fA, frcp(df), f.fpi2);
     const float re = __fadd_rn(f.fpi, fsqrt(q));
-    return frcp(__fmaf_rn(f.fk2, frcp(re), 1.0f));
+    const float den = __fadd_rn(re, f.fk2);
+    return den < INFINITY ? __fmul_rn(re, frcp(den)) : 1.0f;
 }
 
 // Two lanes at once (FP32x2 instructions, sm_100 and later: two faces per
