@@ -371,9 +371,10 @@ __global__ void __launch_bounds__(256) rb2d_batch_kernel(const RbArgs* __restric
     if (rb_skip(a.skip)) return;   // its phase ended since the list was built
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    // the bodies flush their check partials into a.acc (last step of their march)
-    if (TB == 2) rb2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
-    else rb2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    // the bodies flush their check partials into the warp's slot: work item k, warp w -> k * W + w
+    const long long slot = (long long)active[blockIdx.x] * blockDim.y + threadIdx.y;
+    if (TB == 2) rb2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax, slot);
+    else rb2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax, slot);
 }
 
 // The work items of the running instances, in instance order (one block):
@@ -413,11 +414,30 @@ __global__ void rb_reset_batch_kernel(RbDev* st, int ninst)
     if (i < ninst) rb_reset(&st[i]);
 }
 
+// The sum (or max) of slots first .. first+count-1, in order (one thread).
+__device__ __forceinline__ double sum_range(const double* parts, long long first, long long count, int norm_max)
+{
+    double sum = 0.0;
+    unsigned long long mx = 0ull;
+    for (long long k = first; k < first + count; ++k) {
+        const double v = parts[k];
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        mx = bits > mx ? bits : mx;
+        sum += v;
+    }
+    return norm_max ? __longlong_as_double((long long)mx) : sum;
+}
+
+// The FP32 check of every instance, its residual summed from its warps' slots
+// (work items wfirst .. wfirst+wcount-1, W warps each) in a fixed order.
 __global__ void rb_check_judge_batch_kernel(RbDev* st, int ninst, int nchk, int itmax, double tol,
-                                            const double* norm_den, int norm_max)
+                                            const double* norm_den, int norm_max, const double* parts,
+                                            const int* wfirst, const int* wcount, int W)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ninst) rb_check_judge(&st[i], nullptr, 0, nchk, itmax, tol, norm_den[i], norm_max);
+    if (i >= ninst || st[i].skip || st[i].step_done) return;   // no iteration ran: its slots are stale
+    st[i].acc = sum_range(parts, (long long)wfirst[i] * W, (long long)wcount[i] * W, norm_max);
+    rb_check_judge(&st[i], nullptr, 0, nchk, itmax, tol, norm_den[i], norm_max);
 }
 
 // The FP64 judge of every instance (one block); in the step graph's WHILE
@@ -428,11 +448,16 @@ __global__ void rb_check_judge_batch_kernel(RbDev* st, int ninst, int nchk, int 
 __global__ void __launch_bounds__(256) rb_base_judge_batch_kernel(RbDev* st, int ninst, double tol,
                                                                   const double* norm_den, int norm_max,
                                                                   cudaGraphConditionalHandle loop, int in_loop,
-                                                                  int* passes)
+                                                                  int* passes, const double* parts64,
+                                                                  const int* ffirst, const int* fcount)
 {
     int running = 0;
-    for (int i = threadIdx.x; i < ninst; i += blockDim.x)
+    for (int i = threadIdx.x; i < ninst; i += blockDim.x) {
+        // the FP64 residual from the instance's base-kernel slots (its field
+        // chunks ffirst .. ffirst+fcount-1), in a fixed order
+        if (!st[i].step_done) st[i].acc64 = sum_range(parts64, ffirst[i], fcount[i], norm_max);
         if (!rb_base_judge(&st[i], tol, norm_den[i], norm_max)) running = 1;
+    }
     const int any = __syncthreads_or(running);
     if (in_loop && threadIdx.x == 0) {
         *passes += 1;
@@ -467,7 +492,7 @@ __global__ void __launch_bounds__(256) rb_base_batch_kernel(const RbBaseArgs* __
         const int ix = (int)(e % b.sy), iy = (int)(e / b.sy);
         if (ix < b.nx) rb_base_cell(b, ix, iy, 0, part, pmax);   // padding columns hold no cell
     }
-    block_reduce_residual(b.acc64, b.norm_max, part, pmax);
+    block_reduce_residual(b.acc64, b.norm_max, part, pmax, b.parts, blockIdx.x);   // the chunk's slot
 }
 
 // ---------------------------------------------------------------------------
@@ -584,6 +609,14 @@ struct ptd_batch {
     int* wcount = nullptr;
     int* active = nullptr;     // work items of the running instances, and their count
     int* nactive = nullptr;
+    // deterministic residuals of the rebased batch: per-warp check slots (work
+    // item k, warp w -> k * W + w; sized for the smallest work items the tuner
+    // can choose) and per-chunk FP64 slots, with each instance's chunk range
+    double* parts = nullptr;
+    long long nparts = 0;
+    double* parts64 = nullptr;
+    int* ffirst = nullptr;
+    int* fcount = nullptr;
     // packed host <-> device transfers
     double* packed = nullptr;
     PackInst* pinst = nullptr;
@@ -756,7 +789,8 @@ int capture_rb(ptd_batch* b)
         }
         if (err == cudaSuccess) {
             rb_check_judge_batch_kernel<<<nb, 128, 0, b->s>>>(b->rdev, n, b->nchk, b->bp.itmax, b->bp.tol,
-                                                              b->norm_den, b->bp.norm == PTD_NORM_MAX);
+                                                              b->norm_den, b->bp.norm == PTD_NORM_MAX, b->parts,
+                                                              b->wfirst, b->wcount, b->cfg.warps2d);
             err = cudaGetLastError();
             ++nk;
         }
@@ -775,7 +809,8 @@ int capture_rb(ptd_batch* b)
     }
     if (err == cudaSuccess) {
         rb_base_judge_batch_kernel<<<1, 256, 0, b->s>>>(b->rdev, n, b->bp.tol, b->norm_den,
-                                                        b->bp.norm == PTD_NORM_MAX, loop, 1, b->passes);
+                                                        b->bp.norm == PTD_NORM_MAX, loop, 1, b->passes,
+                                                        b->parts64, b->ffirst, b->fcount);
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) err = compact_rb(b);
@@ -886,6 +921,25 @@ int build_chunks(ptd_batch* b, bool cells)
 int fill_tables_rb(ptd_batch* b)
 {
     const int n = b->ninst;
+    {   // slots: the most warps any tuner shape gives (28-column tiles, 16-row chunks)
+        long long np = 0, nf = 0;
+        std::vector<int> ff(n), fc(n);
+        for (int i = 0; i < n; ++i) {
+            const Inst& I = b->inst[i];
+            np += (long long)((I.nx - 2 + 27) / 28 + 7) * ((I.ny - 2 + 15) / 16);
+            ff[i] = (int)nf;
+            fc[i] = (int)((I.nfield + 2047) / 2048);   // the field chunks of build_chunks
+            nf += fc[i];
+        }
+        int rc = balloc(&b->parts, (size_t)np * sizeof(double));
+        if (!rc) rc = balloc(&b->parts64, (size_t)nf * sizeof(double));
+        if (!rc) rc = balloc(&b->ffirst, n * sizeof(int));
+        if (!rc) rc = balloc(&b->fcount, n * sizeof(int));
+        if (rc) return rc;
+        b->nparts = np;
+        BCK(cudaMemcpy(b->ffirst, ff.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(b->fcount, fc.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    }
     std::vector<RbArgs> t[2] = {std::vector<RbArgs>(n), std::vector<RbArgs>(n)};
     std::vector<RbFoldArgs> ft(n);
     std::vector<RbBaseArgs> bt(n);
@@ -921,6 +975,7 @@ int fill_tables_rb(ptd_batch* b)
             a.Df = b->Df ? b->Df + o : nullptr;
             a.skip = &b->rdev[i].skip;
             a.acc = &b->rdev[i].acc;
+            a.parts = b->parts;
             a.norm_max = b->bp.norm == PTD_NORM_MAX;
         }
         RbFoldArgs& f = ft[i];
@@ -957,6 +1012,7 @@ int fill_tables_rb(ptd_batch* b)
         g.Cb = b->Cb64 + o;
         g.Hf = b->Hf + o;
         g.acc64 = &b->rdev[i].acc64;
+        g.parts = b->parts64;
         g.norm_max = b->bp.norm == PTD_NORM_MAX;
     }
     for (int q = 0; q < 2; ++q)
@@ -1071,7 +1127,8 @@ void free_batch(ptd_batch* b)
     if (b->gstep) cudaGraphExecDestroy(b->gstep);
     void* rbp[] = {b->wb64[0], b->wb64[1], b->tb32[0], b->tb32[1], b->Rb32, b->Cb64, b->rdev,
                    b->rbtab[0], b->rbtab[1], b->ftab, b->btab, b->passes, b->wfirst, b->wcount,
-                   b->active, b->nactive, b->packed, b->pinst, b->pwork};
+                   b->active, b->nactive, b->packed, b->pinst, b->pwork, b->parts, b->parts64,
+                   b->ffirst, b->fcount};
     for (void* p : rbp) cudaFree(p);
     if (b->h_rdev) cudaFreeHost(b->h_rdev);
     if (b->h_passes) cudaFreeHost(b->h_passes);
@@ -1476,7 +1533,8 @@ static int batch_rb_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
     rb_base_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->btab, b->rdev, b->fwork, 0);
     BCK(cudaGetLastError());
     rb_base_judge_batch_kernel<<<1, 256, 0, b->s>>>(b->rdev, n, b->bp.tol, b->norm_den, b->bp.norm == PTD_NORM_MAX,
-                                                    cudaGraphConditionalHandle{}, 0, b->passes);
+                                                    cudaGraphConditionalHandle{}, 0, b->passes, b->parts64,
+                                                    b->ffirst, b->fcount);
     BCK(cudaGetLastError());
     BCK(compact_rb(b));
     BCK(cudaMemsetAsync(b->passes, 0, sizeof(int), b->s));

@@ -148,3 +148,22 @@ def test_batch_device_tensors_match_host_arrays():
     assert np.array_equal(it_h, it_d)
     for k in range(len(sizes)):
         assert np.array_equal(np.ravel(Hh[k], order="F"), Hd[k].cpu().numpy())
+
+
+def test_batch_rebased_is_deterministic():
+    """FP32_RB batch: the check and FP64 residuals are summed from per-warp /
+    per-chunk slots in a fixed order, so two solves give the same iterations,
+    residuals and H bit for bit."""
+    sizes, Hs, Ds = ptdiff.batch_instances(5, seed=9, nmin=30, nmax=150)
+    p = ptdiff.batch_params(len(sizes), model=S.LINSTEP, precision="fp32_rb", nt=2)
+    out = []
+    with ptdiff.BatchSolver(p, sizes, sizes) as b:
+        for _ in range(2):
+            H = [h.copy(order="F") for h in Hs]
+            iters, err = b.solve(H, Ds)
+            out.append((iters, err, H))
+    (i1, e1, h1), (i2, e2, h2) = out
+    assert np.array_equal(i1, i2)
+    assert np.array_equal(e1, e2)
+    for a, c in zip(h1, h2):
+        assert np.array_equal(a, c)
