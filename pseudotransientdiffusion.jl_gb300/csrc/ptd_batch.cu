@@ -414,30 +414,36 @@ __global__ void rb_reset_batch_kernel(RbDev* st, int ninst)
     if (i < ninst) rb_reset(&st[i]);
 }
 
-// The sum (or max) of slots first .. first+count-1, in order (one thread).
-__device__ __forceinline__ double sum_range(const double* parts, long long first, long long count, int norm_max)
+// The sum (or max) of slots first .. first+count-1 by one warp, in a fixed
+// order: lane l takes slots first+l, first+l+32, ... in order, then a fixed
+// shuffle tree.  Every lane returns the result.
+__device__ __forceinline__ double warp_sum_range(const double* parts, long long first, long long count, int norm_max)
 {
+    const int lane = threadIdx.x & 31;
     double sum = 0.0;
     unsigned long long mx = 0ull;
-    for (long long k = first; k < first + count; ++k) {
+    for (long long k = first + lane; k < first + count; k += 32) {
         const double v = parts[k];
         const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
         mx = bits > mx ? bits : mx;
         sum += v;
     }
-    return norm_max ? __longlong_as_double((long long)mx) : sum;
+    return norm_max ? __longlong_as_double((long long)warp_max_u64(mx)) : warp_sum(sum);
 }
 
-// The FP32 check of every instance, its residual summed from its warps' slots
-// (work items wfirst .. wfirst+wcount-1, W warps each) in a fixed order.
+// The FP32 check of every instance (one warp each), its residual summed from
+// its warps' slots (work items wfirst .. wfirst+wcount-1, W warps each).
 __global__ void rb_check_judge_batch_kernel(RbDev* st, int ninst, int nchk, int itmax, double tol,
                                             const double* norm_den, int norm_max, const double* parts,
                                             const int* wfirst, const int* wcount, int W)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ninst || st[i].skip || st[i].step_done) return;   // no iteration ran: its slots are stale
-    st[i].acc = sum_range(parts, (long long)wfirst[i] * W, (long long)wcount[i] * W, norm_max);
-    rb_check_judge(&st[i], nullptr, 0, nchk, itmax, tol, norm_den[i], norm_max);
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= ninst || st[i].skip || st[i].step_done) return;   // uniform over the warp; no iteration ran
+    const double acc = warp_sum_range(parts, (long long)wfirst[i] * W, (long long)wcount[i] * W, norm_max);
+    if ((threadIdx.x & 31) == 0) {
+        st[i].acc = acc;
+        rb_check_judge(&st[i], nullptr, 0, nchk, itmax, tol, norm_den[i], norm_max);
+    }
 }
 
 // The FP64 judge of every instance (one block); in the step graph's WHILE
@@ -452,11 +458,16 @@ __global__ void __launch_bounds__(256) rb_base_judge_batch_kernel(RbDev* st, int
                                                                   const int* ffirst, const int* fcount)
 {
     int running = 0;
-    for (int i = threadIdx.x; i < ninst; i += blockDim.x) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = threadIdx.x >> 5; i < ninst; i += nw) {   // one warp per instance
         // the FP64 residual from the instance's base-kernel slots (its field
         // chunks ffirst .. ffirst+fcount-1), in a fixed order
-        if (!st[i].step_done) st[i].acc64 = sum_range(parts64, ffirst[i], fcount[i], norm_max);
-        if (!rb_base_judge(&st[i], tol, norm_den[i], norm_max)) running = 1;
+        if (!st[i].step_done) {
+            const double acc = warp_sum_range(parts64, ffirst[i], fcount[i], norm_max);
+            if (lane == 0) st[i].acc64 = acc;
+        }
+        if (lane == 0 && !rb_base_judge(&st[i], tol, norm_den[i], norm_max)) running = 1;
+        __syncwarp();
     }
     const int any = __syncthreads_or(running);
     if (in_loop && threadIdx.x == 0) {
@@ -778,7 +789,7 @@ int capture_rb(ptd_batch* b)
         cudaGraphDestroy(g);
         return cuda_fail(err, "cudaStreamBeginCaptureToGraph");
     }
-    const int n = b->ninst, nb = (n + 127) / 128;
+    const int n = b->ninst, nb = (n + 3) / 4;   // the check judge: one warp per instance, 4 per block
     const int nl = b->nchk / b->tb;   // launches per check block (tb divides nchk)
     int par = 0, nk = 0;
     for (int blk = 0; blk < b->blocks_per_phase && err == cudaSuccess; ++blk) {
