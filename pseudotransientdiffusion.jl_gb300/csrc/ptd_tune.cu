@@ -51,22 +51,32 @@ LaunchCfg tuned_config(const ptd_params& p)
 {
     LaunchCfg c;
     if (p.ndim == 2) {
-        // short y marches in 2-warp CTAs: many independent warps per SM hide
-        // the memory latency of the march.  Measured at 4096^2 over warps
-        // {1,2,4,8} x rows {4..64}: 16 rows is the best or within 2 % of it
-        // for every arithmetic form (FP64 -6 %, DFH -11 %, DF64 -16 % against
-        // 4 warps x 64 rows); the one recomputed face below each march costs
-        // 1/16 of the y faces.
-        c.warps2d = 2;
-        c.chunk2d = 16;
+        // short y marches in small CTAs: many independent warps per SM hide
+        // the memory latency of the march.  Measured at 4096^2 (NONLIN) over
+        // warps {1,2,4,8} x rows {8,16,32,64}, us per iteration against the
+        // former 2 warps x 16 rows: FP64 1 x 32 587.3 (598.5), DFH 1 x 8 199.0
+        // (202.4), DF64 2 x 8 169.3 (173.4), FP32_RB 8 x 32 (two-iteration
+        // marches of 64 rows) 64.6 (65.6); FP32_DC 2 x 16.
+        switch (p.precision) {
+        case PTD_PREC_FP64: c.warps2d = 1; c.chunk2d = 32; break;
+        case PTD_PREC_DFH: c.warps2d = 1; c.chunk2d = 8; break;
+        case PTD_PREC_DF64: c.warps2d = 2; c.chunk2d = 8; break;
+        case PTD_PREC_FP32_RB: c.warps2d = 8; c.chunk2d = 32; break;
+        default: c.warps2d = 2; c.chunk2d = 16; break;
+        }
     } else if (p.ndim == 3) {
         // 512-thread CTAs of 31 x 15 updated cells, 3 resident per SM at <= 40
-        // registers (456 slots on the 152 SMs of a GB300).
+        // registers (456 slots on the 152 SMs of a GB300), short z marches:
+        // at 512^3 over marches {16..512}, FP64 32 planes 6926 us (64: 7016,
+        // 512: 7388), DF64 32: 2011 (64: 2043), FP32_RB 16: 1196 (64: 1236).
+        // Grids too small for whole waves at that length take the longest
+        // march that fills the slots best (wave quantization).
         const int rows = 16, tw = 31;
         const long long slots = 3LL * sm_count();
         const long long bxy = (long long)((p.nx - 2 + tw - 1) / tw) * ((p.ny - 2 + rows - 2) / (rows - 1));
-        const int best = z_chunk(bxy, p.nz, slots);
-        c.chunk3d = best;
+        const int pref = p.precision == PTD_PREC_FP32_RB ? 16 : 32;
+        const long long nb = bxy * ((p.nz - 2 + pref - 1) / pref);
+        c.chunk3d = nb >= 4 * slots ? pref : z_chunk(bxy, p.nz, slots);
         c.rows3d = rows;
     }
     return c;
