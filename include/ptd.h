@@ -238,6 +238,10 @@ PTD_API int ptd_batch_tune(ptd_batch* b, int32_t* warps, int32_t* chunk, float* 
 /* The launch shape in use: warps per CTA, rows per y chunk, FP32 iterations
  * per launch (2 = the temporally blocked FP32_DC or FP32_RB kernel). */
 PTD_API int ptd_batch_config(ptd_batch* b, int32_t* warps, int32_t* chunk, int32_t* iters_per_launch);
+/* Set the launch shape: warps per CTA (1, 2, 4, 8), rows per y chunk (8..4096)
+ * and FP32 iterations per launch (1, or 2 for FP32_DC / FP32_RB with an even
+ * check cadence). */
+PTD_API int ptd_batch_set_config(ptd_batch* b, int32_t warps, int32_t chunk, int32_t iters_per_launch);
 PTD_API int ptd_batch_counters(ptd_batch* b, int64_t* kernel_launches, int64_t* pt_iterations);
 PTD_API void ptd_batch_destroy(ptd_batch* b);
 

@@ -932,12 +932,13 @@ int build_chunks(ptd_batch* b, bool cells)
 int fill_tables_rb(ptd_batch* b)
 {
     const int n = b->ninst;
-    {   // slots: the most warps any tuner shape gives (28-column tiles, 16-row chunks)
+    {   // slots: the most warps any launch shape gives (28-column tiles, up to 8
+        // warps per CTA, rows per chunk >= 8: ptd_batch_set_config's bounds)
         long long np = 0, nf = 0;
         std::vector<int> ff(n), fc(n);
         for (int i = 0; i < n; ++i) {
             const Inst& I = b->inst[i];
-            np += (long long)((I.nx - 2 + 27) / 28 + 7) * ((I.ny - 2 + 15) / 16);
+            np += (long long)((I.nx - 2 + 27) / 28 + 7) * ((I.ny - 2 + 7) / 8);
             ff[i] = (int)nf;
             fc[i] = (int)((I.nfield + 2047) / 2048);   // the field chunks of build_chunks
             nf += fc[i];
@@ -1729,4 +1730,21 @@ extern "C" int ptd_batch_config(ptd_batch* b, int32_t* warps, int32_t* chunk, in
     if (chunk) *chunk = b->cfg.chunk2d;
     if (iters_per_launch) *iters_per_launch = (b->dc || b->rb) ? b->tb : 1;
     return PTD_OK;
+}
+
+extern "C" int ptd_batch_set_config(ptd_batch* b, int32_t warps, int32_t chunk, int32_t iters_per_launch)
+{
+    if (!b) return bfail(PTD_EINVAL, "batch is NULL");
+    if (warps != 1 && warps != 2 && warps != 4 && warps != 8) return bfail(PTD_EINVAL, "warps must be 1, 2, 4 or 8");
+    if (chunk < 8 || chunk > 4096) return bfail(PTD_EINVAL, "rows per y chunk must be in [8, 4096]");
+    const bool fp32 = b->dc || b->rb;
+    if (iters_per_launch != 1 && !(iters_per_launch == 2 && fp32 && b->nchk % 2 == 0))
+        return bfail(PTD_EINVAL, "iterations per launch: 1, or 2 for FP32_DC / FP32_RB with an even nchk");
+    BCK(cudaStreamSynchronize(b->s));
+    b->cfg.warps2d = warps;
+    b->cfg.chunk2d = chunk;
+    b->tb = iters_per_launch;
+    int rc = upload_work(b);
+    if (!rc) rc = capture(b);
+    return rc;
 }

@@ -52,6 +52,8 @@ def _lib():
         L.ptd_batch_tune.restype = C.c_int
         L.ptd_batch_config.argtypes = [vp, ip, ip, ip]
         L.ptd_batch_config.restype = C.c_int
+        L.ptd_batch_set_config.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
+        L.ptd_batch_set_config.restype = C.c_int
         L.ptd_batch_counters.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.ptd_batch_counters.restype = C.c_int
         L.ptd_batch_destroy.argtypes = [vp]
@@ -109,6 +111,11 @@ class BatchSolver:
         w, c, t = C.c_int32(0), C.c_int32(0), C.c_int32(0)
         _abi.check(_lib().ptd_batch_config(self._h, C.byref(w), C.byref(c), C.byref(t)), "ptd_batch_config")
         return w.value, c.value, t.value
+
+    def set_config(self, warps, chunk, iters_per_launch):
+        """Set the launch shape (warps per CTA, rows per y chunk, FP32
+        iterations per launch)."""
+        _abi.check(_lib().ptd_batch_set_config(self._h, warps, chunk, iters_per_launch), "ptd_batch_set_config")
 
     def solve(self, Hs, Ds=None):
         """Solve in place on the list of fields Hs: Fortran-ordered host arrays,

@@ -167,3 +167,22 @@ def test_batch_rebased_is_deterministic():
     assert np.array_equal(e1, e2)
     for a, c in zip(h1, h2):
         assert np.array_equal(a, c)
+
+
+def test_batch_set_config():
+    """A launch shape set by hand is the one in use, and the solve it gives
+    agrees with the tuned one to the converged-to-tol bound."""
+    sizes, Hs, Ds = ptdiff.batch_instances(4, seed=10, nmin=20, nmax=100)
+    p = ptdiff.batch_params(len(sizes), model=S.LINSTEP, precision="fp32_rb", nt=1)
+    with ptdiff.BatchSolver(p, sizes, sizes) as b:
+        Ha = [h.copy(order="F") for h in Hs]
+        b.solve(Ha, Ds)
+        b.set_config(4, 24, 1)
+        assert b.config() == (4, 24, 1)
+        Hb = [h.copy(order="F") for h in Hs]
+        b.solve(Hb, Ds)
+        with pytest.raises(ptdiff._abi.PtdError):
+            b.set_config(3, 24, 1)
+    for a, c in zip(Ha, Hb):
+        rms = float(np.sqrt(np.mean(np.square(a))))
+        assert rel_l2(c, a) <= 2 * 0.2 * 1e-8 / rms
