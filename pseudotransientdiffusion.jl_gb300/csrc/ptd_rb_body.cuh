@@ -544,7 +544,11 @@ __device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, in
 
     // ---- march: level 1 of row s+1, level 2 of row s.  (Issuing a step's
     // loads one step ahead, in registers, was no faster: 66.6 against 66.4 us
-    // per iteration at 4096^2, its 78 registers halving the resident warps.)
+    // per iteration at 4096^2, its 78 registers halving the resident warps.
+    // Staging them through a per-warp shared-memory ring with cp.async, one to
+    // three steps ahead, was slower at every launch shape that fills the GPU:
+    // 67.5 / 68.6 / 90.5 us against 64.7 at the best shape, the shared loads
+    // costing more issue slots than the hidden latency saved.)
     long long o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float2 p1 = d1, wx1 = f2(0.0f), wy1 = f2(0.0f), r1 = f2(0.0f), h2 = h1, tbx1 = f2(0.0f), tby1 = f2(0.0f);
