@@ -50,6 +50,7 @@ struct AdjArgs {
     const void* g;      // right-hand side (rebased form: minus the base update residual)
     const int* done;
     double* acc;
+    double* parts;      // check-residual slots, one per CTA (summed in a fixed order by the judge)
     // rebased FP32 form (precision FP32_RB): the adjoint PT iteration on the
     // change since an FP64 base (lam_b, w_b), see ptd_rb.cu for the scheme
     float rdtf;
@@ -79,6 +80,7 @@ __device__ __forceinline__ float nmadf(F32, float c, float t, float w) { return 
 // `stall` checks)
 struct AdjState {
     int done, nchecks, iter, best_at;
+    int blocks, pad;    // check blocks run by the solve graph
     double acc, err, target, accept, best;
 };
 
@@ -264,7 +266,9 @@ __global__ void __launch_bounds__(32 * R) adj3d_kernel(const AdjArgs* __restrict
             p ^= 1;
         }
     }
-    if (CHECK) block_reduce_residual(a.acc, 0, part, pmax);
+    if (CHECK)
+        block_reduce_residual(a.acc, 0, part, pmax, a.parts,
+                              ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
 // Gradient accumulation of one step (FP64, one thread per cell of the whole
@@ -334,11 +338,14 @@ __global__ void __launch_bounds__(256) adj_grad_kernel(AdjArgs a, const double* 
     }
 }
 
-__global__ void adj_target_kernel(AdjState* st, double rtol, double accept_rtol, double norm_den,
-                                  double floor_abs)
+__global__ void __launch_bounds__(256) adj_target_kernel(AdjState* st, const double* parts, long long nparts,
+                                                         double rtol, double accept_rtol, double norm_den,
+                                                         double floor_abs)
 {
-    const double gn = sqrt(st->acc) / sqrt(norm_den);
+    const double gn = sqrt(sum_slots(parts, nparts, 0)) / sqrt(norm_den);
+    if (threadIdx.x != 0) return;
     st->acc = 0.0;
+    st->blocks = 0;
     st->target = fmax(rtol * gn, floor_abs);
     st->accept = fmax(accept_rtol * gn, floor_abs);
     st->done = gn == 0.0 ? 1 : 0;
@@ -349,10 +356,28 @@ __global__ void adj_target_kernel(AdjState* st, double rtol, double accept_rtol,
     st->best_at = 0;
 }
 
-__global__ void adj_judge_kernel(AdjState* st, int nchk, int itmax, double norm_den, int stall)
+// After each check block: the err from the check launch's slots (fixed
+// order); ends the solve graph's loop once the solve has stopped.  Every pass
+// of a running solve adds nchk iterations and the solve stops (capped) before
+// one would pass itmax, so the loop ends within itmax/nchk + 1 passes.
+__global__ void __launch_bounds__(256) adj_judge_kernel(AdjState* st, const double* parts, long long nparts,
+                                                        int nchk, int itmax, double norm_den, int stall,
+                                                        cudaGraphConditionalHandle loop)
 {
-    if (st->done) return;
-    const double err = sqrt(st->acc) / sqrt(norm_den);
+    // every thread reads the flag before thread 0 can change it
+    const bool idle = st->done != 0;
+    __syncthreads();
+    if (idle) {   // no PT kernel ran: the slots are stale
+        if (threadIdx.x == 0) {
+            st->blocks += 1;
+            cudaGraphSetConditional(loop, 0);
+        }
+        return;
+    }
+    const double acc = sum_slots(parts, nparts, 0);
+    if (threadIdx.x != 0) return;
+    st->blocks += 1;
+    const double err = sqrt(acc) / sqrt(norm_den);
     st->acc = 0.0;
     st->err = err;
     st->nchecks += 1;
@@ -365,11 +390,12 @@ __global__ void adj_judge_kernel(AdjState* st, int nchk, int itmax, double norm_
     else if (err != err) st->done = 2;
     else if (st->nchecks - st->best_at >= stall && err <= st->accept) st->done = 3;
     else if (st->iter + nchk > itmax) st->done = 2;
+    if (st->done) cudaGraphSetConditional(loop, 0);
 }
 
-// sum over inner cells of v^2 (v as N::T) into acc; loss uses the FP64 variant.
+// sum over inner cells of v^2 (v as N::T), one slot per CTA.
 template <class N>
-__global__ void __launch_bounds__(256) adj_sumsq_kernel(const void* v, double* acc, int nx, int ny, int nz,
+__global__ void __launch_bounds__(256) adj_sumsq_kernel(const void* v, double* parts, int nx, int ny, int nz,
                                                         long long sy, long long sz)
 {
     const long long nix = nx - 2, niy = ny - 2, niz = nz - 2, total = nix * niy * niz;
@@ -381,7 +407,7 @@ __global__ void __launch_bounds__(256) adj_sumsq_kernel(const void* v, double* a
         const double x = N::to_d(ld<N>(v, iz * sz + iy * sy + ix));
         part = fma(x, x, part);
     }
-    block_reduce_residual(acc, 0, part, pm);
+    block_reduce_residual(nullptr, 0, part, pm, parts, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -397,6 +423,7 @@ __global__ void __launch_bounds__(256) adj_sumsq_kernel(const void* v, double* a
 // base confirms the stop.
 struct AdjRbState {
     int skip, done, iter, phase_iter, nchecks, capped, stalled, best_at;
+    int blocks, passes, phases, pad;   // check blocks, loop passes, rebases of the solve graph
     double acc, acc64, err, err64, target, accept, best;
 };
 
@@ -415,21 +442,23 @@ struct AdjFold {
     float* w[3][2];
 };
 
-// lam_b += delta, w_b += omega; clear the parity-0 buffers the next phase reads
-__global__ void adj_rb_fold_kernel(AdjFold f, const AdjRbState* st)
+// lam_b += delta, w_b += omega (the changes of buffer parity par); both
+// buffers cleared, the next iteration may start on either parity
+__global__ void adj_rb_fold_kernel(AdjFold f, const AdjRbState* st, int par)
 {
     if (st->done) return;
-    const int par = st->phase_iter & 1;
     const float* dp = par ? f.d[1] : f.d[0];
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < f.n;
          t += (long long)gridDim.x * blockDim.x) {
         f.lamb[t] += (double)dp[t];
         f.d[0][t] = 0.0f;
+        f.d[1][t] = 0.0f;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const float* wp = par ? f.w[d][1] : f.w[d][0];
             f.wb[d][t] += (double)wp[t];
             f.w[d][0][t] = 0.0f;
+            f.w[d][1][t] = 0.0f;
         }
     }
 }
@@ -447,7 +476,7 @@ struct AdjBase {
     float* tb[3];
     float* rbf;          // -R_b
     double* Cb;
-    double* acc64;
+    double* parts;       // FP64 residual slots, one per CTA
 };
 
 // FP64 base quantities (one thread per cell): t_b for the +d faces, and for
@@ -502,13 +531,16 @@ __global__ void __launch_bounds__(256) adj_rb_base_kernel(AdjBase b, const AdjRb
             accumulate_residual(cb, part, pmax);
         }
     }
-    block_reduce_residual(b.acc64, 0, part, pmax);
+    block_reduce_residual(nullptr, 0, part, pmax, b.parts, blockIdx.x);
 }
 
-__global__ void adj_rb_init_kernel(AdjRbState* st, double rtol, double accept_rtol, double norm_den)
+__global__ void __launch_bounds__(256) adj_rb_init_kernel(AdjRbState* st, const double* parts, long long nparts,
+                                                          double rtol, double accept_rtol, double norm_den)
 {
-    const double gn = sqrt(st->acc) / sqrt(norm_den);
+    const double gn = sqrt(sum_slots(parts, nparts, 0)) / sqrt(norm_den);
+    if (threadIdx.x != 0) return;
     st->acc = 0.0;
+    st->blocks = st->passes = st->phases = 0;
     st->acc64 = 0.0;
     st->target = fmax(rtol * gn, 1e-300);
     st->accept = fmax(accept_rtol * gn, 1e-300);
@@ -518,10 +550,28 @@ __global__ void adj_rb_init_kernel(AdjRbState* st, double rtol, double accept_rt
     st->err = st->err64 = st->best = gn;
 }
 
-__global__ void adj_rb_check_judge_kernel(AdjRbState* st, int nchk, int itmax, double norm_den, int stall)
+// After each check block: the FP32 err from the check launch's slots (fixed
+// order); the phase ends (skip) on the conditions below, and the rebase that
+// follows the block in the solve graph (its IF node) runs when it has.
+__global__ void __launch_bounds__(256) adj_rb_check_judge_kernel(AdjRbState* st, const double* parts,
+                                                                 long long nparts, int nchk, int itmax,
+                                                                 double norm_den, int stall, int phase_cap,
+                                                                 cudaGraphConditionalHandle rebase)
 {
-    if (st->skip || st->done) return;
-    const double err = sqrt(st->acc) / sqrt(norm_den);
+    // every thread reads the flags before thread 0 can change them
+    const bool idle = st->skip || st->done;
+    __syncthreads();
+    if (idle) {   // no PT kernel ran: the slots are stale
+        if (threadIdx.x == 0) {
+            st->blocks += 1;
+            cudaGraphSetConditional(rebase, 0);
+        }
+        return;
+    }
+    const double acc = sum_slots(parts, nparts, 0);
+    if (threadIdx.x != 0) return;
+    st->blocks += 1;
+    const double err = sqrt(acc) / sqrt(norm_den);
     st->acc = 0.0;
     st->err = err;
     st->nchecks += 1;
@@ -534,6 +584,7 @@ __global__ void adj_rb_check_judge_kernel(AdjRbState* st, int nchk, int itmax, d
     if (err != err) {
         st->done = 2;
         st->skip = 1;
+        cudaGraphSetConditional(rebase, 1);
         return;
     }
     if (!(err > st->target)) {
@@ -541,19 +592,30 @@ __global__ void adj_rb_check_judge_kernel(AdjRbState* st, int nchk, int itmax, d
     } else if (st->nchecks - st->best_at >= stall && err <= st->accept) {
         st->skip = 1;
         st->stalled = 1;
-    } else if (err <= 1e-4 * st->err64) {
+    } else if (err <= 1e-4 * st->err64 || st->phase_iter >= phase_cap) {
         st->skip = 1;
     }
     if (st->iter + nchk > itmax) {
         st->skip = 1;
         st->capped = 1;
     }
+    cudaGraphSetConditional(rebase, st->skip ? 1 : 0);
 }
 
-__global__ void adj_rb_base_judge_kernel(AdjRbState* st, double norm_den)
+__global__ void __launch_bounds__(256) adj_rb_base_judge_kernel(AdjRbState* st, const double* parts,
+                                                                long long nparts, double norm_den, int in_loop)
 {
-    if (st->done) return;
-    const double err64 = sqrt(st->acc64) / sqrt(norm_den);
+    // every thread reads the flag before thread 0 can change it
+    const bool stopped = st->done != 0;
+    __syncthreads();
+    if (stopped) {   // the base kernel did not run: the slots are stale
+        if (threadIdx.x == 0 && in_loop) st->phases += 1;
+        return;
+    }
+    const double acc64 = sum_slots(parts, nparts, 0);
+    if (threadIdx.x != 0) return;
+    if (in_loop) st->phases += 1;
+    const double err64 = sqrt(acc64) / sqrt(norm_den);
     st->acc64 = 0.0;
     st->err64 = err64;
     st->phase_iter = 0;
@@ -573,7 +635,20 @@ __global__ void adj_rb_base_judge_kernel(AdjRbState* st, double norm_den)
     }
 }
 
-__global__ void __launch_bounds__(256) adj_misfit_kernel(const double* HN, const double* Ht, void* g, double* acc,
+// Last node of the rebased solve graph's loop body: ends the loop once the
+// solve has stopped; a solve still running after max_passes passes
+// (itmax/nchk + 2) has lost its stop and ends as capped.
+__global__ void adj_rb_loop_judge_kernel(AdjRbState* st, int max_passes, cudaGraphConditionalHandle loop)
+{
+    st->passes += 1;
+    if (!st->done && st->passes > max_passes) {
+        st->done = 2;
+        st->skip = 1;
+    }
+    if (st->done) cudaGraphSetConditional(loop, 0);
+}
+
+__global__ void __launch_bounds__(256) adj_misfit_kernel(const double* HN, const double* Ht, void* g, double* parts,
                                                          int nx, int ny, int nz, long long sy, long long sz, int df64)
 {
     const long long nix = nx - 2, niy = ny - 2, niz = nz - 2, total = nix * niy * niz;
@@ -590,7 +665,7 @@ __global__ void __launch_bounds__(256) adj_misfit_kernel(const double* HN, const
             else reinterpret_cast<double*>(g)[c] = d;
         }
     }
-    block_reduce_residual(acc, 0, part, pm);
+    block_reduce_residual(nullptr, 0, part, pm, parts, blockIdx.x);
 }
 
 __global__ void expd_kernel(const double* m, double* E, long long n)
@@ -649,8 +724,13 @@ struct ptd_adj {
     AdjRbState* h_rbst = nullptr;
     AdjArgs* d_rbargs[2] = {nullptr, nullptr};
     cudaGraphExec_t gphase = nullptr;
-    int blocks_per_phase = 1;
-    int kernels_per_phase = 0;
+    int phase_iters = 200;      // PT iterations of a rebased phase at most
+    int blocks_per_pass = 1;    // check blocks per pass of a solve graph's loop
+    double* parts = nullptr;    // check-residual slots of the check launches
+    long long nparts = 0;
+    double* parts64 = nullptr;  // slots of the grid-stride reductions (one per CTA)
+    long long nparts64 = 0;
+    double* h_parts64 = nullptr;
 };
 
 namespace {
@@ -726,6 +806,7 @@ void adj_fill(ptd_adj* A, int par, AdjArgs& a)
     a.g = A->gbuf;
     a.done = &A->st->done;
     a.acc = &A->st->acc;
+    a.parts = A->parts;
 }
 
 void adj_fill_rb(ptd_adj* A, int par, AdjArgs& a)
@@ -763,11 +844,11 @@ AdjBase adj_base_args(ptd_adj* A)
     b.g = static_cast<const double*>(A->gbuf);
     b.rbf = static_cast<float*>(A->rbf);
     b.Cb = A->Cb;
-    b.acc64 = &A->rbst->acc64;
+    b.parts = A->parts64;
     return b;
 }
 
-cudaError_t adj_rebase(ptd_adj* A)
+cudaError_t adj_rebase(ptd_adj* A, int par, int in_loop)
 {
     AdjFold f;
     std::memset(&f, 0, sizeof(f));
@@ -778,20 +859,51 @@ cudaError_t adj_rebase(ptd_adj* A)
         f.wb[d] = A->wb[d];
         for (int q = 0; q < 2; ++q) f.w[d][q] = static_cast<float*>(A->w[d][q]);
     }
-    adj_rb_fold_kernel<<<fill_blocks(), 256, 0, A->s>>>(f, A->rbst);
+    adj_rb_fold_kernel<<<fill_blocks(), 256, 0, A->s>>>(f, A->rbst, par);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (A->expm) adj_rb_base_kernel<true><<<fill_blocks(), 256, 0, A->s>>>(adj_base_args(A), A->rbst);
     else adj_rb_base_kernel<false><<<fill_blocks(), 256, 0, A->s>>>(adj_base_args(A), A->rbst);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    adj_rb_base_judge_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->dv.norm_den);
+    adj_rb_base_judge_kernel<<<1, 256, 0, A->s>>>(A->rbst, A->parts64, A->nparts64, A->dv.norm_den, in_loop);
     return cudaGetLastError();
 }
 
-// One phase of the rebased adjoint: check blocks of FP32 iterations, each
-// followed by the FP32 judge, then the FP64 rebase and judge.  Every phase
-// starts from buffer parity 0.
+// The WHILE node of a solve graph, and its body graph.
+cudaError_t adj_loop_graph(cudaGraph_t* g, cudaGraphConditionalHandle* loop, cudaGraph_t* body)
+{
+    *g = nullptr;
+    cudaError_t err = cudaGraphCreate(g, 0);
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(loop, *g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = *loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, *g, nullptr, nullptr, 0, &np);
+    if (err == cudaSuccess) *body = np.conditional.phGraph_out[0];
+    return err;
+}
+
+// End a capture that an error interrupted.
+void adj_drop_capture(cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs;
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t dropped = nullptr;
+        cudaStreamEndCapture(s, &dropped);
+        if (dropped) cudaGraphDestroy(dropped);
+    }
+    cudaGetLastError();
+}
+
+// The rebased adjoint solve of one step as one CUDA graph: a WHILE node whose
+// body is one check block (nchk FP32 launches and the check judge) followed by
+// an IF node holding the FP64 rebase (fold, base quantities, base judge), run
+// when the judge has ended the phase; two such blocks when nchk is odd, so
+// that every pass starts on buffer parity 0; last, the loop judge.  No launch
+// is issued past the end of a phase or of the solve.
 int adj_capture_rb(ptd_adj* A)
 {
     for (int q = 0; q < 2; ++q) {
@@ -799,37 +911,80 @@ int adj_capture_rb(ptd_adj* A)
         adj_fill_rb(A, q, a);
         ACK(cudaMemcpy(A->d_rbargs[q], &a, sizeof(a), cudaMemcpyHostToDevice));
     }
-    cudaGraph_t gr = nullptr;
-    ACK(cudaStreamBeginCapture(A->s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t err = cudaSuccess;
-    int par = 0, nk = 0;
-    for (int b = 0; b < A->blocks_per_phase && err == cudaSuccess; ++b) {
+    cudaGraph_t g = nullptr, body = nullptr;
+    cudaGraphConditionalHandle loop;
+    cudaError_t err = adj_loop_graph(&g, &loop, &body);
+    const int nblk = (A->nchk & 1) ? 2 : 1;
+    int par = 0;
+    cudaGraphNode_t prev = nullptr;   // the previous block's IF node
+    for (int b = 0; b < nblk && err == cudaSuccess; ++b) {
+        cudaGraphConditionalHandle rebase;
+        err = cudaGraphConditionalHandleCreate(&rebase, body, 0, cudaGraphCondAssignDefault);
+        if (err == cudaSuccess)
+            err = cudaStreamBeginCaptureToGraph(A->s, body, prev ? &prev : nullptr, nullptr, prev ? 1 : 0,
+                                                cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) break;
         for (int it = 0; it < A->nchk && err == cudaSuccess; ++it) {
             err = adj_launch_rb(A, par, it == A->nchk - 1);
             par ^= 1;
-            ++nk;
         }
         if (err == cudaSuccess) {
-            adj_rb_check_judge_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->nchk, A->p.itmax, A->dv.norm_den, A->stall);
+            adj_rb_check_judge_kernel<<<1, 256, 0, A->s>>>(A->rbst, A->parts, A->nparts, A->nchk, A->p.itmax,
+                                                           A->dv.norm_den, A->stall, A->phase_iters, rebase);
             err = cudaGetLastError();
-            ++nk;
         }
+        // the judge is the capture's last node: the IF node follows it
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        const cudaError_t e1 = cudaStreamGetCaptureInfo(A->s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        cudaGraphNode_t leaf = (e1 == cudaSuccess && nd == 1) ? deps[0] : nullptr;
+        cudaGraph_t captured = body;
+        const cudaError_t e2 = cudaStreamEndCapture(A->s, &captured);
+        if (err == cudaSuccess) err = e1 != cudaSuccess ? e1 : e2;
+        if (err == cudaSuccess && !leaf) err = cudaErrorStreamCaptureInvalidated;
+        cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
+        ip.conditional.handle = rebase;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        cudaGraphNode_t ifn = nullptr;
+        if (err == cudaSuccess) err = cudaGraphAddNode(&ifn, body, &leaf, nullptr, 1, &ip);
+        if (err == cudaSuccess)
+            err = cudaStreamBeginCaptureToGraph(A->s, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) break;
+        err = adj_rebase(A, par, 1);
+        cudaGraph_t ifbody = ip.conditional.phGraph_out[0];
+        const cudaError_t e3 = cudaStreamEndCapture(A->s, &ifbody);
+        if (err == cudaSuccess) err = e3;
+        prev = ifn;
     }
-    if (err == cudaSuccess) err = adj_rebase(A);
-    nk += 3;
-    cudaError_t e2 = cudaStreamEndCapture(A->s, &gr);
+    // the loop's condition, set at the body's level after the last rebase node
+    if (err == cudaSuccess)
+        err = cudaStreamBeginCaptureToGraph(A->s, body, &prev, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+    if (err == cudaSuccess) {
+        adj_rb_loop_judge_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->p.itmax / A->nchk + 2, loop);
+        err = cudaGetLastError();
+        cudaGraph_t captured = body;
+        const cudaError_t e4 = cudaStreamEndCapture(A->s, &captured);
+        if (err == cudaSuccess) err = e4;
+    }
     if (err != cudaSuccess) {
-        if (gr) cudaGraphDestroy(gr);
+        adj_drop_capture(A->s);
+        if (g) cudaGraphDestroy(g);
         return cuda_fail(err, "adjoint capture (rebased)");
     }
-    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-    cudaError_t e3 = cudaGraphInstantiate(&A->gphase, gr, 0);
-    cudaGraphDestroy(gr);
-    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
-    A->kernels_per_phase = nk;
+    const cudaError_t e5 = cudaGraphInstantiate(&A->gphase, g, 0);
+    cudaGraphDestroy(g);
+    if (e5 != cudaSuccess) return cuda_fail(e5, "cudaGraphInstantiate");
+    A->blocks_per_pass = nblk;
     return PTD_OK;
 }
 
+// The FP64 / DF64 adjoint solve of one step as one CUDA graph: a WHILE node
+// whose body is one check block (nchk launches and the judge, which ends the
+// loop once the solve has stopped); two blocks when nchk is odd, so that every
+// pass starts on buffer parity 0.
 int adj_capture(ptd_adj* A)
 {
     for (int q = 0; q < 2; ++q) {
@@ -837,29 +992,37 @@ int adj_capture(ptd_adj* A)
         adj_fill(A, q, a);
         ACK(cudaMemcpy(A->d_args[q], &a, sizeof(a), cudaMemcpyHostToDevice));
     }
-    for (int q = 0; q < 2; ++q) {
-        cudaGraph_t gr = nullptr;
-        ACK(cudaStreamBeginCapture(A->s, cudaStreamCaptureModeThreadLocal));
-        cudaError_t err = cudaSuccess;
-        int par = q;
+    cudaGraph_t g = nullptr, body = nullptr;
+    cudaGraphConditionalHandle loop;
+    cudaError_t err = adj_loop_graph(&g, &loop, &body);
+    if (err == cudaSuccess)
+        err = cudaStreamBeginCaptureToGraph(A->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    const int nblk = (A->nchk & 1) ? 2 : 1;
+    int par = 0;
+    for (int b = 0; b < nblk && err == cudaSuccess; ++b) {
         for (int it = 0; it < A->nchk && err == cudaSuccess; ++it) {
             err = adj_launch(A, par, it == A->nchk - 1);
             par ^= 1;
         }
         if (err == cudaSuccess) {
-            adj_judge_kernel<<<1, 1, 0, A->s>>>(A->st, A->nchk, A->p.itmax, A->dv.norm_den, A->stall);
+            adj_judge_kernel<<<1, 256, 0, A->s>>>(A->st, A->parts, A->nparts, A->nchk, A->p.itmax, A->dv.norm_den,
+                                                  A->stall, loop);
             err = cudaGetLastError();
         }
-        cudaError_t e2 = cudaStreamEndCapture(A->s, &gr);
-        if (err != cudaSuccess) {
-            if (gr) cudaGraphDestroy(gr);
-            return cuda_fail(err, "adjoint capture");
-        }
-        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-        cudaError_t e3 = cudaGraphInstantiate(&A->graph[q], gr, 0);
-        cudaGraphDestroy(gr);
-        if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
     }
+    if (err == cudaSuccess) {
+        cudaGraph_t captured = body;
+        err = cudaStreamEndCapture(A->s, &captured);
+    }
+    if (err != cudaSuccess) {
+        adj_drop_capture(A->s);
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(err, "adjoint capture");
+    }
+    const cudaError_t e3 = cudaGraphInstantiate(&A->graph[0], g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+    A->blocks_per_pass = nblk;
     return PTD_OK;
 }
 
@@ -873,7 +1036,7 @@ void adj_free(ptd_adj* A)
     if (A->fwd) ptd_destroy(A->fwd);
     void* ptrs[] = {A->ck, A->Ht, A->Ed, A->E, A->Hk, A->lam[0], A->lam[1], A->gbuf, A->gm, A->gh, A->stage,
                     A->st, A->d_args[0], A->d_args[1], A->lamb, A->Hk64, A->rbf, A->Cb, A->rbst, A->d_rbargs[0],
-                    A->d_rbargs[1]};
+                    A->d_rbargs[1], A->parts, A->parts64};
     for (void* q : ptrs) cudaFree(q);
     for (int d = 0; d < 3; ++d) {
         for (int q = 0; q < 2; ++q) cudaFree(A->w[d][q]);
@@ -882,6 +1045,7 @@ void adj_free(ptd_adj* A)
     }
     if (A->h_st) cudaFreeHost(A->h_st);
     if (A->h_rbst) cudaFreeHost(A->h_rbst);
+    if (A->h_parts64) cudaFreeHost(A->h_parts64);
     delete A;
 }
 
@@ -904,7 +1068,6 @@ extern "C" int ptd_adj_create(ptd_adj** out, const ptd_params* p)
     A->df64 = p->precision == PTD_PREC_DF64;
     A->rb = p->precision == PTD_PREC_FP32_RB;
     A->expm = p->model == PTD_MODEL_NONLIN_EXPM;
-    A->blocks_per_phase = std::max(1, (200 + A->nchk - 1) / A->nchk);
     derive(A->p, A->dv);
     {   // the adjoint kernels tile like the one-cell-per-lane FP64 kernels
         ptd_params pt = A->p;
@@ -953,6 +1116,15 @@ extern "C" int ptd_adj_create(ptd_adj** out, const ptd_params* p)
     for (int q = 0; q < 2 && !rc; ++q) rc = al((void**)&A->d_args[q], sizeof(AdjArgs));
     if (!rc && cudaMallocHost((void**)&A->h_st, sizeof(AdjState)) != cudaSuccess)
         rc = set_error(PTD_ENOMEM, "adjoint: cudaMallocHost failed");
+    // residual slots: one per CTA of a check launch, one per CTA of the
+    // grid-stride reductions (sums of squares, misfit, rebase)
+    A->nparts = (long long)((A->g.nx - 2 + 30) / 31) * ((A->g.ny - 2 + 14) / 15) *
+                ((A->g.nz - 2 + A->cfg.chunk3d - 1) / A->cfg.chunk3d);
+    A->nparts64 = fill_blocks();
+    if (!rc) rc = al((void**)&A->parts, (size_t)A->nparts * sizeof(double));
+    if (!rc) rc = al((void**)&A->parts64, (size_t)A->nparts64 * sizeof(double));
+    if (!rc && cudaMallocHost((void**)&A->h_parts64, (size_t)A->nparts64 * sizeof(double)) != cudaSuccess)
+        rc = set_error(PTD_ENOMEM, "adjoint: cudaMallocHost failed");
     if (A->rb) {
         if (!rc) rc = al((void**)&A->lamb, b);
         if (!rc) rc = al((void**)&A->Hk64, b);
@@ -982,13 +1154,15 @@ extern "C" void ptd_adj_destroy(ptd_adj* A) { adj_free(A); }
 static int adj_loss(ptd_adj* A, double* loss)
 {
     const double* HN = A->ck + (size_t)A->p.nt * A->g.nfield;
-    ACK(cudaMemsetAsync(&A->st->acc, 0, sizeof(double), A->s));
-    adj_misfit_kernel<<<fill_blocks(), 256, 0, A->s>>>(HN, A->Ht, nullptr, &A->st->acc, A->g.nx, A->g.ny, A->g.nz, A->g.sy,
-                                                  A->g.sz, 0);
+    adj_misfit_kernel<<<(int)A->nparts64, 256, 0, A->s>>>(HN, A->Ht, nullptr, A->parts64, A->g.nx, A->g.ny, A->g.nz,
+                                                          A->g.sy, A->g.sz, 0);
     ACK(cudaGetLastError());
-    ACK(cudaMemcpyAsync(A->h_st, A->st, sizeof(AdjState), cudaMemcpyDeviceToHost, A->s));
+    ACK(cudaMemcpyAsync(A->h_parts64, A->parts64, (size_t)A->nparts64 * sizeof(double), cudaMemcpyDeviceToHost,
+                        A->s));
     ACK(cudaStreamSynchronize(A->s));
-    if (loss) *loss = 0.5 * A->h_st->acc;
+    double acc = 0.0;   // the CTAs' partial sums in a fixed order
+    for (long long i = 0; i < A->nparts64; ++i) acc += A->h_parts64[i];
+    if (loss) *loss = 0.5 * acc;
     return PTD_OK;
 }
 
@@ -1054,10 +1228,9 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
     // g = H^nt - Ht on inner cells
     ACK(cudaMemsetAsync(A->gbuf, 0, b, A->s));
     const double* HN = A->ck + (size_t)A->p.nt * A->g.nfield;
-    adj_misfit_kernel<<<fill_blocks(), 256, 0, A->s>>>(HN, A->Ht, A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
-                                                  A->g.sy, A->g.sz, A->df64);
+    adj_misfit_kernel<<<(int)A->nparts64, 256, 0, A->s>>>(HN, A->Ht, A->gbuf, A->parts64, A->g.nx, A->g.ny,
+                                                          A->g.nz, A->g.sy, A->g.sz, A->df64);
     ACK(cudaGetLastError());
-    ACK(cudaMemsetAsync(&A->st->acc, 0, sizeof(double), A->s));
     const long long cells = (long long)A->g.nx * A->g.ny * A->g.nz;
     for (int n = A->p.nt; n >= 1 && A->rb; --n) {
         // rebased FP32 adjoint solve of step n
@@ -1071,29 +1244,19 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
             ACK(cudaMemsetAsync(A->lam[q], 0, b, A->s));
             for (int d = 0; d < 3; ++d) ACK(cudaMemsetAsync(A->w[d][q], 0, b, A->s));
         }
-        ACK(cudaMemsetAsync(&A->rbst->acc, 0, sizeof(double), A->s));
-        adj_sumsq_kernel<F64><<<fill_blocks(), 256, 0, A->s>>>(A->gbuf, &A->rbst->acc, A->g.nx, A->g.ny, A->g.nz, A->g.sy,
-                                                         A->g.sz);
+        adj_sumsq_kernel<F64><<<(int)A->nparts64, 256, 0, A->s>>>(A->gbuf, A->parts64, A->g.nx, A->g.ny, A->g.nz,
+                                                                  A->g.sy, A->g.sz);
         ACK(cudaGetLastError());
-        adj_rb_init_kernel<<<1, 1, 0, A->s>>>(A->rbst, A->rtol, A->accept_rtol, A->dv.norm_den);
+        adj_rb_init_kernel<<<1, 256, 0, A->s>>>(A->rbst, A->parts64, A->nparts64, A->rtol, A->accept_rtol,
+                                                A->dv.norm_den);
         ACK(cudaGetLastError());
-        ACK(adj_rebase(A));   // base quantities of lam_b = 0 (the fold adds zeros)
-        A->launches += 7;
-        const long long per_phase = (long long)A->blocks_per_phase * A->nchk;
-        const long long phases_max = A->p.itmax / std::max<long long>(per_phase, 1) + A->p.itmax / A->nchk + 2;
-        long long launched = 0, batch = 1;
-        while (launched < phases_max) {
-            const long long k = std::min(batch, phases_max - launched);
-            for (long long j = 0; j < k; ++j) {
-                ACK(cudaGraphLaunch(A->gphase, A->s));
-                A->launches += A->kernels_per_phase;
-            }
-            launched += k;
-            ACK(cudaMemcpyAsync(A->h_rbst, A->rbst, sizeof(AdjRbState), cudaMemcpyDeviceToHost, A->s));
-            ACK(cudaStreamSynchronize(A->s));
-            if (A->h_rbst->done) break;
-            batch = std::min<long long>(batch * 2, 16);
-        }
+        ACK(adj_rebase(A, 0, 0));   // base quantities of lam_b = 0 (the fold adds zeros)
+        A->launches += 5;
+        // the whole solve: one graph launch, ended on the device
+        ACK(cudaGraphLaunch(A->gphase, A->s));
+        ACK(cudaMemcpyAsync(A->h_rbst, A->rbst, sizeof(AdjRbState), cudaMemcpyDeviceToHost, A->s));
+        ACK(cudaStreamSynchronize(A->s));
+        A->launches += (long long)A->h_rbst->blocks * (A->nchk + 1) + A->h_rbst->passes + 3LL * A->h_rbst->phases;
         const AdjRbState& rs = *A->h_rbst;
         A->iterations += rs.iter;
         if (adj_iters) adj_iters[n - 1] = rs.iter;
@@ -1118,29 +1281,21 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         }
         // target: rtol * ||g||_rms
         if (A->df64)
-            adj_sumsq_kernel<DF64><<<fill_blocks(), 256, 0, A->s>>>(A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
-                                                              A->g.sy, A->g.sz);
+            adj_sumsq_kernel<DF64><<<(int)A->nparts64, 256, 0, A->s>>>(A->gbuf, A->parts64, A->g.nx, A->g.ny,
+                                                                       A->g.nz, A->g.sy, A->g.sz);
         else
-            adj_sumsq_kernel<F64><<<fill_blocks(), 256, 0, A->s>>>(A->gbuf, &A->st->acc, A->g.nx, A->g.ny, A->g.nz,
-                                                             A->g.sy, A->g.sz);
+            adj_sumsq_kernel<F64><<<(int)A->nparts64, 256, 0, A->s>>>(A->gbuf, A->parts64, A->g.nx, A->g.ny, A->g.nz,
+                                                                      A->g.sy, A->g.sz);
         ACK(cudaGetLastError());
-        adj_target_kernel<<<1, 1, 0, A->s>>>(A->st, A->rtol, A->accept_rtol, A->dv.norm_den, 1e-300);
+        adj_target_kernel<<<1, 256, 0, A->s>>>(A->st, A->parts64, A->nparts64, A->rtol, A->accept_rtol,
+                                               A->dv.norm_den, 1e-300);
         ACK(cudaGetLastError());
         A->launches += 3;
-        long long launched = 0, batch = 1;
-        const long long blocks_max = std::max(1, A->p.itmax / A->nchk);
-        while (launched < blocks_max) {
-            const long long k = std::min(batch, blocks_max - launched);
-            for (long long j = 0; j < k; ++j) {
-                ACK(cudaGraphLaunch(A->graph[(int)(((launched + j) * A->nchk) & 1)], A->s));
-                A->launches += A->nchk + 1;
-            }
-            launched += k;
-            ACK(cudaMemcpyAsync(A->h_st, A->st, sizeof(AdjState), cudaMemcpyDeviceToHost, A->s));
-            ACK(cudaStreamSynchronize(A->s));
-            if (A->h_st->done) break;
-            batch = std::min<long long>(batch * 2, 64);
-        }
+        // the whole solve: one graph launch, ended on the device
+        ACK(cudaGraphLaunch(A->graph[0], A->s));
+        ACK(cudaMemcpyAsync(A->h_st, A->st, sizeof(AdjState), cudaMemcpyDeviceToHost, A->s));
+        ACK(cudaStreamSynchronize(A->s));
+        A->launches += (long long)A->h_st->blocks * (A->nchk + 1);
         const int iters = A->h_st->iter;
         A->iterations += iters;
         if (adj_iters) adj_iters[n - 1] = iters;

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(256) dc1d_kernel(DcArgs a)
     float part = 0.0f;
     unsigned pmax = 0u;
     dc1d_body<MODEL, CHECK>(a, blockIdx.x, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax), a.parts, block_slot());
 }
 
 template <int MODEL, bool CHECK>
@@ -56,8 +56,8 @@ __global__ void __launch_bounds__(256) dc2d_kernel(DcArgs a, int chunk)
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
-    // the body flushes its check partials into a.acc (last step of its march)
-    dc2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+    // the body flushes its check partials into its warp's slot (last step of its march)
+    dc2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax, warp_slot());
 }
 
 // two inner iterations per launch (temporal blocking), see dc2d_tb2_body
@@ -67,8 +67,9 @@ __global__ void __launch_bounds__(256) dc2d_tb2_kernel(DcArgs a, int chunk)
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
-    // the body flushes its check partials into a.acc (last step of its march)
-    dc2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax);
+    // the body flushes its check partials into its warp's slot (last step of its march)
+    dc2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax,
+                                warp_slot());
 }
 
 template <int MODEL, bool CHECK, int R>
@@ -78,15 +79,16 @@ __global__ void __launch_bounds__(32 * R) dc3d_kernel(DcArgs a, int chunk)
     float part = 0.0f;
     unsigned pmax = 0u;
     dc3d_body<MODEL, CHECK, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, chunk, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax));
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax), a.parts, block_slot());
 }
 
 // ---------------------------------------------------------------------------
 // FP64 residual r = -F(H) with both flux terms from H (consistent form of
 // check_res!, scripts/diff_2D_nonlin.jl:41-44), written as FP32 for the
-// inner solve and reduced (sum r^2 or max |r|) in FP64.
+// inner solve and reduced (sum r^2 or max |r|) in FP64 into the block's slot
+// of parts (summed in a fixed order by the outer judge).
 template <int MODEL>
-__global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, float* rf, double* acc,
+__global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, float* rf, double* parts,
                                                          unsigned long long* hmax)
 {
     unsigned long long hm = 0ull;
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(256) dc_resid64_kernel(PTArgs a, int ndim, flo
     }
     hm = warp_max_u64(hm);
     if ((threadIdx.x & 31) == 0 && hm) atomicMax(hmax, hm);
-    block_reduce_residual(acc, a.norm_max, part, pmax);
+    block_reduce_residual(nullptr, a.norm_max, part, pmax, parts, blockIdx.x);
 }
 
 // H += a * delta on every cell (delta is zero on the boundary); refresh the FP32 copy.
@@ -157,10 +159,13 @@ __global__ void dc_tofloat_kernel(const double* src, float* dst, long long n)
 // the inner control block.  The target is max(eta, floor) * err with floor
 // the attainable relative accuracy of an FP32 solve, ~ eps_32 * cond(J),
 // cond(J) ~ 1 + dt * Dmax * sum_d 4/dx_d^2 (Dmax = H_max^3 for D = H^3).
-__global__ void dc_outer_judge_kernel(DcDev* st, double norm_den, int norm_max, double rtol, double tol,
-                                      double cond_scale, double dconst, int nonlin)
+__global__ void __launch_bounds__(256) dc_outer_judge_kernel(DcDev* st, const double* parts, long long nparts,
+                                                             double norm_den, int norm_max, double rtol,
+                                                             double tol, double cond_scale, double dconst,
+                                                             int nonlin)
 {
-    const double acc = st->outer_acc;
+    const double acc = sum_slots(parts, nparts, norm_max);
+    if (threadIdx.x != 0) return;
     st->outer_acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
     st->outer_err = err;
@@ -182,14 +187,19 @@ __global__ void dc_outer_judge_kernel(DcDev* st, double norm_den, int norm_max, 
 // node: it ends the loop when the inner solve stops.  Every pass adds nchk
 // iterations until no further block fits in the solve's budget (cap), so the
 // loop ends within cap/nchk passes.
-__global__ void dc_inner_judge_kernel(DcDev* st, int nchk, double norm_den, int norm_max, int stall,
-                                      cudaGraphConditionalHandle loop)
+__global__ void __launch_bounds__(256) dc_inner_judge_kernel(DcDev* st, const double* parts, long long nparts,
+                                                             int nchk, double norm_den, int norm_max, int stall,
+                                                             cudaGraphConditionalHandle loop)
 {
-    if (st->done) {
-        cudaGraphSetConditional(loop, 0);
+    // every thread reads the flag before thread 0 can change it
+    const bool done = st->done != 0;
+    __syncthreads();
+    if (done) {   // no inner kernel ran: the slots are stale
+        if (threadIdx.x == 0) cudaGraphSetConditional(loop, 0);
         return;
     }
-    const double acc = st->acc;
+    const double acc = sum_slots(parts, nparts, norm_max);
+    if (threadIdx.x != 0) return;
     st->acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den);
     st->err = err;
@@ -246,6 +256,10 @@ struct DcState {
     double rtol = 1e-3;
     int max_outer = 30;
     int stall = 6;             // inner stagnation window, in checks
+    double* parts = nullptr;   // check-residual slots of the inner check launches
+    long long nparts = 0;
+    double* parts64 = nullptr; // FP64 residual slots of dc_resid64_kernel (one per block)
+    long long nparts64 = 0;
     DcCounters k;
     ptd_ctx_base g;
 };
@@ -311,7 +325,46 @@ static void dc_args(const DcState* dc, int parity, const int* done, DcArgs& a)
     a.r = dc->rf;
     a.done = done;
     a.acc = &dc->dev->acc;
+    a.parts = dc->parts;
     a.norm_max = dc->p.norm == PTD_NORM_MAX;
+}
+
+// Residual slots of an inner check launch with the current launch shape.
+static long long dc_check_slots(const DcState* dc)
+{
+    const LaunchCfg& c = dc->cfg;
+    if (dc->ndim == 1) return (dc->g.nx + 255) / 256;
+    if (dc->ndim == 2) {
+        const long long tiles = dc->tb == 2 ? (dc->g.nx - 2 + 27) / 28 : (dc->g.nx - 2 + 30) / 31;
+        const int W = c.warps2d;
+        return (tiles + W - 1) / W * W * (long long)((dc->g.ny - 2 + c.chunk2d - 1) / c.chunk2d);
+    }
+    return (long long)((dc->g.nx - 2 + 30) / 31) * ((dc->g.ny - 2 + 14) / 15) *
+           ((dc->g.nz - 2 + c.chunk3d - 1) / c.chunk3d);
+}
+
+// (Re)allocate the residual slots for the current launch shape.
+static int dc_alloc_parts(DcState* dc)
+{
+    const long long n = dc_check_slots(dc);
+    if (n > dc->nparts) {
+        cudaFree(dc->parts);
+        dc->parts = nullptr;
+        dc->nparts = 0;
+        if (cudaMalloc((void**)&dc->parts, (size_t)n * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(PTD_ENOMEM, "dc: cudaMalloc failed");
+        }
+    }
+    dc->nparts = n;
+    if (!dc->parts64) {
+        dc->nparts64 = fill_blocks();
+        if (cudaMalloc((void**)&dc->parts64, (size_t)dc->nparts64 * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(PTD_ENOMEM, "dc: cudaMalloc failed");
+        }
+    }
+    return PTD_OK;
 }
 
 #define DCK(call)                                                 \
@@ -363,8 +416,8 @@ static int dc_capture(DcState* dc, int parity)
             ++nk;
         }
         if (err == cudaSuccess) {
-            dc_inner_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->nchk, dc->dv.norm_den, dc->p.norm == PTD_NORM_MAX,
-                                                       dc->stall, loop);
+            dc_inner_judge_kernel<<<1, 256, 0, dc->s>>>(dc->dev, dc->parts, dc->nparts, dc->nchk, dc->dv.norm_den,
+                                                         dc->p.norm == PTD_NORM_MAX, dc->stall, loop);
             err = cudaGetLastError();
             ++nk;
         }
@@ -430,6 +483,7 @@ int dc_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
         if (e == cudaSuccess) e = cudaMemsetAsync(dc->zero_flag, 0, sizeof(int), s);
         if (e != cudaSuccess) rc = cuda_fail(e, "dc: cudaMemsetAsync");
     }
+    if (!rc) rc = dc_alloc_parts(dc);
     for (int q = 0; q < 2 && !rc; ++q) rc = dc_capture(dc, q);
     if (rc) {
         dc_destroy(dc);
@@ -454,6 +508,8 @@ void dc_destroy(DcState* dc)
     cudaFree(dc->Df);
     cudaFree(dc->dev);
     cudaFree(dc->zero_flag);
+    cudaFree(dc->parts);
+    cudaFree(dc->parts64);
     if (dc->h_dev) cudaFreeHost(dc->h_dev);
     delete dc;
 }
@@ -490,18 +546,19 @@ static int dc_residual(DcState* dc, double eta, double* err)
     a.Hin = dc->H;
     a.Hold = dc->Hold;
     a.D = dc->D;
-    const int nb = fill_blocks();
+    const int nb = (int)dc->nparts64;   // one slot per block
     unsigned long long* hm = &dc->dev->hmax_bits;
-    if (dc->model == LIN) dc_resid64_kernel<LIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc, hm);
+    if (dc->model == LIN) dc_resid64_kernel<LIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, dc->parts64, hm);
     else if (dc->model == LINSTEP)
-        dc_resid64_kernel<LINSTEP><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc, hm);
-    else dc_resid64_kernel<NONLIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, &dc->dev->outer_acc, hm);
+        dc_resid64_kernel<LINSTEP><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, dc->parts64, hm);
+    else dc_resid64_kernel<NONLIN><<<nb, 256, 0, dc->s>>>(a, dc->ndim, dc->rf, dc->parts64, hm);
     DCK(cudaGetLastError());
     double cond_scale = 0.0;
     for (int d = 0; d < dc->ndim; ++d) cond_scale += 4.0 / (dc->dv.h[d] * dc->dv.h[d]);
     cond_scale *= dc->p.dt;
-    dc_outer_judge_kernel<<<1, 1, 0, dc->s>>>(dc->dev, dc->dv.norm_den, dc->p.norm == PTD_NORM_MAX, eta,
-                                              kDcStop * dc->p.tol, cond_scale, dc->p.D, dc->model == NONLIN);
+    dc_outer_judge_kernel<<<1, 256, 0, dc->s>>>(dc->dev, dc->parts64, dc->nparts64, dc->dv.norm_den,
+                                                dc->p.norm == PTD_NORM_MAX, eta, kDcStop * dc->p.tol, cond_scale,
+                                                dc->p.D, dc->model == NONLIN);
     DCK(cudaGetLastError());
     dc->k.launches += 2;
     DCK(cudaMemcpyAsync(dc->h_dev, dc->dev, sizeof(DcDev), cudaMemcpyDeviceToHost, dc->s));
@@ -605,7 +662,10 @@ int dc_step(DcState* dc, const ptd_ctx_base& g, int32_t* iters, double* err_hist
 
 int dc_set_config(DcState* dc, const LaunchCfg& cfg)
 {
+    DCK(cudaStreamSynchronize(dc->s));   // the slots may be reallocated
     dc->cfg = cfg;
+    const int rc = dc_alloc_parts(dc);
+    if (rc) return rc;
     for (int q = 0; q < 2; ++q) {
         if (dc->gblock[q]) cudaGraphExecDestroy(dc->gblock[q]);
         dc->gblock[q] = nullptr;

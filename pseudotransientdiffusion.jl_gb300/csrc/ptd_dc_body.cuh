@@ -25,6 +25,7 @@ struct DcArgs {
     const float* r;       // FP32 copy of the FP64 residual
     const int* done;
     double* acc;
+    double* parts;        // check-residual slots (fixed-order sum), or null: atomics into acc
     int norm_max;
 };
 
@@ -138,7 +139,7 @@ __device__ __forceinline__ void dc1d_body(const DcArgs& a, int bx, float& part, 
 
 template <int MODEL, bool CHECK>
 __device__ __forceinline__ void dc2d_body(const DcArgs& a, int tile, int cy, int chunk, float& part,
-                                          unsigned& pmax)
+                                          unsigned& pmax, long long slot = 0)
 {
     const int lane = threadIdx.x;
     const int i = 31 * tile + lane;
@@ -199,8 +200,10 @@ __device__ __forceinline__ void dc2d_body(const DcArgs& a, int tile, int cy, int
                 Db = Dc;
                 Dc = Dn;
             }
-            if (CHECK && j == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane);
+            if (CHECK && j == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
         }
+    } else if (CHECK && a.parts && lane == 0) {
+        a.parts[slot] = 0.0;
     }
 }
 
@@ -244,14 +247,17 @@ __device__ __forceinline__ float dc_star(float Dc, float Db, float Dn)
 
 template <int MODEL, bool CHECK>
 __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy, int chunk, float& part,
-                                              unsigned& pmax)
+                                              unsigned& pmax, long long slot = 0)
 {
     constexpr bool LS = MODEL == LINSTEP;
     const int lane = threadIdx.x;
     const int nx = a.nx, ny = a.ny;
     const int j0 = 1 + cy * chunk;
     const int j1 = min(j0 + chunk, ny - 1);
-    if (28 * tile >= nx - 2 || j0 >= j1) return;   // uniform over the warp
+    if (28 * tile >= nx - 2 || j0 >= j1) {   // uniform over the warp
+        if (CHECK && a.parts && lane == 0) a.parts[slot] = 0.0;
+        return;
+    }
     const int i = 28 * tile + lane - 1;
     const int ic = min(max(i, 0), nx - 1);          // clamped column of this lane's loads
     const bool colin = i >= 1 && i <= nx - 2;       // interior column
@@ -374,7 +380,7 @@ __device__ __forceinline__ void dc2d_tb2_body(const DcArgs& a, int tile, int cy,
         D0 = D1;
         D1 = D2;
         r0 = r1;
-        if (CHECK && s == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane);
+        if (CHECK && s == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
     }
 }
 

@@ -276,8 +276,9 @@ __device__ __forceinline__ unsigned long long widen_max32(unsigned mx)
 // of their y march, with all 32 lanes converged: a reduction after the march
 // made ptxas give their check variants 52-98 registers (32-40 this way),
 // halving the resident warps of a latency-bound kernel.
+// With parts, the warp's result goes into its own slot parts[slot] instead.
 __device__ __forceinline__ void warp_flush_residual32(double* acc, int norm_max, float part_sum, unsigned part_max,
-                                                      int lane)
+                                                      int lane, double* parts = nullptr, long long slot = 0)
 {
     if (norm_max) {
 #pragma unroll
@@ -285,11 +286,55 @@ __device__ __forceinline__ void warp_flush_residual32(double* acc, int norm_max,
             const unsigned w = __shfl_xor_sync(FULL, part_max, o);
             part_max = w > part_max ? w : part_max;
         }
-        if (lane == 0 && part_max) atomicMax(reinterpret_cast<unsigned long long*>(acc), widen_max32(part_max));
+        if (lane == 0 && parts) parts[slot] = __longlong_as_double((long long)widen_max32(part_max));
+        else if (lane == 0 && part_max) atomicMax(reinterpret_cast<unsigned long long*>(acc), widen_max32(part_max));
     } else {
         const double v = warp_sum((double)part_sum);
-        if (lane == 0) atomicAdd(acc, v);
+        if (lane == 0 && parts) parts[slot] = v;
+        else if (lane == 0) atomicAdd(acc, v);
     }
+}
+
+// Slot of this warp (2D kernels: warps numbered x fastest) / block (1D, 3D)
+// in a residual-slot array.
+__device__ __forceinline__ long long warp_slot()
+{
+    return ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.y + threadIdx.y;
+}
+__device__ __forceinline__ long long block_slot()
+{
+    return ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+
+// Fixed-order sum (or max, for the max-norm bit patterns) of nparts slots by a
+// block of 256 threads: thread t takes slots t, t + 256, ... in order, then a
+// fixed tree over the threads.  Every thread returns the result.
+__device__ __forceinline__ double sum_slots(const double* parts, long long nparts, int norm_max)
+{
+    __shared__ double s_sum[256];
+    __shared__ unsigned long long s_max[256];
+    const int t = threadIdx.x;
+    double sum = 0.0;
+    unsigned long long mx = 0ull;
+    for (long long i = t; i < nparts; i += 256) {
+        const double v = parts[i];
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        mx = bits > mx ? bits : mx;
+        sum += v;
+    }
+    s_sum[t] = sum;
+    s_max[t] = mx;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) {
+            s_sum[t] += s_sum[t + o];
+            s_max[t] = s_max[t + o] > s_max[t] ? s_max[t + o] : s_max[t];
+        }
+        __syncthreads();
+    }
+    const double r = norm_max ? __longlong_as_double((long long)s_max[0]) : s_sum[0];
+    __syncthreads();
+    return r;
 }
 
 // FP64 form of warp_flush_residual32 for the 2D kernels whose check partials

@@ -11,17 +11,6 @@
 
 namespace ptd {
 
-// Slot of this warp (2D: warps numbered x fastest) / block (1D, 3D) in
-// RbArgs::parts.
-__device__ __forceinline__ long long warp_slot()
-{
-    return ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.y + threadIdx.y;
-}
-__device__ __forceinline__ long long block_slot()
-{
-    return ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-}
-
 template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) rb1d_kernel(RbArgs a)
 {
@@ -119,46 +108,68 @@ __global__ void __launch_bounds__(256) rb_base_kernel(RbBaseArgs b, const RbDev*
 
 __global__ void rb_reset_kernel(RbDev* st) { rb_reset(st); }
 
-// After each block of nchk iterations: the FP32 check err (rb_check_judge).
+// After each block of nchk iterations: the FP32 check err (rb_check_judge),
+// and whether the FP64 rebase that follows the block in the step graph runs
+// (the condition of its IF node: the phase is over).
 __global__ void __launch_bounds__(256) rb_check_judge_kernel(RbDev* st, const double* parts, long long nparts,
                                                              double* errhist, int errcap, int nchk, int itmax,
-                                                             double tol, double norm_den, int norm_max)
+                                                             double tol, double norm_den, int norm_max,
+                                                             int phase_cap, cudaGraphConditionalHandle rebase)
 {
-    if (st->skip || st->step_done) return;   // no PT kernel ran: the slots are stale
+    // every thread reads the flags before thread 0 can change them
+    const bool idle = st->skip || st->step_done;
+    __syncthreads();
+    if (idle) {   // no PT kernel ran: the slots are stale
+        if (threadIdx.x == 0) {
+            st->blocks += 1;
+            cudaGraphSetConditional(rebase, 0);
+        }
+        return;
+    }
     const double acc = sum_slots(parts, nparts, norm_max);
     if (threadIdx.x == 0) {
+        st->blocks += 1;
         st->acc = acc;
-        rb_check_judge(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max);
+        rb_check_judge(st, errhist, errcap, nchk, itmax, tol, norm_den, norm_max, phase_cap);
+        cudaGraphSetConditional(rebase, st->skip ? 1 : 0);
     }
 }
 
-// After each rebase: the FP64 err of the base (rb_base_judge).  In the body of
-// the step graph's WHILE node (in_loop) it also counts the phase and ends the
-// loop once the step has stopped.  Every phase adds at least one check block
-// of nchk iterations (its first judge runs with skip clear) and a phase that
-// leaves no room for another block before itmax ends the step (capped), so
-// the loop ends within itmax/nchk passes.
+// After each rebase: the FP64 err of the base (rb_base_judge); inside the
+// step graph (in_loop) it also counts the phase.  Every phase adds at least
+// one check block of nchk iterations (its first judge runs with skip clear)
+// and a phase that leaves no room for another block before itmax ends the
+// step (capped), so the step graph's loop ends within itmax/nchk passes.
 __global__ void __launch_bounds__(256) rb_base_judge_kernel(RbDev* st, const double* parts, long long nparts,
-                                                            double tol, double norm_den, int norm_max,
-                                                            cudaGraphConditionalHandle loop, int in_loop)
+                                                            double tol, double norm_den, int norm_max, int in_loop)
 {
     // every thread reads step_done before thread 0 can change it
     const bool stopped = st->step_done != 0;
     __syncthreads();
     if (stopped) {   // the base kernel did not run: the slots are stale
-        if (threadIdx.x == 0 && in_loop) {
-            st->phases += 1;
-            cudaGraphSetConditional(loop, 0);
-        }
+        if (threadIdx.x == 0 && in_loop) st->phases += 1;
         return;
     }
     const double acc = sum_slots(parts, nparts, norm_max);
     if (threadIdx.x == 0) {
         if (in_loop) st->phases += 1;
         st->acc64 = acc;
-        const int done = rb_base_judge(st, tol, norm_den, norm_max);
-        if (in_loop && done) cudaGraphSetConditional(loop, 0);
+        rb_base_judge(st, tol, norm_den, norm_max);
     }
+}
+
+// Last node of the step graph's loop body (at the body's own level, where the
+// loop's condition is set): ends the loop once the step has stopped.  Every
+// pass of a running step adds a check block, so a step still running after
+// max_passes passes (itmax/nchk + 2) has lost its stop: it ends as capped.
+__global__ void rb_loop_judge_kernel(RbDev* st, int max_passes, cudaGraphConditionalHandle loop)
+{
+    st->passes += 1;
+    if (!st->step_done && st->passes > max_passes) {
+        st->step_done = DONE_CAP;
+        st->skip = 1;
+    }
+    if (st->step_done) cudaGraphSetConditional(loop, 0);
 }
 
 __global__ void rb_tofloat_kernel(const double* src, float* dst, long long n)
@@ -195,10 +206,11 @@ struct RbState {
     long long nparts = 0;
     double* parts64 = nullptr;                    // FP64 residual slots of the base kernel
     long long nparts64 = 0;
-    int blocks_per_phase = 1;
+    int phase_iters = 200;                        // PT iterations of a phase at most
     int tblk = 1;                                 // iterations per launch (2: temporal blocking, 2D)
     cudaGraphExec_t gphase = nullptr;
-    int kernels_per_phase = 0;
+    int kernels_per_block = 0;                    // PT launches and check judge of one check block
+    int blocks_per_pass = 1;                      // check blocks per pass of the step graph's loop
     DcCounters k;
 };
 
@@ -425,53 +437,97 @@ int rb_capture(RbState* rb)
         return cuda_fail(err, "conditional graph node");
     }
     cudaGraph_t body = np.conditional.phGraph_out[0];
-    err = cudaStreamBeginCaptureToGraph(rb->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-    if (err != cudaSuccess) {
-        cudaGraphDestroy(g);
-        return cuda_fail(err, "cudaStreamBeginCaptureToGraph");
-    }
-    int par = 0, nk = 0;
+    // The loop body: one check block (nchk/tb launches and the check judge)
+    // followed by an IF node holding the FP64 rebase (fold, base quantities,
+    // base judge), which runs when the judge has ended the phase; two such
+    // blocks when the launch count is odd, so that every pass starts on
+    // buffer parity 0; last, the loop judge.  No launch is issued past the
+    // end of a phase.
     const int nchk = rb->p.nchk;
     const int nl = nchk / rb->tblk;   // launches per check block (tb divides nchk)
-    for (int b = 0; b < rb->blocks_per_phase && err == cudaSuccess; ++b) {
+    const int nblk = (nl & 1) ? 2 : 1;
+    int par = 0;
+    cudaGraphNode_t prev = nullptr;   // the previous block's IF node
+    for (int b = 0; b < nblk && err == cudaSuccess; ++b) {
+        cudaGraphConditionalHandle rebase;
+        err = cudaGraphConditionalHandleCreate(&rebase, body, 0, cudaGraphCondAssignDefault);
+        if (err == cudaSuccess)
+            err = cudaStreamBeginCaptureToGraph(rb->s, body, prev ? &prev : nullptr, nullptr, prev ? 1 : 0,
+                                                cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) break;
         for (int it = 0; it < nl && err == cudaSuccess; ++it) {
             RbArgs a;
             rb_args(rb, par, &rb->dev->skip, a);
             err = rb_launch(a, rb->p.ndim, rb->p.model, it == nl - 1, rb->cfg, rb->s, rb->tblk);
             par ^= 1;
-            ++nk;
         }
         if (err == cudaSuccess) {
             rb_check_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts, rb->nparts, rb->errhist, rb->errcap, nchk,
                                                         rb->p.itmax, rb->p.tol, rb->dv.norm_den,
-                                                        rb->p.norm == PTD_NORM_MAX);
+                                                        rb->p.norm == PTD_NORM_MAX, rb->phase_iters, rebase);
             err = cudaGetLastError();
-            ++nk;
         }
-    }
-    if (err == cudaSuccess) {
-        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, -1, rb->tblk);
+        // the judge is the capture's last node: the IF node follows it
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaError_t e1 = cudaStreamGetCaptureInfo(rb->s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        cudaGraphNode_t leaf = (e1 == cudaSuccess && nd == 1) ? deps[0] : nullptr;
+        cudaGraph_t captured = body;
+        cudaError_t e2 = cudaStreamEndCapture(rb->s, &captured);
+        if (err == cudaSuccess) err = e1 != cudaSuccess ? e1 : e2;
+        if (err == cudaSuccess && !leaf) err = cudaErrorStreamCaptureInvalidated;
+        cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
+        ip.conditional.handle = rebase;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        cudaGraphNode_t ifn = nullptr;
+        if (err == cudaSuccess) err = cudaGraphAddNode(&ifn, body, &leaf, nullptr, 1, &ip);
+        if (err == cudaSuccess)
+            err = cudaStreamBeginCaptureToGraph(rb->s, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) break;
+        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, rb->tblk);
         err = cudaGetLastError();
+        if (err == cudaSuccess) {
+            rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
+            err = cudaGetLastError();
+        }
+        if (err == cudaSuccess) {
+            rb_base_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts64, rb->nparts64, rb->p.tol,
+                                                       rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX, 1);
+            err = cudaGetLastError();
+        }
+        cudaGraph_t ifbody = ip.conditional.phGraph_out[0];
+        e2 = cudaStreamEndCapture(rb->s, &ifbody);
+        if (err == cudaSuccess) err = e2;
+        prev = ifn;
     }
+    // the loop's condition, set at the body's level after the last rebase node
+    if (err == cudaSuccess)
+        err = cudaStreamBeginCaptureToGraph(rb->s, body, &prev, nullptr, 1, cudaStreamCaptureModeThreadLocal);
     if (err == cudaSuccess) {
-        rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
+        rb_loop_judge_kernel<<<1, 1, 0, rb->s>>>(rb->dev, rb->p.itmax / nchk + 2, loop);
         err = cudaGetLastError();
+        cudaGraph_t captured = body;
+        const cudaError_t e4 = cudaStreamEndCapture(rb->s, &captured);
+        if (err == cudaSuccess) err = e4;
     }
-    if (err == cudaSuccess) {
-        rb_base_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts64, rb->nparts64, rb->p.tol, rb->dv.norm_den,
-                                                   rb->p.norm == PTD_NORM_MAX, loop, 1);
-        err = cudaGetLastError();
-    }
-    nk += 3;
-    cudaError_t e2 = cudaStreamEndCapture(rb->s, &body);
-    if (err != cudaSuccess || e2 != cudaSuccess) {
+    if (err != cudaSuccess) {
+        cudaStreamCaptureStatus cs;
+        if (cudaStreamIsCapturing(rb->s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            cudaGraph_t dropped = nullptr;
+            cudaStreamEndCapture(rb->s, &dropped);
+        }
+        cudaGetLastError();
         cudaGraphDestroy(g);
-        return cuda_fail(err != cudaSuccess ? err : e2, "capture rebased phase");
+        return cuda_fail(err, "capture rebased step");
     }
     cudaError_t e3 = cudaGraphInstantiate(&rb->gphase, g, 0);
     cudaGraphDestroy(g);
     if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
-    rb->kernels_per_phase = nk;
+    rb->kernels_per_block = nl + 1;
+    rb->blocks_per_pass = nblk;
     return PTD_OK;
 }
 
@@ -487,8 +543,12 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
     rb->g = g;
     rb->s = s;
     rb->cfg = tuned_config(p);
-    // a phase: the check blocks of ~200 PT iterations between two FP64 rebases
-    rb->blocks_per_phase = std::max(1, (200 + p.nchk - 1) / p.nchk);
+    // a phase: the check blocks between two FP64 rebases, ~200 PT iterations
+    // at most.  Longer phases cost iterations: with 1000 the 2D 4096^2 steps
+    // took 6900 / 6100 / 5800 / 5700 / 5500 PT iterations against FP64's 6500
+    // / 5800 / 5600 / 5500 / 5300, the 3D 512^3 steps 1450 / 1370 / 1330
+    // against 790 / 700 / 680; without the cap the 2D steps did not converge.
+    rb->phase_iters = std::max(p.nchk, 200);
     // two iterations per launch with an even check cadence: 2D (every model),
     // and 3D (LIN, NONLIN) when asked for (PTD_FLAG_RB_TBLOCK_3D: at 512^3
     // 1233 against 1243 us per iteration, issue-bound at half the bytes)
@@ -601,7 +661,7 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
     rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
     RCK(cudaGetLastError());
     rb_base_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts64, rb->nparts64, rb->p.tol, rb->dv.norm_den,
-                                               rb->p.norm == PTD_NORM_MAX, cudaGraphConditionalHandle{}, 0);
+                                               rb->p.norm == PTD_NORM_MAX, 0);
     RCK(cudaGetLastError());
     rb->k.launches += 3;
     rb->h_dev->step_done = DONE_RUNNING;
@@ -612,7 +672,8 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
         RCK(cudaGraphLaunch(rb->gphase, rb->s));
         RCK(cudaMemcpyAsync(rb->h_dev, rb->dev, sizeof(RbDev), cudaMemcpyDeviceToHost, rb->s));
         RCK(cudaStreamSynchronize(rb->s));
-        rb->k.launches += (long long)rb->h_dev->phases * rb->kernels_per_phase;
+        rb->k.launches += (long long)rb->h_dev->blocks * rb->kernels_per_block +
+                          rb->h_dev->blocks / rb->blocks_per_pass + 3LL * rb->h_dev->phases;
     }
     const RbDev& st = *rb->h_dev;
     int32_t iter = st.iter;

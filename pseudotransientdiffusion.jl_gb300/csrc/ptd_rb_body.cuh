@@ -74,7 +74,9 @@ struct RbDev {
     int phase_iter;   // PT iterations of this phase (the buffer parity)
     int nchecks;
     int capped;
-    int phases;       // phases run in this step (passes of the step graph's loop)
+    int phases;       // phases run in this step (FP64 rebases inside the step graph)
+    int blocks;       // check blocks run in this step (one-grid solver)
+    int passes;       // passes of the step graph's loop (one-grid solver)
     int pad1;
     double acc;       // FP32 check residual accumulator (sum or max bits)
     double acc64;     // FP64 base residual accumulator
@@ -876,15 +878,18 @@ struct RbFoldArgs {
 
 __device__ __forceinline__ void rb_fold_elem(const RbFoldArgs& f, int parity, long long t)
 {
+    // both buffers cleared: the next iteration may start on either parity
     const float* dp = parity ? f.d[1] : f.d[0];
     f.H[t] += (double)dp[t];
     f.d[0][t] = 0.0f;
+    f.d[1][t] = 0.0f;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         if (d < f.ndim) {
             const float* wp = parity ? f.w[d][1] : f.w[d][0];
             f.wb[d][t] += (double)wp[t];
             f.w[d][0][t] = 0.0f;
+            f.w[d][1][t] = 0.0f;
         }
     }
 }
@@ -963,9 +968,11 @@ __device__ __forceinline__ void rb_base_cell(const RbBaseArgs& b, int ix, int iy
 // FP32 check err; the phase ends (skip) to confirm err <= tol in FP64, or once
 // it has reduced the residual well below its start (the FP32 base quantities
 // carry rounding relative to the phase-start residual, which bounds what a
-// phase attains), or when no further check block fits before itmax.
+// phase attains), after phase_cap iterations, or when no further check block
+// fits before itmax.
 __device__ __forceinline__ void rb_check_judge(RbDev* st, double* errhist, int errcap, int nchk, int itmax,
-                                               double tol, double norm_den, int norm_max)
+                                               double tol, double norm_den, int norm_max,
+                                               int phase_cap = 0x7fffffff)
 {
     if (st->skip || st->step_done) return;
     const double acc = st->acc;
@@ -982,7 +989,7 @@ __device__ __forceinline__ void rb_check_judge(RbDev* st, double* errhist, int e
         st->skip = 1;
         return;
     }
-    if (!(err > tol) || err <= 1e-4 * st->err64) st->skip = 1;
+    if (!(err > tol) || err <= 1e-4 * st->err64 || st->phase_iter >= phase_cap) st->skip = 1;
     if (st->iter + nchk > itmax) {    // no further check block fits
         st->skip = 1;
         st->capped = 1;
@@ -1013,37 +1020,6 @@ __device__ __forceinline__ int rb_base_judge(RbDev* st, double tol, double norm_
     return st->step_done;
 }
 
-// The sum (or max) of nparts check-residual slots in a fixed order, by one
-// block of 256 threads: thread t takes slots t, t + 256, ... in order, then a
-// fixed tree over the threads.  Every thread returns the result.
-__device__ __forceinline__ double sum_slots(const double* parts, long long nparts, int norm_max)
-{
-    __shared__ double s_sum[256];
-    __shared__ unsigned long long s_max[256];
-    const int t = threadIdx.x;
-    double sum = 0.0;
-    unsigned long long mx = 0ull;
-    for (long long i = t; i < nparts; i += 256) {
-        const double v = parts[i];
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-        mx = bits > mx ? bits : mx;
-        sum += v;
-    }
-    s_sum[t] = sum;
-    s_max[t] = mx;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (t < o) {
-            s_sum[t] += s_sum[t + o];
-            s_max[t] = s_max[t + o] > s_max[t] ? s_max[t + o] : s_max[t];
-        }
-        __syncthreads();
-    }
-    const double r = norm_max ? __longlong_as_double((long long)s_max[0]) : s_sum[0];
-    __syncthreads();
-    return r;
-}
-
 __device__ __forceinline__ void rb_reset(RbDev* st)
 {
     st->skip = 0;
@@ -1053,6 +1029,8 @@ __device__ __forceinline__ void rb_reset(RbDev* st)
     st->nchecks = 0;
     st->capped = 0;
     st->phases = 0;
+    st->blocks = 0;
+    st->passes = 0;
     st->acc = 0.0;
     st->acc64 = 0.0;
     st->err = 0.0;

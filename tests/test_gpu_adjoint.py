@@ -84,3 +84,55 @@ def test_torch_autograd_function():
         gm, gh = A.gradient()
     assert np.allclose(mt.grad.cpu().numpy().transpose(2, 1, 0), gm)
     assert np.allclose(h0.grad.cpu().numpy().transpose(2, 1, 0), gh)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_rb"])
+def test_adjoint_odd_check_cadence_matches_reference_adjoint(prec):
+    """An odd check cadence: every pass of a solve graph's loop holds two check
+    blocks, so that each pass starts on the same buffer parity."""
+    shape = (14, 13, 12)
+    s, H0, m, Ht = problem(shape)
+    with ptdiff.AdjointSolver(ptdiff.make_params(s, shape, precision=prec, nchk=7)) as A:
+        A.forward(H0, m, Ht)
+        gm, gh = A.gradient()
+    Hs = O.forward_checkpoints(s, H0, m)
+    gm_r, gh_r, st = O.adjoint(s, Hs, Ht, m)
+    assert st == 0
+    assert np.linalg.norm(gm - gm_r) <= 1e-6 * np.linalg.norm(gm_r)
+    assert np.linalg.norm(gh - gh_r) <= 1e-6 * np.linalg.norm(gh_r)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "df64", "fp32_rb"])
+def test_adjoint_is_deterministic(prec):
+    """Every norm of the adjoint (check residuals, right-hand sides, rebase
+    residuals, the loss) is summed from per-CTA slots in a fixed order: two
+    gradient evaluations agree bit for bit."""
+    shape = (14, 13, 12)
+    s, H0, m, Ht = problem(shape)
+    out = []
+    for _ in range(2):
+        with make(s, shape, prec) as A:
+            loss = A.forward(H0, m, Ht)
+            gm, gh = A.gradient()
+            out.append((loss, gm, gh, list(A.adjoint_iters)))
+    (l1, m1, h1, i1), (l2, m2, h2, i2) = out
+    assert l1 == l2 and i1 == i2
+    assert np.array_equal(m1, m2) and np.array_equal(h1, h2)
+
+
+@pytest.mark.parametrize("prec,nchk", [("fp64", 10), ("fp32_rb", 10), ("fp64", 7), ("fp32_rb", 7)])
+def test_adjoint_solves_launch_no_block_past_their_stop(prec, nchk):
+    """Each adjoint solve is one graph launch whose loop the device ends: the
+    PT launches of a gradient are its iterations plus at most one idle check
+    block per solve (odd cadences), with a few bookkeeping kernels per check
+    block and per step."""
+    shape = (14, 13, 12)
+    s, H0, m, Ht = problem(shape)
+    with ptdiff.AdjointSolver(ptdiff.make_params(s, shape, precision=prec, nchk=nchk)) as A:
+        A.forward(H0, m, Ht)
+        l0, _ = A.counters()
+        A.gradient()
+        l1, _ = A.counters()
+        its = [int(v) for v in A.adjoint_iters]
+    per_step = [it + (it // nchk + 1) * 5 + nchk + 10 for it in its]
+    assert 0 < l1 - l0 <= sum(per_step), (l1 - l0, its)

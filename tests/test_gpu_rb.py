@@ -230,7 +230,9 @@ def test_rebased_fp32_temporal_blocking_expm_and_iterate():
     ("fp64", "2d_nonlin_4096", (384, 384)), ("dfh", "2d_nonlin_4096", (384, 384)),
     ("fp64", "3d_nonlin_512", (64, 64, 64)), ("df64", "3d_nonlin_512", (64, 64, 64)),
     ("fp32_rb", "2d_nonlin_4096", (384, 384)), ("fp32_rb", "3d_nonlin_512", (64, 64, 64)),
-    ("fp32_rb", "1d_lin_512", (512,))])
+    ("fp32_rb", "1d_lin_512", (512,)),
+    ("fp32_dc", "2d_nonlin_4096", (384, 384)), ("fp32_dc", "3d_nonlin_512", (64, 64, 64)),
+    ("fp32_dc", "1d_lin_512", (512,))])
 def test_check_residual_is_deterministic(prec, name, shape):
     """The check residual is summed from per-warp / per-block slots in a fixed
     order: two solves of the same problem give the same error history bit for
