@@ -70,6 +70,23 @@ struct BDev {
     double dconst;       // Dmax of the linear models
 };
 
+// The sum (or max) of slots first .. first+count-1 by one warp, in a fixed
+// order: lane l takes slots first+l, first+l+32, ... in order, then a fixed
+// shuffle tree.  Every lane returns the result.
+__device__ __forceinline__ double warp_sum_range(const double* parts, long long first, long long count, int norm_max)
+{
+    const int lane = threadIdx.x & 31;
+    double sum = 0.0;
+    unsigned long long mx = 0ull;
+    for (long long k = first + lane; k < first + count; k += 32) {
+        const double v = parts[k];
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        mx = bits > mx ? bits : mx;
+        sum += v;
+    }
+    return norm_max ? __longlong_as_double((long long)warp_max_u64(mx)) : warp_sum(sum);
+}
+
 // ---------------------------------------------------------------------------
 template <class N, int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) pt2d_batch_kernel(const PTArgs* __restrict__ tab,
@@ -80,18 +97,24 @@ __global__ void __launch_bounds__(256) pt2d_batch_kernel(const PTArgs* __restric
     if (step_done(a.done)) return;
     double part = 0.0;
     unsigned long long pmax = 0ull;
-    // the body flushes its check partials into a.acc (last step of its march)
-    pt2d_body<N, MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    // the body flushes its check partials into its warp's slot (work item k,
+    // warp w -> k * W + w; last step of its march)
+    pt2d_body<N, MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax,
+                               (long long)blockIdx.x * blockDim.y + threadIdx.y);
 }
 
+// The check of every running instance (one warp each), its residual summed
+// from its warps' slots (work items wfirst .. wfirst+wcount-1, W warps each)
+// in a fixed order.
 __global__ void judge_batch_kernel(DevState* st, int ninst, int nchk, int itmax, double tol,
-                                   const double* norm_den, int norm_max)
+                                   const double* norm_den, int norm_max, const double* parts, const int* wfirst,
+                                   const int* wcount, int W)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ninst) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= ninst || st[i].done) return;   // uniform over the warp; no iteration ran
+    const double acc = warp_sum_range(parts, (long long)wfirst[i] * W, (long long)wcount[i] * W, norm_max);
+    if ((threadIdx.x & 31) != 0) return;
     DevState& s = st[i];
-    if (s.done) return;
-    const double acc = s.acc;
     s.acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(norm_den[i]);
     s.nchecks += 1;
@@ -99,6 +122,24 @@ __global__ void judge_batch_kernel(DevState* st, int ninst, int nchk, int itmax,
     s.err = err;
     if (!(err > tol)) s.done = (err != err) ? DONE_NAN : DONE_CONVERGED;
     else if (s.iter + nchk > itmax) s.done = DONE_CAP;
+}
+
+// Last node of a pass of a batch solve graph's loop (one block): ends the loop
+// once no instance is running; every pass adds a check block to each running
+// instance and an instance with no room for another before itmax stops, so
+// the loop ends within itmax/nchk + 1 passes (max_passes: a bound kept all
+// the same).
+template <class S>
+__global__ void __launch_bounds__(256) batch_loop_judge_kernel(const S* st, int ninst, int* passes, int max_passes,
+                                                               cudaGraphConditionalHandle loop)
+{
+    int running = 0;
+    for (int i = threadIdx.x; i < ninst; i += blockDim.x) running |= st[i].done == 0;
+    const int any = __syncthreads_or(running);
+    if (threadIdx.x == 0) {
+        *passes += 1;
+        if (!any || *passes >= max_passes) cudaGraphSetConditional(loop, 0);
+    }
 }
 
 __global__ void reset_batch_kernel(DevState* st, int ninst)
@@ -122,8 +163,9 @@ __global__ void __launch_bounds__(256) dc2d_batch_kernel(const DcArgs* __restric
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
-    // the body flushes its check partials into a.acc (last step of its march)
-    dc2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    // the body flushes its check partials into its warp's slot (last step of its march)
+    dc2d_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax,
+                            (long long)blockIdx.x * blockDim.y + threadIdx.y);
 }
 
 // two inner iterations per launch (temporal blocking, ptd_dc_body.cuh)
@@ -136,17 +178,21 @@ __global__ void __launch_bounds__(256) dc2d_tb2_batch_kernel(const DcArgs* __res
     if (dc_done(a.done)) return;
     float part = 0.0f;
     unsigned pmax = 0u;
-    // the body flushes its check partials into a.acc (last step of its march)
-    dc2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax);
+    // the body flushes its check partials into its warp's slot (last step of its march)
+    dc2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax,
+                                (long long)blockIdx.x * blockDim.y + threadIdx.y);
 }
 
-__global__ void inner_judge_batch_kernel(BDev* st, int ninst, int nchk, int itmax, int norm_max, int stall)
+// The inner check of every instance still in its inner solve (one warp each),
+// its residual summed from its warps' slots in a fixed order.
+__global__ void inner_judge_batch_kernel(BDev* st, int ninst, int nchk, int itmax, int norm_max, int stall,
+                                         const double* parts, const int* wfirst, const int* wcount, int W)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ninst) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= ninst || st[i].done) return;   // uniform over the warp; no iteration ran
+    const double acc = warp_sum_range(parts, (long long)wfirst[i] * W, (long long)wcount[i] * W, norm_max);
+    if ((threadIdx.x & 31) != 0) return;
     BDev& s = st[i];
-    if (s.done) return;
-    const double acc = s.acc;
     s.acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(s.norm_den);
     s.err = err;
@@ -165,7 +211,8 @@ __global__ void inner_judge_batch_kernel(BDev* st, int ninst, int nchk, int itma
 // cells (cwork: {instance, first inner cell, count}); writes r as FP32.
 template <int MODEL>
 __global__ void __launch_bounds__(256) resid64_batch_kernel(const PTArgs* __restrict__ tab, BDev* st,
-                                                            float* const* rf, const int4* __restrict__ cwork)
+                                                            float* const* rf, const int4* __restrict__ cwork,
+                                                            double* parts64)
 {
     const int4 w = cwork[blockIdx.x];
     const int inst = w.x;
@@ -209,18 +256,21 @@ __global__ void __launch_bounds__(256) resid64_batch_kernel(const PTArgs* __rest
     }
     hm = warp_max_u64(hm);
     if ((threadIdx.x & 31) == 0 && hm) atomicMax(&st[inst].hmax_bits, hm);
-    block_reduce_residual(&st[inst].outer_acc, a.norm_max, part, pmax);
+    block_reduce_residual(nullptr, a.norm_max, part, pmax, parts64, blockIdx.x);   // the chunk's slot
 }
 
 // Per-instance inexact-Newton state machine (see ptd_dc.cu).
+// One warp per instance: the FP64 residual from the instance's chunk slots
+// (ffirst .. ffirst+fcount-1) in a fixed order, then its Newton state.
 __global__ void outer_judge_batch_kernel(BDev* st, int ninst, int norm_max, double tol, double rtol,
-                                         int max_outer, int itmax, int nonlin)
+                                         int max_outer, int itmax, int nonlin, const double* parts64,
+                                         const int* ffirst, const int* fcount)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ninst) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= ninst || st[i].phase >= PH_CONVERGED) return;   // uniform over the warp
+    const double acc = warp_sum_range(parts64, ffirst[i], fcount[i], norm_max);
+    if ((threadIdx.x & 31) != 0) return;
     BDev& s = st[i];
-    if (s.phase >= PH_CONVERGED) return;
-    const double acc = s.outer_acc;
     s.outer_acc = 0.0;
     const double err = norm_max ? acc : sqrt(acc) / sqrt(s.norm_den);
     const double hmax = __longlong_as_double((long long)s.hmax_bits);
@@ -369,8 +419,8 @@ __global__ void __launch_bounds__(256) rb2d_batch_kernel(const RbArgs* __restric
     const int4 w = work[active[blockIdx.x]];
     const RbArgs a = tab[w.x];
     if (rb_skip(a.skip)) return;   // its phase ended since the list was built
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     // the bodies flush their check partials into the warp's slot: work item k, warp w -> k * W + w
     const long long slot = (long long)active[blockIdx.x] * blockDim.y + threadIdx.y;
     if (TB == 2) rb2d_tb2_body<MODEL, CHECK>(a, w.y * blockDim.y + threadIdx.y, w.z, chunk, part, pmax, slot);
@@ -412,23 +462,6 @@ __global__ void rb_reset_batch_kernel(RbDev* st, int ninst)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ninst) rb_reset(&st[i]);
-}
-
-// The sum (or max) of slots first .. first+count-1 by one warp, in a fixed
-// order: lane l takes slots first+l, first+l+32, ... in order, then a fixed
-// shuffle tree.  Every lane returns the result.
-__device__ __forceinline__ double warp_sum_range(const double* parts, long long first, long long count, int norm_max)
-{
-    const int lane = threadIdx.x & 31;
-    double sum = 0.0;
-    unsigned long long mx = 0ull;
-    for (long long k = first + lane; k < first + count; k += 32) {
-        const double v = parts[k];
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-        mx = bits > mx ? bits : mx;
-        sum += v;
-    }
-    return norm_max ? __longlong_as_double((long long)warp_max_u64(mx)) : warp_sum(sum);
 }
 
 // The FP32 check of every instance (one warp each), its residual summed from
@@ -603,12 +636,12 @@ struct ptd_batch {
     int4* fwork = nullptr;
     int nfwork = 0;
     // FP32_RB (H64, Hold64, D64, Hf, Df, d, w32 as above): FP64 base fluxes,
-    // FP32 base defects, FP64 check residual, per-instance control blocks
+    // FP32 base defects, the base check residual (FP32), per-instance control blocks
     bool rb = false;
     double* wb64[2] = {nullptr, nullptr};
     float* tb32[2] = {nullptr, nullptr};
     float* Rb32 = nullptr;
-    double* Cb64 = nullptr;
+    float* Cb32 = nullptr;
     RbDev* rdev = nullptr;
     RbDev* h_rdev = nullptr;
     RbArgs* rbtab[2] = {nullptr, nullptr};
@@ -744,21 +777,23 @@ int upload_work(ptd_batch* b)
     if (rc) return rc;
     BCK(cudaMemcpy(b->work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice));
     b->nwork = (int)work.size();
+    // each instance's work items (contiguous): its check slots
+    std::vector<int> first(b->ninst, 0), count(b->ninst, 0);
+    for (int k = (int)work.size() - 1; k >= 0; --k) {
+        first[work[k].x] = k;
+        count[work[k].x] += 1;
+    }
+    if (!b->wfirst) rc = balloc(&b->wfirst, b->ninst * sizeof(int));
+    if (!rc && !b->wcount) rc = balloc(&b->wcount, b->ninst * sizeof(int));
+    if (rc) return rc;
+    BCK(cudaMemcpy(b->wfirst, first.data(), b->ninst * sizeof(int), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->wcount, count.data(), b->ninst * sizeof(int), cudaMemcpyHostToDevice));
     if (b->rb) {
-        std::vector<int> first(b->ninst, 0), count(b->ninst, 0);
-        for (int k = (int)work.size() - 1; k >= 0; --k) {
-            first[work[k].x] = k;
-            count[work[k].x] += 1;
-        }
         if (b->active) cudaFree(b->active);
         b->active = nullptr;
         rc = balloc(&b->active, work.size() * sizeof(int));
-        if (!rc && !b->wfirst) rc = balloc(&b->wfirst, b->ninst * sizeof(int));
-        if (!rc && !b->wcount) rc = balloc(&b->wcount, b->ninst * sizeof(int));
         if (!rc && !b->nactive) rc = balloc(&b->nactive, sizeof(int));
         if (rc) return rc;
-        BCK(cudaMemcpy(b->wfirst, first.data(), b->ninst * sizeof(int), cudaMemcpyHostToDevice));
-        BCK(cudaMemcpy(b->wcount, count.data(), b->ninst * sizeof(int), cudaMemcpyHostToDevice));
         BCK(cudaMemset(b->nactive, 0, sizeof(int)));
     }
     return PTD_OK;
@@ -841,14 +876,39 @@ int capture_rb(ptd_batch* b)
 int capture(ptd_batch* b)
 {
     if (b->rb) return capture_rb(b);
+    // FP64 / DF64: the whole step; FP32_DC: one inner solve of every instance
+    // in its inner phase.  One graph: a WHILE node whose body is one check
+    // block of every running instance (nchk/tb launches and the per-instance
+    // judge; two blocks when the launch count is odd, so that every pass starts
+    // on buffer parity 0) and the loop judge, which ends the loop once no
+    // instance is running.
     for (int q = 0; q < 2; ++q) {
         if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
         b->g[q] = nullptr;
-        cudaGraph_t gr = nullptr;
-        BCK(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
-        cudaError_t err = cudaSuccess;
-        int par = q, nk = 0;
-        const int nl = b->dc ? b->nchk / b->tb : b->nchk;   // launches per check block
+    }
+    cudaGraph_t g = nullptr;
+    BCK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle loop;
+    cudaError_t err = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    cudaGraph_t body = err == cudaSuccess ? np.conditional.phGraph_out[0] : nullptr;
+    if (err == cudaSuccess)
+        err = cudaStreamBeginCaptureToGraph(b->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err, "batch capture");
+    }
+    const int n = b->ninst, nbw = (n + 3) / 4;   // judges: one warp per instance, 4 per block
+    const int nl = b->dc ? b->nchk / b->tb : b->nchk;   // launches per check block
+    const int nblk = (nl & 1) ? 2 : 1;
+    const int W = b->cfg.warps2d, norm_max = b->bp.norm == PTD_NORM_MAX;
+    int par = 0, nk = 0;
+    for (int blk = 0; blk < nblk && err == cudaSuccess; ++blk) {
         for (int it = 0; it < nl && err == cudaSuccess; ++it) {
             const bool check = it == nl - 1;
             err = b->dc ? launch_dc_batch(b, par, check) : launch_pt_batch(b, par, check);
@@ -856,27 +916,32 @@ int capture(ptd_batch* b)
             ++nk;
         }
         if (err == cudaSuccess) {
-            const int tb = 128, nb = (b->ninst + tb - 1) / tb;
             if (b->dc)
-                inner_judge_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, b->ninst, b->nchk, b->bp.itmax,
-                                                              b->bp.norm == PTD_NORM_MAX, b->stall);
+                inner_judge_batch_kernel<<<nbw, 128, 0, b->s>>>(b->bst, n, b->nchk, b->bp.itmax, norm_max, b->stall,
+                                                                b->parts, b->wfirst, b->wcount, W);
             else
-                judge_batch_kernel<<<nb, tb, 0, b->s>>>(b->st, b->ninst, b->nchk, b->bp.itmax, b->bp.tol,
-                                                        b->norm_den, b->bp.norm == PTD_NORM_MAX);
+                judge_batch_kernel<<<nbw, 128, 0, b->s>>>(b->st, n, b->nchk, b->bp.itmax, b->bp.tol, b->norm_den,
+                                                          norm_max, b->parts, b->wfirst, b->wcount, W);
             err = cudaGetLastError();
             ++nk;
         }
-        cudaError_t e2 = cudaStreamEndCapture(b->s, &gr);
-        if (err != cudaSuccess) {
-            if (gr) cudaGraphDestroy(gr);
-            return cuda_fail(err, "batch capture");
-        }
-        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-        cudaError_t e3 = cudaGraphInstantiate(&b->g[q], gr, 0);
-        cudaGraphDestroy(gr);
-        if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
-        b->kernels_per_graph = nk;
     }
+    if (err == cudaSuccess) {
+        const int max_passes = b->bp.itmax / b->nchk + 2;
+        if (b->dc) batch_loop_judge_kernel<BDev><<<1, 256, 0, b->s>>>(b->bst, n, b->passes, max_passes, loop);
+        else batch_loop_judge_kernel<DevState><<<1, 256, 0, b->s>>>(b->st, n, b->passes, max_passes, loop);
+        err = cudaGetLastError();
+        ++nk;
+    }
+    cudaError_t e2 = cudaStreamEndCapture(b->s, &body);
+    if (err != cudaSuccess || e2 != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(err != cudaSuccess ? err : e2, "batch capture");
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&b->g[0], g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
+    b->kernels_per_graph = nk;   // per pass
     return PTD_OK;
 }
 
@@ -929,28 +994,41 @@ int build_chunks(ptd_batch* b, bool cells)
 
 // FP32_RB: the per-instance argument blocks of the iteration (per buffer
 // parity), the fold and the base kernels.
+// Residual slots of every form: per-warp check slots, the most warps any
+// launch shape gives (28-column tiles at most, up to 8 warps per CTA, rows per
+// chunk >= 8: ptd_batch_set_config's bounds), and one FP64 slot per chunk of
+// build_chunks -- cell chunks (the FP32_DC residual) or field chunks (the
+// FP32_RB base) -- with each instance's chunk range.
+int alloc_slots(ptd_batch* b, bool cells)
+{
+    const int n = b->ninst;
+    long long np = 0, nf = 0;
+    std::vector<int> ff(n), fc(n);
+    for (int i = 0; i < n; ++i) {
+        const Inst& I = b->inst[i];
+        np += (long long)((I.nx - 2 + 27) / 28 + 7) * ((I.ny - 2 + 7) / 8);
+        ff[i] = (int)nf;
+        const long long m = cells ? (long long)(I.nx - 2) * (I.ny - 2) : I.nfield;
+        fc[i] = (int)((m + 2047) / 2048);   // the chunks of build_chunks
+        nf += fc[i];
+    }
+    int rc = balloc(&b->parts, (size_t)np * sizeof(double));
+    if (!rc) rc = balloc(&b->parts64, (size_t)nf * sizeof(double));
+    if (!rc) rc = balloc(&b->ffirst, n * sizeof(int));
+    if (!rc) rc = balloc(&b->fcount, n * sizeof(int));
+    if (rc) return rc;
+    b->nparts = np;
+    BCK(cudaMemcpy(b->ffirst, ff.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->fcount, fc.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    return PTD_OK;
+}
+
 int fill_tables_rb(ptd_batch* b)
 {
     const int n = b->ninst;
-    {   // slots: the most warps any launch shape gives (28-column tiles, up to 8
-        // warps per CTA, rows per chunk >= 8: ptd_batch_set_config's bounds)
-        long long np = 0, nf = 0;
-        std::vector<int> ff(n), fc(n);
-        for (int i = 0; i < n; ++i) {
-            const Inst& I = b->inst[i];
-            np += (long long)((I.nx - 2 + 27) / 28 + 7) * ((I.ny - 2 + 7) / 8);
-            ff[i] = (int)nf;
-            fc[i] = (int)((I.nfield + 2047) / 2048);   // the field chunks of build_chunks
-            nf += fc[i];
-        }
-        int rc = balloc(&b->parts, (size_t)np * sizeof(double));
-        if (!rc) rc = balloc(&b->parts64, (size_t)nf * sizeof(double));
-        if (!rc) rc = balloc(&b->ffirst, n * sizeof(int));
-        if (!rc) rc = balloc(&b->fcount, n * sizeof(int));
+    {
+        const int rc = alloc_slots(b, false);
         if (rc) return rc;
-        b->nparts = np;
-        BCK(cudaMemcpy(b->ffirst, ff.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-        BCK(cudaMemcpy(b->fcount, fc.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     }
     std::vector<RbArgs> t[2] = {std::vector<RbArgs>(n), std::vector<RbArgs>(n)};
     std::vector<RbFoldArgs> ft(n);
@@ -982,7 +1060,7 @@ int fill_tables_rb(ptd_batch* b)
                 a.tb[d] = b->tb32[dd] + o;
             }
             a.Rb = b->Rb32 + o;
-            a.Cb = b->Cb64 + o;
+            a.Cb = b->Cb32 + o;
             a.Hf = b->Hf + o;
             a.Df = b->Df ? b->Df + o : nullptr;
             a.skip = &b->rdev[i].skip;
@@ -1021,7 +1099,7 @@ int fill_tables_rb(ptd_batch* b)
         }
         g.D = b->D64 ? b->D64 + o : nullptr;
         g.Rb = b->Rb32 + o;
-        g.Cb = b->Cb64 + o;
+        g.Cb = b->Cb32 + o;
         g.Hf = b->Hf + o;
         g.acc64 = &b->rdev[i].acc64;
         g.parts = b->parts64;
@@ -1039,6 +1117,10 @@ int fill_tables(ptd_batch* b)
 {
     if (b->rb) return fill_tables_rb(b);
     const int n = b->ninst;
+    {
+        const int rc = alloc_slots(b, b->dc);
+        if (rc) return rc;
+    }
     if (!b->dc) {
         std::vector<PTArgs> t[2] = {std::vector<PTArgs>(n), std::vector<PTArgs>(n)};
         std::vector<double> nd(n);
@@ -1062,6 +1144,7 @@ int fill_tables(ptd_batch* b)
                 a.D = b->D ? at(b->D) : nullptr;
                 a.done = &b->st[i].done;
                 a.acc = &b->st[i].acc;
+                a.parts = b->parts;
             }
         }
         for (int q = 0; q < 2; ++q)
@@ -1100,6 +1183,7 @@ int fill_tables(ptd_batch* b)
             a.r = b->rf + I.off;
             a.done = &b->bst[i].done;
             a.acc = &b->bst[i].acc;
+            a.parts = b->parts;
             a.norm_max = b->bp.norm == PTD_NORM_MAX;
         }
         PTArgs& a = r[i];
@@ -1137,7 +1221,7 @@ void free_batch(ptd_batch* b)
     for (int q = 0; q < 2; ++q)
         if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
     if (b->gstep) cudaGraphExecDestroy(b->gstep);
-    void* rbp[] = {b->wb64[0], b->wb64[1], b->tb32[0], b->tb32[1], b->Rb32, b->Cb64, b->rdev,
+    void* rbp[] = {b->wb64[0], b->wb64[1], b->tb32[0], b->tb32[1], b->Rb32, b->Cb32, b->rdev,
                    b->rbtab[0], b->rbtab[1], b->ftab, b->btab, b->passes, b->wfirst, b->wcount,
                    b->active, b->nactive, b->packed, b->pinst, b->pwork, b->parts, b->parts64,
                    b->ffirst, b->fcount};
@@ -1316,22 +1400,20 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
             if (!rc) rc = balloc(&b->tb32[d], fb);
         }
         if (!rc) rc = balloc(&b->Rb32, fb);
-        if (!rc) rc = balloc(&b->Cb64, db);
+        if (!rc) rc = balloc(&b->Cb32, fb);
         if (!rc) rc = balloc(&b->rdev, n * sizeof(RbDev));
         for (int q = 0; q < 2 && !rc; ++q) rc = balloc(&b->rbtab[q], n * sizeof(RbArgs));
         if (!rc) rc = balloc(&b->ftab, n * sizeof(RbFoldArgs));
         if (!rc) rc = balloc(&b->btab, n * sizeof(RbBaseArgs));
         if (!rc) rc = balloc(&b->norm_den, n * sizeof(double));
-        if (!rc) rc = balloc(&b->passes, sizeof(int));
-        if (!rc && (cudaMallocHost((void**)&b->h_rdev, n * sizeof(RbDev)) != cudaSuccess ||
-                    cudaMallocHost((void**)&b->h_passes, sizeof(int)) != cudaSuccess))
+        if (!rc && cudaMallocHost((void**)&b->h_rdev, n * sizeof(RbDev)) != cudaSuccess)
             rc = bfail(PTD_ENOMEM, "batch: cudaMallocHost failed");
         if (!rc) {
-            double* zd[] = {b->wb64[0], b->wb64[1], b->Cb64};
+            double* zd[] = {b->wb64[0], b->wb64[1]};
             for (double* z : zd)
                 if (cudaMemset(z, 0, db) != cudaSuccess) rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
             // faces past the last one of each direction are read (never used) by the halo lanes
-            float* zf[] = {b->tb32[0], b->tb32[1], b->Rb32};
+            float* zf[] = {b->tb32[0], b->tb32[1], b->Rb32, b->Cb32};
             for (float* z : zf)
                 if (cudaMemset(z, 0, fb) != cudaSuccess) rc = bfail(PTD_ECUDA, "batch: cudaMemset failed");
             if (cudaMemset(b->rdev, 0, n * sizeof(RbDev)) != cudaSuccess)
@@ -1372,6 +1454,9 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
         if (!rc && cudaMallocHost((void**)&b->h_bst, n * sizeof(BDev)) != cudaSuccess)
             rc = bfail(PTD_ENOMEM, "batch: cudaMallocHost failed");
     }
+    if (!rc) rc = balloc(&b->passes, sizeof(int));   // passes of a solve graph's loop
+    if (!rc && cudaMallocHost((void**)&b->h_passes, sizeof(int)) != cudaSuccess)
+        rc = bfail(PTD_ENOMEM, "batch: cudaMallocHost failed");
     if (!rc) {
         void* zs[] = {b->H[0], b->H[1], b->Hold, b->W[0][0], b->W[0][1], b->W[1][0], b->W[1][1], b->D,
                       b->H64, b->Hold64, b->D64};
@@ -1420,22 +1505,15 @@ static int batch_pt_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
     reset_batch_kernel<<<nb, tb, 0, b->s>>>(b->st, n);
     BCK(cudaGetLastError());
     b->launches += 1;
-    const long long blocks_max = b->bp.itmax / b->nchk;
-    long long launched = 0, batch = 1;
-    while (launched < blocks_max) {
-        const long long k = std::min(batch, blocks_max - launched);
-        for (long long j = 0; j < k; ++j) {
-            BCK(cudaGraphLaunch(b->g[(int)(((launched + j) * b->nchk) & 1)], b->s));
-            b->launches += b->kernels_per_graph;
-        }
-        launched += k;
-        int rc = batch_read_states(b);
+    // the whole step: one graph launch, ended on the device
+    BCK(cudaMemsetAsync(b->passes, 0, sizeof(int), b->s));
+    if (b->nchk <= b->bp.itmax) BCK(cudaGraphLaunch(b->g[0], b->s));
+    BCK(cudaMemcpyAsync(b->h_passes, b->passes, sizeof(int), cudaMemcpyDeviceToHost, b->s));
+    {
+        const int rc = batch_read_states(b);
         if (rc) return rc;
-        bool all = true;
-        for (int i = 0; i < n; ++i) all = all && b->h_st[i].done != DONE_RUNNING;
-        if (all) break;
-        batch = std::min<long long>(batch * 2, 64);
     }
+    b->launches += (long long)(*b->h_passes) * b->kernels_per_graph;
     // bring every instance back to parity 0, then Hold <- H
     const size_t es = sizeof(double);
     for (int i = 0; i < n; ++i) {
@@ -1459,16 +1537,18 @@ static int batch_pt_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
 
 static int batch_residual(ptd_batch* b)
 {
-    if (b->model == LIN) resid64_batch_kernel<LIN><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork);
+    if (b->model == LIN)
+        resid64_batch_kernel<LIN><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork, b->parts64);
     else if (b->model == LINSTEP)
-        resid64_batch_kernel<LINSTEP><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork);
-    else resid64_batch_kernel<NONLIN><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork);
+        resid64_batch_kernel<LINSTEP><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork, b->parts64);
+    else resid64_batch_kernel<NONLIN><<<b->ncwork, 256, 0, b->s>>>(b->rtab, b->bst, b->rf_ptrs, b->cwork, b->parts64);
     BCK(cudaGetLastError());
-    const int n = b->ninst, tb = 128, nb = (n + tb - 1) / tb;
+    const int n = b->ninst, nbw = (n + 3) / 4;   // one warp per instance, 4 per block
     const double rtol = b->bp.dc_inner_rtol > 0.0 ? b->bp.dc_inner_rtol : 1e-3;
     const int max_outer = b->bp.dc_max_outer > 0 ? b->bp.dc_max_outer : 30;
-    outer_judge_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, n, b->bp.norm == PTD_NORM_MAX, b->bp.tol, rtol, max_outer,
-                                                   b->bp.itmax, b->model == NONLIN);
+    outer_judge_batch_kernel<<<nbw, 128, 0, b->s>>>(b->bst, n, b->bp.norm == PTD_NORM_MAX, b->bp.tol, rtol,
+                                                    max_outer, b->bp.itmax, b->model == NONLIN, b->parts64, b->ffirst,
+                                                    b->fcount);
     BCK(cudaGetLastError());
     b->launches += 2;
     return PTD_OK;
@@ -1495,22 +1575,13 @@ static int batch_dc_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
             zero_batch_kernel<<<b->nfwork, 256, 0, b->s>>>(b->dtab[0], b->bst, b->fwork, 2);
             BCK(cudaGetLastError());
             b->launches += 1;
-            long long launched = 0, batch = 1;
-            const long long blocks_max = b->bp.itmax / b->nchk;
-            while (launched < blocks_max) {
-                const long long k = std::min(batch, blocks_max - launched);
-                for (long long j = 0; j < k; ++j) {
-                    BCK(cudaGraphLaunch(b->g[(int)(((launched + j) * (b->nchk / b->tb)) & 1)], b->s));
-                    b->launches += b->kernels_per_graph;
-                }
-                launched += k;
-                rc = batch_read_states(b);
-                if (rc) return rc;
-                bool all = true;
-                for (int i = 0; i < n; ++i) all = all && b->h_bst[i].done;
-                if (all) break;
-                batch = std::min<long long>(batch * 2, 32);
-            }
+            // the inner solves: one graph launch, ended on the device
+            BCK(cudaMemsetAsync(b->passes, 0, sizeof(int), b->s));
+            BCK(cudaGraphLaunch(b->g[0], b->s));
+            BCK(cudaMemcpyAsync(b->h_passes, b->passes, sizeof(int), cudaMemcpyDeviceToHost, b->s));
+            rc = batch_read_states(b);
+            if (rc) return rc;
+            b->launches += (long long)(*b->h_passes) * b->kernels_per_graph;
             for (int i = 0; i < n; ++i)
                 if (b->h_bst[i].phase == PH_INNER) b->iterations += b->h_bst[i].iter;
             parity_batch_kernel<<<nb, tb, 0, b->s>>>(b->bst, b->cur_parity, n, b->tb);

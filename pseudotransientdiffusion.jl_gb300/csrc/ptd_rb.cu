@@ -15,18 +15,18 @@ template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) rb1d_kernel(RbArgs a)
 {
     if (rb_skip(a.skip)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     rb1d_body<MODEL, CHECK>(a, blockIdx.x, part, pmax);
-    if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax, a.parts, blockIdx.x);
+    if (CHECK) block_reduce_residual(a.acc, a.norm_max, (double)part, widen_max32(pmax), a.parts, blockIdx.x);
 }
 
 template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) rb2d_kernel(RbArgs a, int chunk)
 {
     if (rb_skip(a.skip)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     // the body flushes its check partials into its warp's slot (last step of its march)
     rb2d_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax, warp_slot());
 }
@@ -36,8 +36,8 @@ template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256) rb2d_tb2_pair_kernel(RbArgs a, int chunk)
 {
     if (rb_skip(a.skip)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     if constexpr (MODEL == LIN || MODEL == NONLIN)
         rb2d_tb2_pair_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax,
                                          warp_slot());
@@ -52,8 +52,8 @@ template <int MODEL, bool CHECK>
 __global__ void __launch_bounds__(256, (MODEL == NONLIN && !CHECK) ? 8 : 0) rb2d_tb2_kernel(RbArgs a, int chunk)
 {
     if (rb_skip(a.skip)) return;
-    double part = 0.0;
-    unsigned long long pmax = 0ull;
+    float part = 0.0f;
+    unsigned pmax = 0u;
     // the body flushes its check partials into its warp's slot (last step of its march)
     rb2d_tb2_body<MODEL, CHECK>(a, blockIdx.x * blockDim.y + threadIdx.y, blockIdx.y, chunk, part, pmax, warp_slot());
 }
@@ -104,6 +104,91 @@ __global__ void __launch_bounds__(256) rb_base_kernel(RbBaseArgs b, const RbDev*
         rb_base_cell(b, ix, (int)(rest % b.ny), (int)(rest / b.ny), part, pmax);
     }
     block_reduce_residual(b.acc64, b.norm_max, part, pmax, b.parts, blockIdx.x);
+}
+
+// 2D / 3D: rb_base_cell's quantities with each face evaluated once.  A warp
+// takes 32 consecutive x cells of one row and marches over a chunk of rows
+// (2D) or planes (3D, one y row per warp): the face to a cell's left is the
+// next lane down's right face (a shuffle), the face below it in the march the
+// previous step's face above; only the tile's first lane and the march's
+// first step evaluate theirs, and in 3D both y faces are evaluated per cell.
+// Every face is the same rb_u64 evaluation, so the quantities are
+// rb_base_cell's bit for bit; the residual goes into the block's slot.
+constexpr int kBaseChunk = 32;   // rows (2D) / planes (3D) per warp
+template <int NDIM>
+__global__ void __launch_bounds__(256) rb_base_march_kernel(RbBaseArgs b, const RbDev* st)
+{
+    if (st && st->step_done) return;   // uniform over the grid
+    const int lane = threadIdx.x;
+    const int ix = 32 * blockIdx.x + lane;
+    const int ixc = min(ix, b.nx - 1);   // lanes past the row compute on its last cell, store nothing
+    const bool own = ix < b.nx;
+    int iy, k0, k1, nm;
+    long long sm;   // the march: y in 2D, z in 3D
+    if (NDIM == 2) {
+        iy = 0;
+        k0 = (blockIdx.y * blockDim.y + threadIdx.y) * kBaseChunk;
+        nm = b.ny;
+        sm = b.sy;
+    } else {
+        iy = blockIdx.y * blockDim.y + threadIdx.y;
+        k0 = blockIdx.z * kBaseChunk;
+        nm = b.nz;
+        sm = b.sz;
+    }
+    k1 = min(k0 + kBaseChunk, nm);
+    double part = 0.0;
+    unsigned long long pmax = 0ull;
+    if (k0 < k1 && iy < b.ny) {   // uniform over the warp
+        const bool xin = ixc >= 1 && ixc <= b.nx - 2;
+        const bool yin = NDIM == 2 || (iy >= 1 && iy <= b.ny - 2);
+        double udn = 0.0;   // the face below the cell in the march
+        for (int k = k0; k < k1; ++k) {
+            const long long c = NDIM == 2 ? (long long)k * b.sy + ixc : (long long)k * b.sz + (long long)iy * b.sy + ixc;
+            const bool min_ = k >= 1 && k <= nm - 2;
+            const bool inner = xin && yin && min_;
+            // x faces: right by every lane, left from the lane below
+            const double ur = ixc <= b.nx - 2 ? rb_u64(b, c, c + 1) : 0.0;
+            double ul = __shfl_up_sync(FULL, ur, 1);
+            if (lane == 0 && inner) ul = rb_u64(b, c - 1, c);
+            // march faces: above now, below from the previous step
+            const double uup = k <= nm - 2 ? rb_u64(b, c, c + sm) : 0.0;
+            if (k == k0 && inner) udn = rb_u64(b, c - sm, c);
+            if (own) {
+                b.Hf[c] = __double2float_rn(b.H[c]);
+                const int dm = NDIM - 1;   // the march direction's index
+                if (ixc <= b.nx - 2) b.tb[0][c] = (float)(b.wb[0][c] + ur);
+                if (k <= nm - 2) b.tb[dm][c] = (float)(b.wb[dm][c] + uup);
+                double uyr = 0.0;
+                if (NDIM == 3 && iy <= b.ny - 2) {
+                    uyr = rb_u64(b, c, c + b.sy);
+                    b.tb[1][c] = (float)(b.wb[1][c] + uyr);
+                }
+                if (inner) {
+                    // the order of rb_base_cell: x, y, z
+                    double divw = 0.0, divu = 0.0;
+                    divw = fma(b.wb[0][c] - b.wb[0][c - 1], b.sig[0], divw);
+                    divu = fma(ur - ul, b.sig[0], divu);
+                    if (NDIM == 3) {
+                        const double uyl = rb_u64(b, c - b.sy, c);
+                        divw = fma(b.wb[1][c] - b.wb[1][c - b.sy], b.sig[1], divw);
+                        divu = fma(uyr - uyl, b.sig[1], divu);
+                    }
+                    divw = fma(b.wb[dm][c] - b.wb[dm][c - sm], b.sig[dm], divw);
+                    divu = fma(uup - udn, b.sig[dm], divu);
+                    const double dh = (b.H[c] - b.Hold[c]) * b.rdt;
+                    b.Rb[c] = (float)(dh + divw);
+                    const double cb = divu - dh;
+                    if (NDIM == 3) b.Cb64[c] = cb;
+                    else b.Cb[c] = (float)cb;
+                    accumulate_residual(cb, part, pmax);
+                }
+            }
+            udn = uup;
+        }
+    }
+    block_reduce_residual(b.acc64, b.norm_max, part, pmax, b.parts,
+                          ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
 __global__ void rb_reset_kernel(RbDev* st) { rb_reset(st); }
@@ -190,7 +275,8 @@ struct RbState {
     float* w[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     float* tb[3] = {nullptr, nullptr, nullptr};
     float* Rb = nullptr;
-    double* Cb = nullptr;
+    float* Cb = nullptr;                          // base check residual (1D, 2D: FP32)
+    double* Cb64 = nullptr;                       // base check residual (3D: FP64)
     float* Hf = nullptr;
     float* Df = nullptr;
     double* H = nullptr;                          // owned by the context: the base H_b
@@ -245,6 +331,7 @@ void rb_args(const RbState* rb, int parity, const int* skip, RbArgs& a)
     }
     a.Rb = rb->Rb;
     a.Cb = rb->Cb;
+    a.Cb64 = rb->Cb64;
     a.Hf = rb->Hf;
     a.Df = rb->Df;
     a.skip = skip;
@@ -345,6 +432,25 @@ long long rb_check_slots(const RbState* rb)
     return (long long)((p.nx - 2 + 30) / 31) * ((p.ny - 2 + 14) / 15) * nzc;
 }
 
+// The grid of rb_base_march_kernel (8 warps per CTA); its CTA count is the
+// number of FP64 residual slots of a rebase.
+dim3 base_grid(const RbState* rb)
+{
+    const ptd_params& p = rb->p;
+    const unsigned gx = (p.nx + 31) / 32;
+    if (p.ndim == 2) return dim3(gx, ((p.ny + kBaseChunk - 1) / kBaseChunk + 7) / 8, 1);
+    return dim3(gx, (p.ny + 7) / 8, (p.nz + kBaseChunk - 1) / kBaseChunk);
+}
+
+// One rebase's base kernel: 1D grid-stride, 2D / 3D the march kernel.
+cudaError_t launch_base(const RbState* rb, const RbBaseArgs& b, const RbDev* st)
+{
+    if (rb->p.ndim == 1) rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(b, st);
+    else if (rb->p.ndim == 2) rb_base_march_kernel<2><<<base_grid(rb), dim3(32, 8), 0, rb->s>>>(b, st);
+    else rb_base_march_kernel<3><<<base_grid(rb), dim3(32, 8), 0, rb->s>>>(b, st);
+    return cudaGetLastError();
+}
+
 // (Re)allocate the residual slots for the current launch configuration.
 int rb_alloc_parts(RbState* rb)
 {
@@ -360,7 +466,8 @@ int rb_alloc_parts(RbState* rb)
     }
     rb->nparts = n;
     if (!rb->parts64) {
-        rb->nparts64 = fill_blocks();
+        const dim3 bg = base_grid(rb);
+        rb->nparts64 = rb->p.ndim == 1 ? fill_blocks() : (long long)bg.x * bg.y * bg.z;
         if (cudaMalloc((void**)&rb->parts64, (size_t)rb->nparts64 * sizeof(double)) != cudaSuccess) {
             cudaGetLastError();
             return set_error(PTD_ENOMEM, "rb: cudaMalloc failed");
@@ -408,6 +515,7 @@ RbBaseArgs base_args(const RbState* rb)
     b.D = rb->D;
     b.Rb = rb->Rb;
     b.Cb = rb->Cb;
+    b.Cb64 = rb->Cb64;
     b.Hf = rb->Hf;
     b.acc64 = &rb->dev->acc64;
     b.parts = rb->parts64;
@@ -489,10 +597,7 @@ int rb_capture(RbState* rb)
         if (err != cudaSuccess) break;
         rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, rb->tblk);
         err = cudaGetLastError();
-        if (err == cudaSuccess) {
-            rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
-            err = cudaGetLastError();
-        }
+        if (err == cudaSuccess) err = launch_base(rb, base_args(rb), rb->dev);
         if (err == cudaSuccess) {
             rb_base_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts64, rb->nparts64, rb->p.tol,
                                                        rb->dv.norm_den, rb->p.norm == PTD_NORM_MAX, 1);
@@ -574,7 +679,8 @@ int rb_create(const ptd_ctx_base& g, const ptd_params& p, const Derived& dv, cud
         if (!rc) rc = alloc((void**)&rb->tb[d], fb);
     }
     if (!rc) rc = alloc((void**)&rb->Rb, fb);
-    if (!rc) rc = alloc((void**)&rb->Cb, (size_t)g.nfield * sizeof(double));
+    if (!rc && p.ndim < 3) rc = alloc((void**)&rb->Cb, (size_t)g.nfield * sizeof(float));
+    if (!rc && p.ndim == 3) rc = alloc((void**)&rb->Cb64, (size_t)g.nfield * sizeof(double));
     if (!rc) rc = alloc((void**)&rb->Hf, fb);
     if (!rc && (p.model == PTD_MODEL_LINSTEP || p.model == PTD_MODEL_NONLIN_EXPM)) rc = alloc((void**)&rb->Df, fb);
     if (!rc) rc = alloc((void**)&rb->dev, sizeof(RbDev));
@@ -619,6 +725,7 @@ void rb_destroy(RbState* rb)
     }
     cudaFree(rb->Rb);
     cudaFree(rb->Cb);
+    cudaFree(rb->Cb64);
     cudaFree(rb->Hf);
     cudaFree(rb->Df);
     cudaFree(rb->dev);
@@ -658,8 +765,7 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
 {
     rb_reset_kernel<<<1, 1, 0, rb->s>>>(rb->dev);
     RCK(cudaGetLastError());
-    rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), rb->dev);
-    RCK(cudaGetLastError());
+    RCK(launch_base(rb, base_args(rb), rb->dev));
     rb_base_judge_kernel<<<1, 256, 0, rb->s>>>(rb->dev, rb->parts64, rb->nparts64, rb->p.tol, rb->dv.norm_den,
                                                rb->p.norm == PTD_NORM_MAX, 0);
     RCK(cudaGetLastError());
@@ -711,8 +817,7 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
 // Fixed FP32 iterations without checks (perf protocol), then one rebase.
 int rb_iterate(RbState* rb, int32_t niter)
 {
-    rb_base_kernel<<<fill_blocks(), 256, 0, rb->s>>>(base_args(rb), nullptr);
-    RCK(cudaGetLastError());
+    RCK(launch_base(rb, base_args(rb), nullptr));
     int par = 0;
     long long nl = 0;
     RCK(rb_run_plain(rb, niter, rb->zero_flag, par, nl));

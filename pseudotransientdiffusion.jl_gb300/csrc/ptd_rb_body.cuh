@@ -55,7 +55,8 @@ struct RbArgs {
     float* wout[3];
     const float* tb[3];   // base flux defect w_b + u(H_b), per face
     const float* Rb;      // base update residual
-    const double* Cb;     // base check residual (FP64: read on check iterations only)
+    const float* Cb;      // base check residual, rounded to FP32 (1D, 2D; read on check iterations only)
+    const double* Cb64;   // base check residual, FP64 (3D)
     const float* Hf;      // H_b as FP32 (iteration parameters, u_d)
     const float* Df;      // LINSTEP: D, NONLIN_EXPM: exp(m), as FP32
     const int* skip;
@@ -168,7 +169,7 @@ __device__ __forceinline__ bool rb_skip(const int* skip) { return __ldcg(skip) !
 // ---------------------------------------------------------------------------
 // 1D: one thread per cell; the left face is recomputed (1D grids are small).
 template <int MODEL, bool CHECK>
-__device__ __forceinline__ void rb1d_body(const RbArgs& a, int bx, double& part, unsigned long long& pmax)
+__device__ __forceinline__ void rb1d_body(const RbArgs& a, int bx, float& part, unsigned& pmax)
 {
     constexpr bool LS = MODEL == LINSTEP;
     constexpr bool HASD = LS || MODEL == NONLIN_EXPM;   // a per-cell field in Df
@@ -192,7 +193,7 @@ __device__ __forceinline__ void rb1d_body(const RbArgs& a, int bx, double& part,
         const float dnew = fmaf(-e, fmaf(dc, a.rdt, a.Rb[i] + (wr - wl) * a.sig[0]), dc);
         a.dout[i] = dnew;
         if (CHECK)
-            accumulate_residual(a.Cb[i] + (double)((ur - ul) * a.sig[0]) - (double)dnew * (double)a.rdt, part,
+            accumulate_residual32(fmaf(-dnew, a.rdt, a.Cb[i] + (ur - ul) * a.sig[0]), part,
                                 pmax);
     }
 }
@@ -200,8 +201,8 @@ __device__ __forceinline__ void rb1d_body(const RbArgs& a, int bx, double& part,
 // ---------------------------------------------------------------------------
 // 2D: the tiling of ptd_pt_body.cuh (31 updated columns per warp, y march).
 template <int MODEL, bool CHECK>
-__device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
-                                          unsigned long long& pmax, long long slot = 0)
+__device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int chunk, float& part,
+                                          unsigned& pmax, long long slot = 0)
 {
     constexpr bool LS = MODEL == LINSTEP;
     constexpr bool HASD = LS || MODEL == NONLIN_EXPM;   // a per-cell field in Df
@@ -255,7 +256,7 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
                 a.dout[idx] = dnew;
                 if (CHECK) {
                     const float divu = fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]);
-                    accumulate_residual(a.Cb[idx] + (double)divu - (double)dnew * (double)a.rdt, part, pmax);
+                    accumulate_residual32(fmaf(-dnew, a.rdt, a.Cb[idx] + divu), part, pmax);
                 }
             }
             dc = dn;
@@ -266,7 +267,7 @@ __device__ __forceinline__ void rb2d_body(const RbArgs& a, int tile, int cy, int
                 Db = Dc;
                 Dc = Dn;
             }
-            if (CHECK && j == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
+            if (CHECK && j == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
         }
     } else if (CHECK && a.parts && lane == 0) {
         a.parts[slot] = 0.0;   // a warp with no cells: its slot still holds this check's (empty) part
@@ -293,8 +294,8 @@ __device__ __forceinline__ float rb_star(float Dc, float Db, float Dn)
 }
 
 template <int MODEL, bool CHECK>
-__device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
-                                              unsigned long long& pmax, long long slot = 0)
+__device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy, int chunk, float& part,
+                                              unsigned& pmax, long long slot = 0)
 {
     constexpr bool HASD = MODEL == LINSTEP || MODEL == NONLIN_EXPM;
     const int lane = threadIdx.x;
@@ -429,7 +430,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
             a.wout[1][os] = wy2;
             if (CHECK) {
                 const float divu = fmaf(uy2 - uy2b, s1, (ux2 - ux2l) * s0);
-                accumulate_residual(a.Cb[os] + (double)divu - (double)q * (double)rdt, part, pmax);
+                accumulate_residual32(fmaf(-q, rdt, a.Cb[os] + divu), part, pmax);
             }
         }
         // shift the windows
@@ -448,7 +449,7 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
         D0 = D1;
         D0r = D1r;
         D1 = D2;
-        if (CHECK && s == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
+        if (CHECK && s == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
     }
 }
 
@@ -465,8 +466,8 @@ __device__ __forceinline__ void rb2d_tb2_body(const RbArgs& a, int tile, int cy,
 // pair is one aligned 8-byte access): level 1 updates q = 1..62, level 2
 // q = 2..61 (60 columns per warp).
 template <int MODEL, bool CHECK>
-__device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, int cy, int chunk, double& part,
-                                                   unsigned long long& pmax, long long slot = 0)
+__device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, int cy, int chunk, float& part,
+                                                   unsigned& pmax, long long slot = 0)
 {
     static_assert(MODEL == LIN || MODEL == NONLIN, "the pair kernel serves LIN and NONLIN");
     const int lane = threadIdx.x;
@@ -579,8 +580,8 @@ __device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, in
         if (CHECK) {
             const float2 ux2l = left(ux2);
             const float2 divu = fma2(sub2(uy2, uy2b), s1, mul2(sub2(ux2, ux2l), s0));
-            if (u2a) accumulate_residual(a.Cb[os] + (double)divu.x - (double)q.x * (double)rdt.x, part, pmax);
-            if (u2b) accumulate_residual(a.Cb[os + 1] + (double)divu.y - (double)q.y * (double)rdt.y, part, pmax);
+            if (u2a) accumulate_residual32(fmaf(-q.x, rdt.x, a.Cb[os] + divu.x), part, pmax);
+            if (u2b) accumulate_residual32(fmaf(-q.y, rdt.y, a.Cb[os + 1] + divu.y), part, pmax);
         }
         // shift the windows
         p0 = p1;
@@ -594,7 +595,7 @@ __device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, in
         h0 = h1;
         h0r = h1r;
         h1 = h2;
-        if (CHECK && s == j1 - 1) warp_flush_residual(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
+        if (CHECK && s == j1 - 1) warp_flush_residual32(a.acc, a.norm_max, part, pmax, lane, a.parts, slot);
     }
 }
 
@@ -693,7 +694,10 @@ __device__ __forceinline__ void rb3d_body(const RbArgs& a, int bx, int by, int b
                 if (CHECK) {
                     const float uyb = su[p][r - 1][lane];
                     const float divu = fmaf(uz - uzb, a.sig[2], fmaf(uy - uyb, a.sig[1], (ux - uxl) * a.sig[0]));
-                    accumulate_residual(a.Cb[idx] + (double)divu - (double)dnew * (double)a.rdt, part, pmax);
+                    // 3D: the FP64 pipe, otherwise idle in this kernel, forms and sums the
+                    // residual from an FP64 base term (an FP32 residual, or an FP32 base term
+                    // widened here, made the 512^3 step 7-16 ms longer)
+                    accumulate_residual(a.Cb64[idx] + (double)divu - (double)dnew * (double)a.rdt, part, pmax);
                 }
             }
             dc = dn;
@@ -836,7 +840,7 @@ __device__ __forceinline__ void rb3d_tb2_body(const RbArgs& a, int bx, int by, i
                 if (CHECK) {
                     const float uy2b = su2[r - 1][lane];
                     const float divu = fmaf(uz2 - uz2b, s2, fmaf(uy2 - uy2b, s1, (ux2 - ux2l) * s0));
-                    accumulate_residual(a.Cb[o0] + (double)divu - (double)q * (double)rdt, part, pmax);
+                    accumulate_residual(a.Cb64[o0] + (double)divu - (double)q * (double)rdt, part, pmax);
                 }
             }
             if (own_x) a.wout[0][o0] = wx2;
@@ -909,7 +913,8 @@ struct RbBaseArgs {
     const double* D;
     float* tb[3];
     float* Rb;
-    double* Cb;
+    float* Cb;           // 1D, 2D: C_b rounded to FP32
+    double* Cb64;        // 3D: C_b
     float* Hf;
     double* acc64;
     double* parts;      // per-block slots of the FP64 residual (NULL: atomics into acc64)
@@ -958,7 +963,7 @@ __device__ __forceinline__ void rb_base_cell(const RbBaseArgs& b, int ix, int iy
         const double dh = (b.H[c] - b.Hold[c]) * b.rdt;
         b.Rb[c] = (float)(dh + divw);
         const double cb = divu - dh;
-        b.Cb[c] = cb;
+        b.Cb[c] = (float)cb;
         accumulate_residual(cb, part, pmax);
     }
 }

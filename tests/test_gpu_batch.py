@@ -150,12 +150,14 @@ def test_batch_device_tensors_match_host_arrays():
         assert np.array_equal(np.ravel(Hh[k], order="F"), Hd[k].cpu().numpy())
 
 
-def test_batch_rebased_is_deterministic():
-    """FP32_RB batch: the check and FP64 residuals are summed from per-warp /
-    per-chunk slots in a fixed order, so two solves give the same iterations,
-    residuals and H bit for bit."""
+@pytest.mark.parametrize("prec", ["fp32_rb", "fp64", "df64", "fp32_dc"])
+def test_batch_is_deterministic(prec):
+    """Every form of the batch sums its check residuals (and the FP64 residuals
+    of the rebased and defect-correction forms) from per-warp / per-chunk
+    slots in a fixed order, so two solves give the same iterations, residuals
+    and H bit for bit."""
     sizes, Hs, Ds = ptdiff.batch_instances(5, seed=9, nmin=30, nmax=150)
-    p = ptdiff.batch_params(len(sizes), model=S.LINSTEP, precision="fp32_rb", nt=2)
+    p = ptdiff.batch_params(len(sizes), model=S.LINSTEP, precision=prec, nt=2)
     out = []
     with ptdiff.BatchSolver(p, sizes, sizes) as b:
         for _ in range(2):
@@ -186,3 +188,25 @@ def test_batch_set_config():
     for a, c in zip(Ha, Hb):
         rms = float(np.sqrt(np.mean(np.square(a))))
         assert rel_l2(c, a) <= 2 * 0.2 * 1e-8 / rms
+
+
+@pytest.mark.parametrize("prec,nchk", [("fp64", 10), ("fp64", 7), ("fp32_dc", 10)])
+def test_batch_launches_end_with_the_solve(prec, nchk):
+    """A batch step is one graph launch whose loop the device ends once every
+    instance has stopped: the PT launches are the largest instance's
+    iterations plus at most one idle check block, with a few bookkeeping
+    kernels per check block.  (The rebased batch runs phases of ~200
+    iterations common to all instances, ended by the FP64 rebase of every
+    running instance; its launches for an instance whose phase is over return
+    after one load.)"""
+    sizes, Hs, Ds = ptdiff.batch_instances(4, seed=12, nmin=24, nmax=96)
+    p = ptdiff.batch_params(len(sizes), model=S.LINSTEP, precision=prec, nt=1, nchk=nchk, itmax=10000 * nchk)
+    with ptdiff.BatchSolver(p, sizes, sizes) as b:
+        l0, _ = b.counters()
+        iters, _ = b.solve([h.copy(order="F") for h in Hs], Ds)
+        l1, _ = b.counters()
+    if prec == "fp32_dc":   # inner iterations of several inner solves: a loose bound
+        assert 0 < l1 - l0 <= 3 * int(np.max(iters)) + 200
+    else:
+        m = int(np.max(iters))
+        assert 0 < l1 - l0 <= m + 6 * (m // nchk + 2) + 2 * nchk + 20, (l1 - l0, m)
