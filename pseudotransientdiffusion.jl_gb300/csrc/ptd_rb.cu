@@ -80,12 +80,8 @@ __global__ void __launch_bounds__(512) rb3d_kernel(RbArgs a, int chunk)
     if (CHECK) block_reduce_residual(a.acc, a.norm_max, part, pmax, a.parts, block_slot());
 }
 
-__global__ void rb_fold_kernel(RbFoldArgs f, const RbDev* st, int parity, int tb)
+__global__ void rb_fold_kernel(RbFoldArgs f, int parity)
 {
-    if (parity < 0) {
-        if (st->step_done) return;
-        parity = (st->phase_iter / tb) & 1;   // one buffer swap per launch of tb iterations
-    }
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < f.n;
          t += (long long)gridDim.x * blockDim.x)
         rb_fold_elem(f, parity, t);
@@ -524,10 +520,10 @@ RbBaseArgs base_args(const RbState* rb)
 }
 
 // The rebased PT iteration of one physical step as one CUDA graph: a WHILE
-// node whose body is one phase -- blocks of nchk iterations each followed by
-// the FP32 judge, then the rebase (fold, base quantities, FP64 judge) -- and
-// which the FP64 judge ends when the step stops.  Every phase starts from
-// buffer parity 0.
+// node whose body is one check block of nchk iterations with its FP32 judge,
+// followed by the rebase (fold, base quantities, FP64 judge) in an IF node
+// that the judge opens when the phase is over, and the loop judge, which ends
+// the loop when the step stops (the body's layout is below).
 int rb_capture(RbState* rb)
 {
     cudaGraph_t g = nullptr;
@@ -595,7 +591,7 @@ int rb_capture(RbState* rb)
             err = cudaStreamBeginCaptureToGraph(rb->s, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                                 cudaStreamCaptureModeThreadLocal);
         if (err != cudaSuccess) break;
-        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, rb->tblk);
+        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), par);
         err = cudaGetLastError();
         if (err == cudaSuccess) err = launch_base(rb, base_args(rb), rb->dev);
         if (err == cudaSuccess) {
@@ -793,7 +789,7 @@ int rb_step(RbState* rb, int32_t* iters, double* err_hist, int32_t err_cap, int3
         int par = 0;
         long long nl = 0;
         RCK(rb_run_plain(rb, tail, rb->zero_flag, par, nl));
-        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
+        rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), par);
         RCK(cudaGetLastError());
         rb->k.launches += nl + 1;
         iter = rb->p.itmax;
@@ -821,7 +817,7 @@ int rb_iterate(RbState* rb, int32_t niter)
     int par = 0;
     long long nl = 0;
     RCK(rb_run_plain(rb, niter, rb->zero_flag, par, nl));
-    rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), rb->dev, par, 1);
+    rb_fold_kernel<<<fill_blocks(), 256, 0, rb->s>>>(fold_args(rb), par);
     RCK(cudaGetLastError());
     rb->k.launches += nl + 2;
     rb->k.iterations += niter;

@@ -867,10 +867,9 @@ __device__ __forceinline__ void rb3d_tb2_body(const RbArgs& a, int bx, int by, i
 }
 
 // ---------------------------------------------------------------------------
-// Rebase, FP64.  Fold the changes into the base: H_b += delta, w_b += omega
-// (positions that are never updated hold zeros), and clear the buffers the
-// next phase starts from (parity 0).  parity < 0: the buffers of the phase's
-// own parity (RbDev::phase_iter, tb iterations per launch).
+// Rebase, FP64.  Fold the changes of buffer parity `parity` into the base:
+// H_b += delta, w_b += omega (positions that are never updated hold zeros),
+// and clear both buffers, so that the next iteration may start on either.
 struct RbFoldArgs {
     long long n;
     double* H;

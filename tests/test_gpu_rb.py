@@ -249,3 +249,23 @@ def test_check_residual_is_deterministic(prec, name, shape):
     assert i1 == i2
     assert np.array_equal(e1, e2)
     assert np.array_equal(np.ravel(h1), np.ravel(h2))
+
+
+@pytest.mark.parametrize("name,shape,nchk", [("2d_nonlin_4096", (256, 256), 100), ("3d_nonlin_512", (48, 48, 48), 10),
+                                             ("2d_nonlin_4096", (200, 180), 7)])
+def test_rebased_step_launches_no_kernel_past_its_stop(name, shape, nchk):
+    """A step is one graph launch: one check block per pass of its loop, the
+    FP64 rebase in an IF node opened at the end of a phase.  Its launches are
+    its PT launches (iterations / iterations per launch) plus a few
+    bookkeeping kernels per check block and per rebase, and at most one idle
+    check block (odd launch counts)."""
+    s = S.CONFIGS[name]
+    H = S.initial_condition(s, *shape)
+    with ptdiff.Solver(ptdiff.make_params(s, shape, nt=2, nchk=nchk, precision="fp32_rb")) as sol:
+        l0, _ = sol.counters()
+        iters, _, st = sol.solve(H)
+        l1, _ = sol.counters()
+    assert st == 0
+    tb = 2 if len(shape) == 2 and nchk % 2 == 0 else 1
+    bound = sum(it // tb + 6 * (it // nchk + 2) + nchk for it in (int(v) for v in iters))
+    assert 0 < l1 - l0 <= bound, (l1 - l0, list(iters))
