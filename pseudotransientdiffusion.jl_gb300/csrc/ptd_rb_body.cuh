@@ -551,7 +551,8 @@ __device__ __forceinline__ void rb2d_tb2_pair_body(const RbArgs& a, int tile, in
     // Staging them through a per-warp shared-memory ring with cp.async, one to
     // three steps ahead, was slower at every launch shape that fills the GPU:
     // 67.5 / 68.6 / 90.5 us against 64.7 at the best shape, the shared loads
-    // costing more issue slots than the hidden latency saved.)
+    // costing more issue slots than the hidden latency saved.  Capping the
+    // registers at 48 for five CTAs per SM spilled 40 bytes and took 73 us.)
     long long o = oC;   // offset of row s+1
     for (int s = j0; s < j1; ++s, o += sy) {
         float2 p1 = d1, wx1 = f2(0.0f), wy1 = f2(0.0f), r1 = f2(0.0f), h2 = h1, tbx1 = f2(0.0f), tby1 = f2(0.0f);
