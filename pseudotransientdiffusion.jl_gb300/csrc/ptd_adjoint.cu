@@ -702,7 +702,7 @@ struct ptd_adj {
     AdjState* h_st = nullptr;
     double* h_acc = nullptr;
     AdjArgs* d_args[2] = {nullptr, nullptr};
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph = nullptr;   // one FP64 / DF64 adjoint solve
     int nchk = 20;
     double rtol = 1e-10;        // adjoint solve target, relative to its right-hand side
     double accept_rtol = 1e-7;  // a solve stalled at an arithmetic floor below this is accepted
@@ -1019,7 +1019,7 @@ int adj_capture(ptd_adj* A)
         if (g) cudaGraphDestroy(g);
         return cuda_fail(err, "adjoint capture");
     }
-    const cudaError_t e3 = cudaGraphInstantiate(&A->graph[0], g, 0);
+    const cudaError_t e3 = cudaGraphInstantiate(&A->graph, g, 0);
     cudaGraphDestroy(g);
     if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
     A->blocks_per_pass = nblk;
@@ -1030,8 +1030,7 @@ void adj_free(ptd_adj* A)
 {
     if (!A) return;
     if (A->s) cudaStreamSynchronize(A->s);
-    for (int q = 0; q < 2; ++q)
-        if (A->graph[q]) cudaGraphExecDestroy(A->graph[q]);
+    if (A->graph) cudaGraphExecDestroy(A->graph);
     if (A->gphase) cudaGraphExecDestroy(A->gphase);
     if (A->fwd) ptd_destroy(A->fwd);
     void* ptrs[] = {A->ck, A->Ht, A->Ed, A->E, A->Hk, A->lam[0], A->lam[1], A->gbuf, A->gm, A->gh, A->stage,
@@ -1292,7 +1291,7 @@ extern "C" int ptd_adj_gradient(ptd_adj* A, double* grad_m, double* grad_H0, int
         ACK(cudaGetLastError());
         A->launches += 3;
         // the whole solve: one graph launch, ended on the device
-        ACK(cudaGraphLaunch(A->graph[0], A->s));
+        ACK(cudaGraphLaunch(A->graph, A->s));
         ACK(cudaMemcpyAsync(A->h_st, A->st, sizeof(AdjState), cudaMemcpyDeviceToHost, A->s));
         ACK(cudaStreamSynchronize(A->s));
         A->launches += (long long)A->h_st->blocks * (A->nchk + 1);

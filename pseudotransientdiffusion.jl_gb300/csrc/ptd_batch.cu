@@ -674,7 +674,7 @@ struct ptd_batch {
     int nchk = 10;
     int tb = 1;        // FP32_DC, FP32_RB: FP32 iterations per launch (2: temporal blocking)
     int stall = 10;
-    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    cudaGraphExec_t g = nullptr;   // FP64 / DF64: one step; FP32_DC: one round of inner solves
     int kernels_per_graph = 0;
     long long launches = 0, iterations = 0;
 };
@@ -882,10 +882,8 @@ int capture(ptd_batch* b)
     // judge; two blocks when the launch count is odd, so that every pass starts
     // on buffer parity 0) and the loop judge, which ends the loop once no
     // instance is running.
-    for (int q = 0; q < 2; ++q) {
-        if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
-        b->g[q] = nullptr;
-    }
+    if (b->g) cudaGraphExecDestroy(b->g);
+    b->g = nullptr;
     cudaGraph_t g = nullptr;
     BCK(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle loop;
@@ -938,7 +936,7 @@ int capture(ptd_batch* b)
         cudaGraphDestroy(g);
         return cuda_fail(err != cudaSuccess ? err : e2, "batch capture");
     }
-    cudaError_t e3 = cudaGraphInstantiate(&b->g[0], g, 0);
+    cudaError_t e3 = cudaGraphInstantiate(&b->g, g, 0);
     cudaGraphDestroy(g);
     if (e3 != cudaSuccess) return cuda_fail(e3, "cudaGraphInstantiate");
     b->kernels_per_graph = nk;   // per pass
@@ -1218,8 +1216,7 @@ void free_batch(ptd_batch* b)
 {
     if (!b) return;
     if (b->s) cudaStreamSynchronize(b->s);
-    for (int q = 0; q < 2; ++q)
-        if (b->g[q]) cudaGraphExecDestroy(b->g[q]);
+    if (b->g) cudaGraphExecDestroy(b->g);
     if (b->gstep) cudaGraphExecDestroy(b->gstep);
     void* rbp[] = {b->wb64[0], b->wb64[1], b->tb32[0], b->tb32[1], b->Rb32, b->Cb32, b->rdev,
                    b->rbtab[0], b->rbtab[1], b->ftab, b->btab, b->passes, b->wfirst, b->wcount,
@@ -1507,7 +1504,7 @@ static int batch_pt_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
     b->launches += 1;
     // the whole step: one graph launch, ended on the device
     BCK(cudaMemsetAsync(b->passes, 0, sizeof(int), b->s));
-    if (b->nchk <= b->bp.itmax) BCK(cudaGraphLaunch(b->g[0], b->s));
+    if (b->nchk <= b->bp.itmax) BCK(cudaGraphLaunch(b->g, b->s));
     BCK(cudaMemcpyAsync(b->h_passes, b->passes, sizeof(int), cudaMemcpyDeviceToHost, b->s));
     {
         const int rc = batch_read_states(b);
@@ -1577,7 +1574,7 @@ static int batch_dc_step(ptd_batch* b, int32_t* iters, double* err_last, int* na
             b->launches += 1;
             // the inner solves: one graph launch, ended on the device
             BCK(cudaMemsetAsync(b->passes, 0, sizeof(int), b->s));
-            BCK(cudaGraphLaunch(b->g[0], b->s));
+            BCK(cudaGraphLaunch(b->g, b->s));
             BCK(cudaMemcpyAsync(b->h_passes, b->passes, sizeof(int), cudaMemcpyDeviceToHost, b->s));
             rc = batch_read_states(b);
             if (rc) return rc;
