@@ -604,6 +604,12 @@ struct ptd_batch {
     std::vector<Inst> inst;
     long long total = 0;       // elements of one concatenated field
     cudaStream_t s = nullptr;
+    // host <-> device copies of the instances, spread over four copy
+    // streams (joined to s by events), so that the set-up of the many small
+    // copies overlaps
+    cudaStream_t cs[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[4] = {nullptr, nullptr, nullptr, nullptr};
     LaunchCfg cfg;
     // plain PT (FP64 / DF64)
     void* H[2] = {nullptr, nullptr};
@@ -1233,6 +1239,11 @@ void free_batch(ptd_batch* b)
     for (void* p : ptrs) cudaFree(p);
     if (b->h_st) cudaFreeHost(b->h_st);
     if (b->h_bst) cudaFreeHost(b->h_bst);
+    for (int k = 0; k < 4; ++k) {
+        if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);
+        if (b->cs[k]) cudaStreamDestroy(b->cs[k]);
+    }
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->s) cudaStreamDestroy(b->s);
     delete b;
 }
@@ -1263,18 +1274,37 @@ int setup_packing(ptd_batch* b)
     return PTD_OK;
 }
 
+// The instances' copies between the caller's arrays and the packed buffer,
+// instance i on copy stream i % 4, after the work queued so far on the
+// solver's stream and before the work queued on it next.
+int copy_instances(ptd_batch* b, double* const* dst, const double* const* src, bool to_packed)
+{
+    BCK(cudaEventRecord(b->ev_fork, b->s));
+    for (int k = 0; k < 4; ++k) BCK(cudaStreamWaitEvent(b->cs[k], b->ev_fork, 0));
+    long long poff = 0;
+    for (int i = 0; i < b->ninst; ++i) {
+        const Inst& I = b->inst[i];
+        const size_t n = (size_t)I.nx * I.ny;
+        if (to_packed)
+            BCK(cudaMemcpyAsync(b->packed + poff, src[i], n * sizeof(double), cudaMemcpyDefault, b->cs[i % 4]));
+        else
+            BCK(cudaMemcpyAsync(dst[i], b->packed + poff, n * sizeof(double), cudaMemcpyDefault, b->cs[i % 4]));
+        poff += (long long)n;
+    }
+    for (int k = 0; k < 4; ++k) {
+        BCK(cudaEventRecord(b->ev_join[k], b->cs[k]));
+        BCK(cudaStreamWaitEvent(b->s, b->ev_join[k], 0));
+    }
+    return PTD_OK;
+}
+
 // Upload instance fields: src[i] (nx_i*ny_i doubles, host or device) into
 // the concatenated padded field dst (FP64): one contiguous copy per instance
 // into the packed buffer, then one conversion kernel.
 int upload(ptd_batch* b, double* dst, const double* const* src)
 {
-    long long poff = 0;
-    for (int i = 0; i < b->ninst; ++i) {
-        const Inst& I = b->inst[i];
-        const size_t n = (size_t)I.nx * I.ny;
-        BCK(cudaMemcpyAsync(b->packed + poff, src[i], n * sizeof(double), cudaMemcpyDefault, b->s));
-        poff += (long long)n;
-    }
+    const int rc = copy_instances(b, nullptr, src, true);
+    if (rc) return rc;
     unpack_batch_kernel<<<b->npwork, 256, 0, b->s>>>(b->packed, dst, b->pinst, b->pwork);
     BCK(cudaGetLastError());
     return PTD_OK;
@@ -1284,14 +1314,7 @@ int download(ptd_batch* b, double* const* dst, const double* src)
 {
     pack_batch_kernel<<<b->npwork, 256, 0, b->s>>>(src, b->packed, b->pinst, b->pwork);
     BCK(cudaGetLastError());
-    long long poff = 0;
-    for (int i = 0; i < b->ninst; ++i) {
-        const Inst& I = b->inst[i];
-        const size_t n = (size_t)I.nx * I.ny;
-        BCK(cudaMemcpyAsync(dst[i], b->packed + poff, n * sizeof(double), cudaMemcpyDefault, b->s));
-        poff += (long long)n;
-    }
-    return PTD_OK;
+    return copy_instances(b, dst, nullptr, false);
 }
 
 }  // namespace
@@ -1377,6 +1400,11 @@ extern "C" int ptd_batch_create(ptd_batch** out, const ptd_batch_params* p, cons
     // FP32_RB: a phase is the check blocks of ~200 iterations between two rebases
     b->blocks_per_phase = std::max(1, (200 + b->nchk - 1) / b->nchk);
     cudaError_t e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+        e = cudaStreamCreateWithFlags(&b->cs[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         free_batch(b);
         return cuda_fail(e, "cudaStreamCreateWithFlags");
